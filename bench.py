@@ -1,0 +1,390 @@
+"""Benchmark of the hot path: batched point evaluation of a quantics tree
+tensor network (60-vertex balanced binary tree, 3 variables x 20 bits,
+chi = 128, Gaussian tensors of unit Frobenius norm, 10^7 points in [0,1)^3).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--points P]
+                    [--precision mixed|f32|f64] [--impl ours|reference]
+
+Prints one JSON line.  `value` is points/s over all ranks with inputs already
+in device memory; `e2e` is the same through the public C-ABI call with host
+buffers (host->device and device->host copies inside the timed region).
+Under torchrun every rank evaluates its own share of points (weak scaling:
+the per-GPU point count is fixed), no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "itensornumericalanalysis.jl_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "MPO-apply+truncate/s & point evals/s, mixed vs FP64 plain, rel.err<=1e-8"
+WORKLOAD = "batched_evaluate: binary tree 60 vertices, 3 vars x 20 bits, chi=128, fp32 tensors"
+N_VERT, CHI, NDIM = 60, 128, 3
+
+
+# ------------------------------------------------------------- workload --
+def config3_tensors(seed: int = 1):
+    """Tensors of the 60-vertex heap-ordered binary tree in the device layout
+    [site, parent, children...], Gaussian, unit Frobenius norm, float32."""
+    import itensornumericalanalysis as ina
+
+    g = ina.named_binary_tree(N_VERT)
+    s = ina.continuous_siteinds(g, map_dimension=NDIM)
+    lay = s.layout
+    rng = np.random.default_rng(seed)
+    ts = {}
+    for i, v in enumerate(lay.order):
+        shape = (2, CHI if lay.parent[i] >= 0 else 1) + (CHI,) * len(lay.children[i])
+        t = rng.standard_normal(shape, dtype=np.float32)
+        ts[v] = t / np.linalg.norm(t)
+    return s, ts
+
+
+def config3_points(n: int, seed: int = 1, offset: int = 0) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    if offset:
+        rng.random((offset, NDIM))  # advance to this rank's share
+    return rng.random((n, NDIM))
+
+
+def oracle_net(s, ts):
+    """The same network in the oracle's labelled-tensor form."""
+    import oracle as O
+
+    so = O.siteinds(O.binary_tree_graph(N_VERT), map_dimension=NDIM)
+    link = {frozenset(e): O.Index(CHI, "L") for e in so.edges}
+    net = O.Net(so, {}, link)
+    lay = s.layout
+    for i, v in enumerate(lay.order):
+        nb = lay.neighbours_in_layout_order(i)
+        arr = ts[v].astype(np.float64)
+        if lay.parent[i] < 0:
+            arr = arr[:, 0]
+        inds = so.site[v] + [link[frozenset((v, lay.order[j]))] for j in nb]
+        net.T[v] = O.Tensor(arr, inds)
+    return net
+
+
+def _oracle_worker(args):
+    seed, pts = args
+    import itensornumericalanalysis.indexmap  # noqa: F401  (host layout only)
+    import oracle as O
+
+    s, ts = config3_tensors(seed)
+    net = oracle_net(s, ts)
+    t0 = time.perf_counter()
+    vals = [O.evaluate(net, list(p), [1, 2, 3]) for p in pts]
+    return time.perf_counter() - t0, vals
+
+
+def cpu_baseline(n_points: int, cores: int, seed: int = 1):
+    """The oracle (a port of the reference's per-point evaluate) on host cores."""
+    import multiprocessing as mp
+
+    pts = config3_points(n_points, seed)
+    chunks = [pts[i::cores] for i in range(cores)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_oracle_worker, [(seed, c) for c in chunks if len(c)])
+    wall = time.perf_counter() - t0
+    busy = max(r[0] for r in res)
+    vals = np.empty(n_points)
+    for i, (_, v) in enumerate(res):
+        vals[i::cores] = v
+    return n_points / busy, wall, pts, vals
+
+
+# ----------------------------------------------------------------- clocks --
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, flag in zip(names, parts[4:8]):
+                if flag.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- main --
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+            "fallback": True}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if _cuda() else "gloo")
+    return ws, rank, local
+
+
+def _cuda() -> bool:
+    import torch
+
+    return torch.cuda.is_available()
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if _cuda() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n = args.cpu_points
+    times = []
+    for _ in range(args.warmup):
+        cpu_baseline(max(cores, n // 4), cores)
+    for _ in range(args.steps):
+        rate, wall, _, _ = cpu_baseline(n, cores)
+        times.append(n / rate)
+    rate = n / float(np.mean(times))
+    sample = f"{n} points of the workload per step, oracle port, {cores} processes"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "points/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "points_per_step": n},
+        "cpu_baseline": {"value": rate, "unit": "points/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": rate, "unit": "points/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--points", type=int, default=10_000_000)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "f32", "f64"])
+    ap.add_argument("--f64-points", type=int, default=1 << 15)
+    ap.add_argument("--cpu-points", type=int, default=96)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+
+    import itensornumericalanalysis as ina
+    from itensornumericalanalysis import _build, _lib
+
+    if not _build.LIB_PATH.exists():
+        _build.build()
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    ctx = _lib.Context(local, stream.cuda_stream)
+    ina.set_default_context(ctx)
+
+    s, ts = config3_tensors(1)
+    f32net = ina.ITensorNetworkFunction.from_tensors(s, ts, ctx=ctx, dtype=_lib.F32)
+    f64net = f32net.astype(_lib.F64)
+    P = args.points
+    Xh = config3_points(P, 1, offset=rank * P)
+    Xd = torch.from_numpy(Xh).cuda()
+    out = torch.empty(2 * P, dtype=torch.float32, device="cuda")
+    dims = (ctypes.c_int32 * 3)(1, 2, 3)
+    prec = {"mixed": _lib.PREC_MIXED, "f32": _lib.PREC_F32, "f64": _lib.PREC_F64}[args.precision]
+    net = f64net if args.precision == "f64" else f32net
+
+    def step_device(n=P, x=Xd, o=out, which=net, pr=prec):
+        ctx.call("tnfa_evaluate", which.handle, x.data_ptr(), n, 3, dims, _lib.MEM_DEVICE,
+                 o.data_ptr(), _lib.OUT_F32_SCALED, _lib.MEM_DEVICE, pr)
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    ctx.kernel_stats(reset=True)
+    ctx.set_timing(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_device()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop()
+    ctx.set_timing(False)
+    t_dev = e0.elapsed_time(e1) / 1e3 / args.steps
+    t_dev = max_over_ranks(t_dev, ws)
+    stats = ctx.kernel_stats(reset=True)
+    value = ws * P / t_dev
+
+    # dominant kernel: live CUDA-event time and algorithmic flops
+    fam = max(stats, key=lambda k: stats[k]["ms"]) if stats else None
+    peaks = measured_peaks()
+    roof = None
+    if fam:
+        st = stats[fam]
+        tc = fam == "contract_tc"
+        achieved = st["flops"] / (st["ms"] / 1e3) / 1e12
+        peak = peaks["bf16_tflops"]
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None, "kernel": fam,
+                "kernel_share": st["ms"] / sum(v["ms"] for v in stats.values()),
+                "peak_source": "MEASURED_PEAKS.json bf16 burst" if "fallback" not in peaks
+                else "fallback", "split_passes_not_counted": 3 if tc else 1}
+    launches = sum(v["launches"] for v in stats.values()) // args.steps
+
+    # end to end: pinned host X -> device -> result back, through the C ABI
+    Xpin = torch.from_numpy(Xh).pin_memory()
+    outpin = torch.empty(2 * P, dtype=torch.float32).pin_memory()
+    def step_e2e():
+        ctx.call("tnfa_evaluate", net.handle, Xpin.data_ptr(), P, 3, dims, _lib.MEM_HOST,
+                 outpin.data_ptr(), _lib.OUT_F32_SCALED, _lib.MEM_HOST, prec)
+    step_e2e()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, ws)
+
+    # accuracy against the FP64 plain path, and the FP64 plain rate
+    nf = min(args.f64_points, P)
+    o64 = torch.empty(nf, dtype=torch.float64, device="cuda")
+    def step_f64():
+        ctx.call("tnfa_evaluate", f64net.handle, Xd.data_ptr(), nf, 3, dims, _lib.MEM_DEVICE,
+                 o64.data_ptr(), _lib.OUT_F64, _lib.MEM_DEVICE, _lib.PREC_F64)
+    step_f64()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    step_f64()
+    torch.cuda.synchronize()
+    f64_rate = nf / (time.perf_counter() - t0)
+    ref64 = o64.cpu().numpy()
+    o = out.cpu().numpy()
+    got = np.ldexp(o[:nf].astype(np.float64), o[P:P + nf].view(np.int32))
+    rel = np.abs(got - ref64) / np.abs(ref64)
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"mixed": "bf16", "f32": "f32", "f64": "f64"}[args.precision],
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "points_per_gpu": P, "vertices": N_VERT, "chi": CHI,
+                   "precision": args.precision, "output": "f32 mantissa + i32 exponent",
+                   "l2": "inputs larger than L2 (X 240 MB/rank at 1e7 points, tensors 470 MB)"},
+        "roofline": roof,
+        "e2e": {"value": ws * P / t_e2e, "unit": "points/s", "h2d_bytes_per_step": P * 3 * 8,
+                "d2h_bytes_per_step": P * 8},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "fp64_plain": {"value": f64_rate, "unit": "points/s", "sample_points": nf,
+                       "speedup_of_value": value / ws / f64_rate},
+        "rel_err_vs_fp64": {"median": float(np.median(rel)), "max": float(np.max(rel)),
+                            "points": nf},
+        "kernels": {k: {"launches_per_step": v["launches"] // args.steps,
+                        "ms_per_step": v["ms"] / args.steps} for k, v in stats.items()},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        rate, wall, pts, vals = cpu_baseline(args.cpu_points, cores)
+        # the oracle's values against the device FP64 path on the same points
+        chk = f64net.evaluate_batch(pts, [1, 2, 3], precision="f64")
+        result["cpu_baseline"] = {
+            "value": rate, "unit": "points/s", "cores": cores, "kind": "port",
+            "sample": f"{args.cpu_points} points, oracle per-point evaluate, {cores} processes",
+            "rel_err_device_f64_vs_oracle": float(np.max(np.abs(chk - vals) / np.abs(vals))),
+        }
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,269 @@
+/*
+ * tnfa.h -- flat C ABI of libtnfa, the GB300 (sm_103a) engine for quantics
+ * tree tensor network functions.
+ *
+ * A "network" (tnfa_net) is a tree -- or a forest -- of dense tensors held in
+ * device memory.  Each vertex carries zero or more site legs (one per quantics
+ * digit; an operator carries out/in pairs fused into one leg of dim base^2),
+ * one bond to its parent (dimension 1 for a root) and one bond per child.
+ *
+ * Canonical tensor layout (host <-> device): per vertex a row-major array with
+ * axes [site legs in declaration order..., parent bond, child bonds in
+ * ascending vertex order]; vertices concatenated in vertex order.  Vertices are
+ * topologically ordered: parent[v] < v, parent[root] = -1.
+ *
+ * Every entry point returns a tnfa_status.  No exception crosses the ABI.  The
+ * caller owns every host buffer; the library owns tnfa_ctx / tnfa_net objects
+ * and frees them in the matching *_destroy call.  Calls on one context are
+ * ordered on that context's stream; a context must be used by one host thread
+ * at a time.
+ *
+ * Each declaration names the reference function it replaces (paths are within
+ * the ITensorNumericalAnalysis.jl project).
+ */
+#ifndef TNFA_H
+#define TNFA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+typedef enum {
+  TNFA_OK = 0,
+  TNFA_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad enum, size mismatch        */
+  TNFA_ERR_CUDA = 2,             /* a CUDA runtime call failed                    */
+  TNFA_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed                      */
+  TNFA_ERR_TOPOLOGY = 4,         /* parent[] not a topologically ordered forest   */
+  TNFA_ERR_SHAPE = 5,            /* bond / site dimensions of operands disagree   */
+  TNFA_ERR_DTYPE = 6,            /* element type not supported by this entry      */
+  TNFA_ERR_NOT_CONVERGED = 7,    /* iterative factorisation / solver hit its cap  */
+  TNFA_ERR_TIMEOUT = 8,          /* a device-side wait ran out of its budget      */
+  TNFA_ERR_DOMAIN = 9,           /* a coordinate is negative or not finite        */
+  TNFA_ERR_UNSUPPORTED = 10      /* valid request this build does not implement   */
+} tnfa_status;
+
+typedef enum { TNFA_F64 = 0, TNFA_F32 = 1, TNFA_C128 = 2 } tnfa_dtype;
+
+typedef enum { TNFA_MEM_HOST = 0, TNFA_MEM_DEVICE = 1 } tnfa_memory;
+
+/* Arithmetic used by tnfa_evaluate. */
+typedef enum {
+  TNFA_PREC_F64 = 0,   /* plain FP64 on the CUDA cores                                */
+  TNFA_PREC_F32 = 1,   /* FP32 on the CUDA cores                                      */
+  TNFA_PREC_MIXED = 2  /* tcgen05 tensor cores, split-BF16 (hi/lo) operands, FP32 acc */
+} tnfa_precision;
+
+/* Leg kinds (tnfa_topology.leg_kind). */
+typedef enum {
+  TNFA_LEG_REAL = 0,     /* digit of the real part of a variable            */
+  TNFA_LEG_IMAG = 1,     /* digit of the imaginary part (complex index map)  */
+  TNFA_LEG_OPERATOR = 2  /* fused (out, in) leg of an operator, dim base^2   */
+} tnfa_leg_kind;
+
+/* Output encodings of tnfa_evaluate. */
+typedef enum {
+  TNFA_OUT_F64 = 0,        /* double per point (real networks)                        */
+  TNFA_OUT_F32 = 1,        /* float per point (may under/overflow)                    */
+  TNFA_OUT_F32_SCALED = 2, /* float mantissa + int32 base-2 exponent per point:
+                              value = out_f32[p] * 2^out_i32[p]; the i32 array follows
+                              the f32 array in the same buffer (8 bytes per point)    */
+  TNFA_OUT_C128 = 3        /* (re, im) double pair per point (complex networks)      */
+} tnfa_out;
+
+typedef struct tnfa_ctx tnfa_ctx;
+typedef struct tnfa_net tnfa_net;
+
+typedef struct {
+  int32_t n_vertices;
+  const int32_t* parent;    /* [n_vertices]  parent vertex, -1 for a root; parent[v] < v   */
+  const int32_t* link_dim;  /* [n_vertices]  dim of bond (v, parent[v]); must be 1 at roots */
+  const int32_t* n_legs;    /* [n_vertices]  number of site legs at v (may be 0)            */
+  const int32_t* leg_dim;   /* [sum n_legs]  leg dimension (base, or base^2 for operators)  */
+  const int32_t* leg_var;   /* [sum n_legs]  1-based continuous variable of the leg         */
+  const int32_t* leg_digit; /* [sum n_legs]  1-based digit, 1 = most significant            */
+  const int32_t* leg_kind;  /* [sum n_legs]  tnfa_leg_kind                                  */
+} tnfa_topology;
+
+typedef struct {
+  double cutoff;     /* relative discarded weight: sum(dropped s^2)/sum(s^2) <= cutoff */
+  int32_t maxdim;    /* 0 = unbounded                                                  */
+  int32_t mindim;    /* >= 1                                                           */
+  int32_t normalize; /* nonzero: rescale the result to unit 2-norm                     */
+  int32_t precision; /* tnfa_precision of the contractions                             */
+} tnfa_trunc_params;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Bind to `device` and order all work on `stream` (a cudaStream_t; NULL = the
+ * library creates its own stream). */
+int tnfa_ctx_create(int device, void* stream, tnfa_ctx** out);
+int tnfa_ctx_destroy(tnfa_ctx* ctx);
+int tnfa_ctx_synchronize(tnfa_ctx* ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char* tnfa_last_error_string(const tnfa_ctx* ctx);
+/* Library version string, e.g. "tnfa 0.1.0 sm_103a". */
+const char* tnfa_version(void);
+
+/* Kernel accounting (no reference counterpart; used by benchmarks).  Every
+ * kernel launch is counted per family ("contract_tc", "contract_simt",
+ * "digitize", ...) together with its algorithmic flops and bytes; with timing
+ * enabled each launch is also bracketed by CUDA events on the context stream.
+ * tnfa_ctx_kernel_stats synchronises the stream and returns up to `max`
+ * families: names (32 bytes each, NUL-terminated), launches, summed duration
+ * in ms (0 when timing was off), flops and bytes.  reset != 0 clears the
+ * counters afterwards. */
+int tnfa_ctx_set_timing(tnfa_ctx* ctx, int enable);
+int tnfa_ctx_kernel_stats(tnfa_ctx* ctx, int32_t max, char* names, int64_t* launches, double* ms,
+                          double* flops, double* bytes, int32_t* n_families, int reset);
+
+/* ---- networks ----------------------------------------------------------- */
+
+/* Build a network from the canonical layout.  Replaces the construction of an
+ * ITensorNetworkFunction (src/itensornetworkfunction.jl:18-22) paired with its
+ * IndsNetworkMap (src/indsnetworkmap.jl:9-13, src/IndexMaps/realindexmap.jl:6-9,
+ * src/IndexMaps/complexindexmap.jl:6-10).  `tensors` is n_elements scalars of
+ * `dtype` in host or device memory. */
+int tnfa_net_create(tnfa_ctx* ctx, const tnfa_topology* topo, int dtype, const void* tensors,
+                    int memory, tnfa_net** out);
+int tnfa_net_destroy(tnfa_net* net);
+/* Shape query: n_vertices, dtype, total element count; link_dim_out (may be
+ * NULL) receives the current bond dimensions (they change under truncation). */
+int tnfa_net_info(const tnfa_net* net, int32_t* n_vertices, int32_t* dtype, int64_t* n_elements,
+                  int32_t* link_dim_out);
+/* Copy the tensors back in canonical layout (n_elements scalars). */
+int tnfa_net_download(tnfa_ctx* ctx, const tnfa_net* net, void* tensors, int memory);
+/* Deep copy (src/itensornetworkfunction.jl:33-35 Base.copy). */
+int tnfa_net_copy(tnfa_ctx* ctx, const tnfa_net* net, tnfa_net** out);
+/* Multiply the tensor of `vertex` by the scalar (re, im); im must be 0 for
+ * real networks.  Used by the constructors' `c` factors
+ * (src/elementary_functions.jl:50,98,102) and scalar * function. */
+int tnfa_net_scale(tnfa_ctx* ctx, tnfa_net* net, int32_t vertex, double re, double im);
+
+/* ---- evaluation (hot path) ---------------------------------------------- */
+
+/* Batched point evaluation f(x_p), p < n_points.  Replaces evaluate
+ * (src/itensornetworkfunction.jl:96-112), i.e. calculate_ind_values
+ * (src/IndexMaps/realindexmap.jl:67-76, src/IndexMaps/abstractindexmap.jl:121-138;
+ * complex maps src/IndexMaps/complexindexmap.jl:116-132), project
+ * (src/itensornetworkfunction.jl:84-94) and the tree contraction scalar(tn; alg="bp").
+ * X: n_points x n_cols row-major doubles, column j holding variable dims[j]
+ * (1-based); for networks with TNFA_LEG_IMAG legs n_cols = 2*n_dims with
+ * (re, im) per variable.  Every variable that has a leg must be listed.
+ * out: per `out_kind` (tnfa_out).  A negative / non-finite coordinate gives
+ * TNFA_ERR_DOMAIN (the reference's digit loop never terminates for those). */
+int tnfa_evaluate(tnfa_ctx* ctx, const tnfa_net* net, const double* X, int64_t n_points,
+                  int32_t n_dims, const int32_t* dims, int x_memory, void* out, int out_kind,
+                  int out_memory, int precision);
+
+/* ---- integration -------------------------------------------------------- */
+
+/* Left Riemann sum over [0,1)^n: contract every site leg with the uniform
+ * vector 1/base (1 when take_sum != 0) and contract the tree.  Replaces
+ * integrate(f) (src/integration.jl:6-17).  out: 1 double (real) or 2 (complex),
+ * host memory. */
+int tnfa_integrate(tnfa_ctx* ctx, const tnfa_net* net, int take_sum, double* out);
+
+/* <sum| O |f>: integral of O*f.  Replaces integrate(op, f) (src/integration.jl:20-32). */
+int tnfa_integrate_operator(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* net, int take_sum,
+                            double* out);
+
+/* Contract the site legs of variables vars[0..n_vars) with the uniform
+ * vector (1/base, or 1 when take_sum) and absorb vertices left without legs
+ * into a neighbour.  Replaces partial_integrate (src/integration.jl:35-54) with
+ * merge_internal_tensors (src/utils.jl:99-113).  The result has fewer
+ * vertices; query it with tnfa_net_info / tnfa_net_topology. */
+int tnfa_partial_integrate(tnfa_ctx* ctx, const tnfa_net* net, int32_t n_vars, const int32_t* vars,
+                           int take_sum, tnfa_net** out);
+/* Topology of a network (arrays sized by tnfa_net_info's n_vertices and the
+ * leg count returned in *n_legs_total). Any pointer may be NULL. */
+int tnfa_net_topology(const tnfa_net* net, int32_t* parent, int32_t* link_dim, int32_t* n_legs,
+                      int32_t* leg_dim, int32_t* leg_var, int32_t* leg_digit, int32_t* leg_kind,
+                      int32_t* n_legs_total);
+
+/* ---- network algebra ---------------------------------------------------- */
+
+/* Direct sum: f + g (bond dims add).  Replaces ITensorNetworks' add used by
+ * `+` (src/elementary_functions.jl:67,82,99,119,134; semantics as
+ * src/fixes.jl:39-91).  Same topology and legs required. */
+int tnfa_add(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, tnfa_net** out);
+/* Pointwise product f * g (bond dims multiply).  Replaces multiply
+ * (src/elementary_operators.jl:260-292). */
+int tnfa_multiply(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, tnfa_net** out);
+/* diag(f) as an operator network (legs base^2).  Replaces operator_proj
+ * (src/elementary_operators.jl:247-258). */
+int tnfa_operator_proj(tnfa_ctx* ctx, const tnfa_net* f, tnfa_net** out);
+/* Forest union: g's vertices appended after f's (the product of two
+ * functions of disjoint vertex sets).  Replaces the disjoint-vertex branch of
+ * multiply (src/elementary_operators.jl:263-270). */
+int tnfa_net_concat(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, tnfa_net** out);
+/* Element-type conversion: F64 <-> F32, F64 -> C128, F32 -> C128. */
+int tnfa_net_convert(tnfa_ctx* ctx, const tnfa_net* f, int dtype, tnfa_net** out);
+
+/* ---- operator application and truncation -------------------------------- */
+
+/* y = O f, contracted exactly site by site then truncated with `params`.
+ * Replaces operate (src/elementary_operators.jl:294-319), which calls
+ * ITensorNetworks.contract(O, f; alg="fit", cutoff, maxdim, normalize). */
+int tnfa_apply(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f,
+               const tnfa_trunc_params* params, tnfa_net** out);
+/* Batched form: n independent (op[i], f[i]) pairs of uneven shapes in one
+ * scheduled pass. */
+int tnfa_apply_batched(tnfa_ctx* ctx, int32_t n, const tnfa_net* const* ops,
+                       const tnfa_net* const* fs, const tnfa_trunc_params* params,
+                       tnfa_net** outs);
+/* QR-orthogonalise toward the root(s), then SVD-truncate every bond with
+ * `params`.  Replaces truncate (src/itensornetworkfunction.jl:114-118). */
+int tnfa_truncate(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_trunc_params* params,
+                  tnfa_net** out);
+/* Same for n networks at once. */
+int tnfa_truncate_batched(tnfa_ctx* ctx, int32_t n, const tnfa_net* const* fs,
+                          const tnfa_trunc_params* params, tnfa_net** outs);
+/* Inner product <f|g> (conjugating f) and 2-norm.  out: 1 or 2 doubles. */
+int tnfa_inner(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, double* out);
+
+/* ---- linear solve -------------------------------------------------------- */
+
+typedef struct {
+  int32_t nsweeps;      /* maximum number of sweeps                               */
+  int32_t maxdim;       /* bond cap of the solution                               */
+  double cutoff;        /* truncation of the two-site updates                     */
+  double tol;           /* stop when ||A x - b|| / ||b|| <= tol                   */
+  int32_t krylov_dim;   /* local solver iterations per two-site update           */
+  int32_t precision;    /* tnfa_precision of the local contractions               */
+  double a0, a1;        /* solve (a0 + a1*A) x = b                                */
+} tnfa_linsolve_params;
+
+/* Solve (a0 + a1 A) x = b by two-site alternating sweeps with a local
+ * Krylov solver; x0 seeds the sweep.  Replaces ITensorNetworks.linsolve as
+ * named for the Laplace solve (examples/2d_laplace_solver.jl:33-34 uses the
+ * same sweep machinery through dmrg).  rel_residual receives the final
+ * ||(a0 + a1 A) x - b|| / ||b|| computed exactly in FP64. */
+int tnfa_linsolve(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnfa_net* x0,
+                  const tnfa_linsolve_params* params, tnfa_net** x, double* rel_residual);
+
+/* ---- differentiation ----------------------------------------------------- */
+
+/* Vector-Jacobian product of batched evaluation: dtensors += sum_p dout[p] *
+ * d f(x_p) / d tensors, canonical layout, real networks, FP64 or FP32 per
+ * the network dtype.  No reference counterpart (the reference has no AD);
+ * it backs the rrule of evaluate. */
+int tnfa_evaluate_vjp(tnfa_ctx* ctx, const tnfa_net* net, const double* X, int64_t n_points,
+                      int32_t n_dims, const int32_t* dims, int x_memory, const double* dout,
+                      int dout_memory, void* dtensors, int dtensors_memory);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TNFA_H */

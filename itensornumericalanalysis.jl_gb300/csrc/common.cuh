@@ -1,0 +1,236 @@
+// Shared internals of libtnfa: error plumbing, context / network objects,
+// scalar types and small device helpers.  Nothing here is part of the ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/tnfa.h"
+
+namespace tnfa {
+
+// ---------------------------------------------------------------- errors --
+// Internal code throws tnfa::Error; every extern "C" entry point catches it
+// (TNFA_API_BEGIN/END) and turns it into a status plus a context message.
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+[[noreturn]] inline void fail(int status, const std::string& msg) { throw Error(status, msg); }
+
+inline void check_cuda(cudaError_t e, const char* what, const char* file, int line) {
+  if (e != cudaSuccess) {
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    fail(e == cudaErrorMemoryAllocation ? TNFA_ERR_OUT_OF_MEMORY : TNFA_ERR_CUDA, buf);
+  }
+}
+#define TNFA_CUDA(call) ::tnfa::check_cuda((call), #call, __FILE__, __LINE__)
+#define TNFA_CHECK(cond, status, msg)  \
+  do {                                  \
+    if (!(cond)) ::tnfa::fail((status), (msg)); \
+  } while (0)
+#define TNFA_LAUNCH_CHECK() TNFA_CUDA(cudaGetLastError())
+
+// ---------------------------------------------------------------- scalars --
+struct cplx {
+  double re, im;
+};
+__host__ __device__ inline cplx operator+(cplx a, cplx b) { return {a.re + b.re, a.im + b.im}; }
+__host__ __device__ inline cplx operator-(cplx a, cplx b) { return {a.re - b.re, a.im - b.im}; }
+__host__ __device__ inline cplx operator*(cplx a, cplx b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+__host__ __device__ inline cplx& operator+=(cplx& a, cplx b) {
+  a.re += b.re;
+  a.im += b.im;
+  return a;
+}
+
+template <class T> struct Sc;
+template <> struct Sc<double> {
+  __host__ __device__ static double zero() { return 0.0; }
+  __host__ __device__ static double one() { return 1.0; }
+  __device__ static double absmax(double x) { return fabs(x); }
+  __device__ static double scale2(double x, int e) { return scalbn(x, e); }
+  __device__ static double fma(double a, double b, double c) { return ::fma(a, b, c); }
+  __host__ __device__ static double conj(double x) { return x; }
+};
+template <> struct Sc<float> {
+  __host__ __device__ static float zero() { return 0.0f; }
+  __host__ __device__ static float one() { return 1.0f; }
+  __device__ static float absmax(float x) { return fabsf(x); }
+  __device__ static float scale2(float x, int e) { return scalbnf(x, e); }
+  __device__ static float fma(float a, float b, float c) { return fmaf(a, b, c); }
+  __host__ __device__ static float conj(float x) { return x; }
+};
+template <> struct Sc<cplx> {
+  __host__ __device__ static cplx zero() { return {0.0, 0.0}; }
+  __host__ __device__ static cplx one() { return {1.0, 0.0}; }
+  __device__ static double absmax(cplx z) { return fmax(fabs(z.re), fabs(z.im)); }
+  __device__ static cplx scale2(cplx z, int e) { return {scalbn(z.re, e), scalbn(z.im, e)}; }
+  __device__ static cplx fma(cplx a, cplx b, cplx c) {
+    return {::fma(a.re, b.re, ::fma(-a.im, b.im, c.re)), ::fma(a.re, b.im, ::fma(a.im, b.re, c.im))};
+  }
+  __host__ __device__ static cplx conj(cplx z) { return {z.re, -z.im}; }
+};
+
+inline size_t dtype_size(int dtype) {
+  switch (dtype) {
+    case TNFA_F64: return 8;
+    case TNFA_F32: return 4;
+    case TNFA_C128: return 16;
+  }
+  fail(TNFA_ERR_DTYPE, "unknown dtype " + std::to_string(dtype));
+}
+
+// ------------------------------------------------------------- objects --
+struct Ctx;
+
+// Host-side description of a forest plus its device tensors.
+struct Topo {
+  int V = 0;
+  std::vector<int> parent, link, nlegs, leg_off;  // leg_off[v]: first leg of v
+  std::vector<int> leg_dim, leg_var, leg_digit, leg_kind;
+  std::vector<std::vector<int>> children;  // ascending
+  std::vector<int> site_dim;               // product of the leg dims of v
+  std::vector<int64_t> off;                // element offset of v's tensor
+  int64_t n_elem = 0;
+
+  int64_t size(int v) const {
+    int64_t s = (int64_t)site_dim[v] * link[v];
+    for (int c : children[v]) s *= link[c];
+    return s;
+  }
+  void finalize();  // children, site_dim, off, n_elem from the arrays above
+  void validate() const;
+  std::vector<int> roots() const {
+    std::vector<int> r;
+    for (int v = 0; v < V; ++v)
+      if (parent[v] < 0) r.push_back(v);
+    return r;
+  }
+};
+
+}  // namespace tnfa
+
+namespace tnfa {
+// Per-family launch accounting of a context (see tnfa_ctx_kernel_stats).
+struct KernelFamily {
+  std::string name;
+  int64_t launches = 0;
+  double flops = 0, bytes = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;  // unresolved
+  double ms = 0;
+};
+}  // namespace tnfa
+
+struct tnfa_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int sm_count = 0;
+  size_t eval_budget = 0;  // bytes of device scratch an evaluate call may hold
+  std::string last_error;
+  bool timing = false;
+  std::vector<tnfa::KernelFamily> families;
+  std::vector<cudaEvent_t> event_pool;
+};
+
+struct tnfa_net {
+  tnfa_ctx* ctx = nullptr;
+  tnfa::Topo topo;
+  int dtype = TNFA_F64;
+  void* d = nullptr;  // device tensors, canonical layout
+  // Lazily built derived copies (invalidated by any in-place change).
+  mutable void* d_f32 = nullptr;   // FP32 copy of a real network
+  mutable void* d_bhi = nullptr;   // BF16 hi part (tensor-core evaluation)
+  mutable void* d_blo = nullptr;   // BF16 lo part
+  void invalidate_caches() const;
+};
+
+namespace tnfa {
+
+// Device memory from the stream-ordered allocator of the context's stream.
+void* dalloc(tnfa_ctx* ctx, size_t bytes);
+void dfree(tnfa_ctx* ctx, void* p);
+
+// RAII scratch buffer.
+struct DBuf {
+  tnfa_ctx* ctx = nullptr;
+  void* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(tnfa_ctx* c, size_t bytes) : ctx(c), n(bytes) { p = bytes ? dalloc(c, bytes) : nullptr; }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : ctx(o.ctx), p(o.p), n(o.n) { o.p = nullptr; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    reset();
+    ctx = o.ctx;
+    p = o.p;
+    n = o.n;
+    o.p = nullptr;
+    return *this;
+  }
+  ~DBuf() { reset(); }
+  void reset() {
+    if (p) dfree(ctx, p);
+    p = nullptr;
+  }
+  template <class T> T* as() const { return (T*)p; }
+};
+
+tnfa_net* new_net(tnfa_ctx* ctx, const Topo& topo, int dtype);  // allocates d
+void require_net(const tnfa_net* net, const char* what);
+void require_ctx(const tnfa_ctx* ctx);
+
+// Element-type conversions on the device.
+void convert_f64_to_f32(tnfa_ctx* ctx, const double* src, float* dst, int64_t n);
+
+// Launch accounting: construct before a launch, destroy after it.  Counts
+// the launch and its algorithmic work; records CUDA events when timing is on.
+struct KernelScope {
+  tnfa_ctx* ctx;
+  int fam;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  KernelScope(tnfa_ctx* c, const char* family, double flops, double bytes);
+  ~KernelScope();
+};
+
+inline unsigned grid_for(int64_t n, int block, int cap = 1 << 20) {
+  int64_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (unsigned)g;
+}
+
+}  // namespace tnfa
+
+// Entry-point wrappers: map exceptions to statuses, record the message.
+#define TNFA_API_BEGIN(ctxp) \
+  tnfa_ctx* __tnfa_ctx = (ctxp); \
+  try {
+#define TNFA_API_END                                                   \
+  }                                                                    \
+  catch (const tnfa::Error& e) {                                       \
+    if (__tnfa_ctx) __tnfa_ctx->last_error = e.what();                 \
+    return e.status;                                                   \
+  }                                                                    \
+  catch (const std::bad_alloc&) {                                      \
+    if (__tnfa_ctx) __tnfa_ctx->last_error = "host allocation failed"; \
+    return TNFA_ERR_OUT_OF_MEMORY;                                     \
+  }                                                                    \
+  catch (const std::exception& e) {                                    \
+    if (__tnfa_ctx) __tnfa_ctx->last_error = e.what();                 \
+    return TNFA_ERR_INVALID_ARGUMENT;                                  \
+  }                                                                    \
+  if (__tnfa_ctx) __tnfa_ctx->last_error.clear();                      \
+  return TNFA_OK;

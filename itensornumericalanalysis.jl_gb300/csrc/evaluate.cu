@@ -1,0 +1,772 @@
+// Batched point evaluation of a tree tensor network function.
+//
+// Reference path (ITensorNumericalAnalysis.jl): evaluate
+// (src/itensornetworkfunction.jl:96-112) = calculate_ind_values (digits by
+// greedy subtraction, src/IndexMaps/abstractindexmap.jl:121-138) -> project
+// (one-hot slice of every site leg, :84-94) -> scalar(tn; alg="bp") (exact on
+// a tree).  It handles one point per call.
+//
+// Here all points of a chunk go through the tree vertex by vertex (children
+// before parents):
+//   1. k_digitize: coordinates -> site value s_v(p) of every vertex (u8).
+//   2. per vertex: group the points by s_v (count / scan / scatter), so that a
+//      tile of points shares one slice T_v[s].
+//   3. per vertex: out[p, a] = sum_k A[p, k] T_v[s][a][k] with A the row-wise
+//      Kronecker product of the children's messages.  Leaves are never
+//      materialised: a parent reads the leaf slice T_leaf[s_leaf(p)] directly.
+//      Each message row is rescaled by a power of two when it is read (exact)
+//      and the exponent is carried per point, so deep trees neither underflow
+//      nor overflow.
+//   4. k_combine: product over the roots of the forest, times 2^exponent.
+#include <algorithm>
+#include <type_traits>
+
+#include "evaluate.cuh"
+
+namespace tnfa {
+
+// ----------------------------------------------------------- digitize ----
+struct DigitEntry {
+  int col;     // column of X
+  int base;
+  int vertex;
+  int stride;  // weight of this leg inside the vertex's site value
+  double invb; // base^-digit, correctly rounded
+  int start;   // first digit of a (variable, part): reload the remainder
+};
+
+__global__ void k_digitize(const double* __restrict__ X, int ncols, int Pc,
+                           const DigitEntry* __restrict__ prog, int nprog, uint8_t* __restrict__ S,
+                           int64_t ldS, int* __restrict__ err) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < Pc; p += gridDim.x * blockDim.x) {
+    double xr = 0.0;
+    for (int e = 0; e < nprog; ++e) {
+      DigitEntry d = prog[e];
+      if (d.start) {
+        xr = X[(int64_t)p * ncols + d.col];
+        if (!(xr >= 0.0) || !isfinite(xr)) {
+          atomicOr(err, 1);
+          xr = 0.0;
+        }
+      }
+      // Largest digit value v with xr >= v * base^-digit; subtract it.
+      int dig = 0;
+      for (int v = d.base - 1; v >= 1; --v) {
+        double t = (double)v * d.invb;
+        if (xr >= t) {
+          dig = v;
+          xr -= t;
+          break;
+        }
+      }
+      uint8_t* sp = S + (int64_t)d.vertex * ldS + p;
+      *sp = (uint8_t)(*sp + dig * d.stride);
+    }
+  }
+}
+
+// ----------------------------------------------------------- grouping ----
+__global__ void k_group_count(const uint8_t* __restrict__ S, int Pc, int ng, int* __restrict__ cnt) {
+  __shared__ int h[256];
+  for (int i = threadIdx.x; i < ng; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < Pc; p += gridDim.x * blockDim.x)
+    atomicAdd(&h[S[p]], 1);
+  __syncthreads();
+  for (int i = threadIdx.x; i < ng; i += blockDim.x)
+    if (h[i]) atomicAdd(&cnt[i], h[i]);
+}
+
+// Single thread: offsets, tile starts and scatter cursors from the counts.
+__global__ void k_group_scan(int* meta, int ng, int tp) {
+  int* off = meta;
+  int* cnt = meta + ng;
+  int* ts = meta + 2 * ng;
+  int* cur = meta + 3 * ng + 1;
+  int o = 0, t = 0;
+  for (int g = 0; g < ng; ++g) {
+    off[g] = o;
+    cur[g] = o;
+    ts[g] = t;
+    o += cnt[g];
+    t += (cnt[g] + tp - 1) / tp;
+  }
+  ts[ng] = t;
+}
+
+// Identity grouping (vertex without site legs).
+__global__ void k_group_identity(int* meta, int Pc, int tp) {
+  meta[0] = 0;
+  meta[1] = Pc;
+  meta[2] = 0;
+  meta[3] = (Pc + tp - 1) / tp;
+  meta[4] = 0;
+}
+
+constexpr int SCATTER_ITEMS = 8;
+__global__ void k_group_scatter(const uint8_t* __restrict__ S, int Pc, int ng, int* __restrict__ cur,
+                                int* __restrict__ perm) {
+  __shared__ int h[256];
+  __shared__ int base[256];
+  for (int i = threadIdx.x; i < ng; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  int p0 = blockIdx.x * blockDim.x * SCATTER_ITEMS;
+  int loc[SCATTER_ITEMS];
+  int grp[SCATTER_ITEMS];
+#pragma unroll
+  for (int i = 0; i < SCATTER_ITEMS; ++i) {
+    int p = p0 + i * blockDim.x + threadIdx.x;
+    grp[i] = -1;
+    if (p < Pc) {
+      grp[i] = S[p];
+      loc[i] = atomicAdd(&h[grp[i]], 1);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < ng; i += blockDim.x) base[i] = h[i] ? atomicAdd(&cur[i], h[i]) : 0;
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < SCATTER_ITEMS; ++i) {
+    int p = p0 + i * blockDim.x + threadIdx.x;
+    if (grp[i] >= 0) perm[base[grp[i]] + loc[i]] = p;
+  }
+}
+
+// ------------------------------------------------------- contraction ----
+template <class T>
+__device__ inline bool locate_tile(const VertexJob<T>& j, int tp, int b, int& row0, int& nrows,
+                                   int& g) {
+  int ng = j.ngroups;
+  if (b >= j.tile_start[ng]) return false;
+  int gg = 0;
+  while (gg + 1 < ng && j.tile_start[gg + 1] <= b) ++gg;
+  g = gg;
+  row0 = j.grp_off[gg] + (b - j.tile_start[gg]) * tp;
+  nrows = min(tp, j.grp_off[gg] + j.grp_cnt[gg] - row0);
+  return nrows > 0;
+}
+
+template <class T> struct Frexp;
+template <> struct Frexp<double> {
+  __device__ static int e(double m) {
+    int ex = 0;
+    frexp(m, &ex);
+    return ex;
+  }
+};
+template <> struct Frexp<float> {
+  __device__ static int e(float m) {
+    int ex = 0;
+    frexpf(m, &ex);
+    return ex;
+  }
+};
+
+// Load the message rows of every child for the tile's points into shared
+// memory (child c at rows + choff_c * tp, row-major tp x dim_c), rescale each
+// row by 2^-e so that its largest entry lies in [0.5, 1), and accumulate the
+// exponents of the tile's points into eacc.
+template <class T>
+__device__ void load_children(const VertexJob<T>& j, const int* pts, int nrows, int tp, T* rows,
+                              int* eacc) {
+  int off = 0;
+  for (int c = 0; c < j.nchild; ++c) {
+    const ChildSrc<T> s = j.ch[c];
+    T* dst = rows + (int64_t)off * tp;
+    for (int idx = threadIdx.x; idx < tp * s.dim; idx += blockDim.x) {
+      int r = idx / s.dim, i = idx - r * s.dim;
+      T v = Sc<T>::zero();
+      if (r < nrows) {
+        int p = pts[r];
+        v = s.S ? s.ptr[(int64_t)s.S[p] * s.dim + i] : s.ptr[(int64_t)p * s.dim + i];
+      }
+      dst[idx] = v;
+    }
+    off += s.dim;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  off = 0;
+  for (int c = 0; c < j.nchild; ++c) {
+    const ChildSrc<T> s = j.ch[c];
+    T* base = rows + (int64_t)off * tp;
+    for (int r = warp; r < nrows; r += nw) {
+      T* row = base + (int64_t)r * s.dim;
+      decltype(Sc<T>::absmax(Sc<T>::zero())) m = 0;
+      for (int i = lane; i < s.dim; i += 32) m = max(m, Sc<T>::absmax(row[i]));
+      for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+      int ex = (m > 0) ? Frexp<decltype(m)>::e(m) : 0;
+      if (ex != 0)
+        for (int i = lane; i < s.dim; i += 32) row[i] = Sc<T>::scale2(row[i], -ex);
+      if (lane == 0) atomicAdd(&eacc[r], ex + (s.exps ? s.exps[pts[r]] : 0));
+    }
+    off += s.dim;
+  }
+  __syncthreads();
+}
+
+// A[r, k] for the tile: product of the children's row entries.
+template <class T>
+__device__ inline T kr_entry(const VertexJob<T>& j, const T* rows, int tp, int r, int k) {
+  T a = Sc<T>::one();
+  int off_end = 0;
+  for (int c = 0; c < j.nchild; ++c) off_end += j.ch[c].dim;
+  int off = off_end;
+  for (int c = j.nchild - 1; c >= 0; --c) {
+    int d = j.ch[c].dim;
+    off -= d;
+    int kc = k % d;
+    k /= d;
+    a = a * rows[(int64_t)off * tp + (int64_t)r * d + kc];
+  }
+  return a;
+}
+
+// General SIMT contraction: CTA tile = TP points x 128 output columns,
+// 256 threads, register micro-tile (TP/8) x 4, K streamed in chunks of 16.
+template <class T, int TP>
+__global__ void __launch_bounds__(256) k_contract_gemm(const VertexJob<T> j) {
+  constexpr int TA = 128, KC = 16, RM = TP / 8;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int row0, nrows, g;
+  if (!locate_tile(j, TP, blockIdx.x, row0, nrows, g)) return;
+  const int a0 = blockIdx.y * TA;
+  int sumdim = 0;
+  for (int c = 0; c < j.nchild; ++c) sumdim += j.ch[c].dim;
+  T* rows = (T*)smem_raw;
+  T* As = rows + (int64_t)sumdim * TP;  // [KC][TP]
+  T* Bs = As + KC * TP;                 // [KC][TA]
+  int* pts = (int*)(Bs + KC * TA);
+  int* eacc = pts + TP;
+  for (int r = threadIdx.x; r < TP; r += blockDim.x) {
+    pts[r] = r < nrows ? (j.perm ? j.perm[row0 + r] : row0 + r) : 0;
+    eacc[r] = 0;
+  }
+  __syncthreads();
+  load_children(j, pts, nrows, TP, rows, eacc);
+
+  const T* Bg = j.B + (int64_t)g * j.chi_a * j.K;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  T acc[RM][4];
+#pragma unroll
+  for (int i = 0; i < RM; ++i)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[i][q] = Sc<T>::zero();
+
+  for (int k0 = 0; k0 < j.K; k0 += KC) {
+    for (int idx = threadIdx.x; idx < KC * TP; idx += blockDim.x) {
+      int kk = idx / TP, r = idx - kk * TP;
+      int k = k0 + kk;
+      As[idx] = (k < j.K && r < nrows) ? kr_entry(j, rows, TP, r, k) : Sc<T>::zero();
+    }
+    for (int idx = threadIdx.x; idx < KC * TA; idx += blockDim.x) {
+      int a = idx / KC, kk = idx - a * KC;
+      int k = k0 + kk, aa = a0 + a;
+      Bs[kk * TA + a] = (k < j.K && aa < j.chi_a) ? Bg[(int64_t)aa * j.K + k] : Sc<T>::zero();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < KC; ++kk) {
+      T av[RM], bv[4];
+#pragma unroll
+      for (int i = 0; i < RM; ++i) av[i] = As[kk * TP + ty * RM + i];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) bv[q] = Bs[kk * TA + tx + 32 * q];
+#pragma unroll
+      for (int i = 0; i < RM; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[i][q] = Sc<T>::fma(av[i], bv[q], acc[i][q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < RM; ++i) {
+    int r = ty * RM + i;
+    if (r >= nrows) continue;
+    int p = pts[r];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int a = a0 + tx + 32 * q;
+      if (a < j.chi_a) j.out[(int64_t)p * j.chi_a + a] = acc[i][q];
+    }
+  }
+  if (blockIdx.y == 0)
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) j.out_exp[pts[r]] = eacc[r];
+}
+
+// Narrow outputs (chi_a <= 16): one warp per point, lanes split K, shuffle
+// reduction.  Used at the roots (chi_a = 1) and on thin bonds.
+template <class T>
+__global__ void __launch_bounds__(256) k_contract_narrow(const VertexJob<T> j) {
+  constexpr int TP = 8, NA = 16;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int row0, nrows, g;
+  if (!locate_tile(j, TP, blockIdx.x, row0, nrows, g)) return;
+  int sumdim = 0;
+  for (int c = 0; c < j.nchild; ++c) sumdim += j.ch[c].dim;
+  T* rows = (T*)smem_raw;
+  int* pts = (int*)(rows + (int64_t)sumdim * TP);
+  int* eacc = pts + TP;
+  for (int r = threadIdx.x; r < TP; r += blockDim.x) {
+    pts[r] = r < nrows ? (j.perm ? j.perm[row0 + r] : row0 + r) : 0;
+    eacc[r] = 0;
+  }
+  __syncthreads();
+  load_children(j, pts, nrows, TP, rows, eacc);
+  const int lane = threadIdx.x & 31, r = threadIdx.x >> 5;
+  if (r >= nrows) return;
+  const T* Bg = j.B + (int64_t)g * j.chi_a * j.K;
+  T acc[NA];
+#pragma unroll
+  for (int q = 0; q < NA; ++q) acc[q] = Sc<T>::zero();
+  for (int k = lane; k < j.K; k += 32) {
+    T a = kr_entry(j, rows, TP, r, k);
+#pragma unroll
+    for (int q = 0; q < NA; ++q)
+      if (q < j.chi_a) acc[q] = Sc<T>::fma(a, Bg[(int64_t)q * j.K + k], acc[q]);
+  }
+  int p = pts[r];
+#pragma unroll
+  for (int q = 0; q < NA; ++q) {
+    if (q >= j.chi_a) break;
+    T v = acc[q];
+    for (int o = 16; o; o >>= 1) {
+      if constexpr (sizeof(T) == 16) {
+        cplx z = *(cplx*)&v;
+        z.re += __shfl_xor_sync(0xffffffffu, z.re, o);
+        z.im += __shfl_xor_sync(0xffffffffu, z.im, o);
+        v = *(T*)&z;
+      } else {
+        v = v + __shfl_xor_sync(0xffffffffu, v, o);
+      }
+    }
+    if (lane == 0) j.out[(int64_t)p * j.chi_a + q] = v;
+  }
+  if (lane == 0) j.out_exp[p] = eacc[r];
+}
+
+// ------------------------------------------------------------ combine ----
+template <class T>
+__device__ inline void write_out(void* out, int kind, int64_t p, int64_t P, T v, int e);
+template <>
+__device__ inline void write_out<double>(void* out, int kind, int64_t p, int64_t P, double v, int e) {
+  if (kind == TNFA_OUT_F64) {
+    ((double*)out)[p] = scalbn(v, e);
+  } else if (kind == TNFA_OUT_F32) {
+    ((float*)out)[p] = (float)scalbn(v, e);
+  } else {  // scaled f32
+    int ex = 0;
+    double m = frexp(v, &ex);
+    ((float*)out)[p] = (float)m;
+    ((int*)((float*)out + P))[p] = (v == 0.0) ? 0 : e + ex;
+  }
+}
+template <>
+__device__ inline void write_out<float>(void* out, int kind, int64_t p, int64_t P, float v, int e) {
+  write_out<double>(out, kind, p, P, (double)v, e);
+}
+template <>
+__device__ inline void write_out<cplx>(void* out, int kind, int64_t p, int64_t P, cplx v, int e) {
+  ((cplx*)out)[p] = cplx{scalbn(v.re, e), scalbn(v.im, e)};
+}
+
+template <class T>
+__global__ void k_combine(const T* __restrict__ rootv, const int* __restrict__ roote, int nroots,
+                          int Pc, void* out, int kind, int64_t P, int64_t p0) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < Pc; p += gridDim.x * blockDim.x) {
+    T v = Sc<T>::one();
+    int e = 0;
+    for (int r = 0; r < nroots; ++r) {
+      v = v * rootv[(int64_t)r * Pc + p];
+      e += roote[(int64_t)r * Pc + p];
+    }
+    write_out<T>(out, kind, p0 + p, P, v, e);
+  }
+}
+
+// -------------------------------------------------------------- driver ----
+struct EvalPlan {
+  std::vector<int> order;        // vertices computed, children before parents
+  std::vector<char> fused_leaf;  // non-root leaf read directly by its parent
+  std::vector<int> slot;         // message slot of a computed non-root vertex
+  int nslots = 0;
+  std::vector<int> roots;
+  int chimax = 1;
+};
+
+static EvalPlan make_plan(const Topo& T) {
+  EvalPlan P;
+  P.fused_leaf.assign(T.V, 0);
+  P.slot.assign(T.V, -1);
+  P.roots = T.roots();
+  for (int v = 0; v < T.V; ++v)
+    if (T.parent[v] >= 0 && T.children[v].empty()) P.fused_leaf[v] = 1;
+  // Post-order DFS per root keeps the number of live messages near the depth.
+  for (int r : P.roots) {
+    std::vector<std::pair<int, int>> st{{r, 0}};
+    while (!st.empty()) {
+      auto& [v, i] = st.back();
+      if (i < (int)T.children[v].size()) {
+        int c = T.children[v][i++];
+        st.push_back({c, 0});
+      } else {
+        if (!P.fused_leaf[v]) P.order.push_back(v);
+        st.pop_back();
+      }
+    }
+  }
+  std::vector<int> free_slots;
+  int n = 0;
+  for (int v : P.order) {
+    for (int c : T.children[v])
+      if (!P.fused_leaf[c]) free_slots.push_back(P.slot[c]);
+    if (T.parent[v] >= 0) {
+      if (free_slots.empty()) free_slots.push_back(n++);
+      P.slot[v] = free_slots.back();
+      free_slots.pop_back();
+      P.chimax = std::max(P.chimax, T.link[v]);
+    }
+  }
+  P.nslots = n;
+  return P;
+}
+
+template <class T> struct FamilyName;
+template <> struct FamilyName<double> { static constexpr const char* v = "contract_f64"; };
+template <> struct FamilyName<float> { static constexpr const char* v = "contract_f32"; };
+template <> struct FamilyName<cplx> { static constexpr const char* v = "contract_c128"; };
+
+template <class T>
+static void launch_contract(tnfa_ctx* ctx, const VertexJob<T>& j, int Pc) {
+  int sumdim = 0;
+  for (int c = 0; c < j.nchild; ++c) sumdim += j.ch[c].dim;
+  KernelScope ks(ctx, FamilyName<T>::v, 2.0 * Pc * (double)j.K * j.chi_a,
+                 (double)sizeof(T) * ((double)Pc * (sumdim + j.chi_a) +
+                                      (double)j.site_dim * j.chi_a * j.K));
+  if (j.chi_a <= 16) {
+    constexpr int TP = 8;
+    size_t sm = (size_t)sumdim * TP * sizeof(T) + 2 * TP * sizeof(int);
+    TNFA_CHECK(sm <= 200 * 1024, TNFA_ERR_UNSUPPORTED, "children bonds too large for evaluation");
+    if (sm > 48 * 1024)
+      TNFA_CUDA(cudaFuncSetAttribute(k_contract_narrow<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sm));
+    unsigned gx = (unsigned)((Pc + TP - 1) / TP + j.ngroups);
+    k_contract_narrow<T><<<gx, 256, sm, ctx->stream>>>(j);
+  } else {
+    constexpr int TA = 128, KC = 16;
+    size_t row_bytes = (size_t)sumdim * sizeof(T);
+    unsigned gy = (unsigned)((j.chi_a + TA - 1) / TA);
+    if (row_bytes * 32 + (size_t)KC * (32 + TA) * sizeof(T) <= 160 * 1024) {
+      constexpr int TP = 32;
+      size_t sm = row_bytes * TP + (size_t)KC * (TP + TA) * sizeof(T) + 2 * TP * sizeof(int);
+      if (sm > 48 * 1024)
+        TNFA_CUDA(cudaFuncSetAttribute(k_contract_gemm<T, TP>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      dim3 grid((unsigned)((Pc + TP - 1) / TP + j.ngroups), gy);
+      k_contract_gemm<T, TP><<<grid, 256, sm, ctx->stream>>>(j);
+    } else {
+      constexpr int TP = 8;
+      size_t sm = row_bytes * TP + (size_t)KC * (TP + TA) * sizeof(T) + 2 * TP * sizeof(int);
+      TNFA_CHECK(sm <= 200 * 1024, TNFA_ERR_UNSUPPORTED, "children bonds too large for evaluation");
+      if (sm > 48 * 1024)
+        TNFA_CUDA(cudaFuncSetAttribute(k_contract_gemm<T, TP>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      dim3 grid((unsigned)((Pc + TP - 1) / TP + j.ngroups), gy);
+      k_contract_gemm<T, TP><<<grid, 256, sm, ctx->stream>>>(j);
+    }
+  }
+  TNFA_LAUNCH_CHECK();
+}
+
+static int contract_tile_rows(int chi_a, int sumdim, size_t tsize) {
+  if (chi_a <= 16) return 8;
+  size_t row_bytes = (size_t)sumdim * tsize;
+  return (row_bytes * 32 + (size_t)16 * (32 + 128) * tsize <= 160 * 1024) ? 32 : 8;
+}
+
+template <class T>
+static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, const double* X,
+                          int64_t P, int ncols, const std::vector<DigitEntry>& prog, int xmem,
+                          void* out, int out_kind, int out_mem, bool use_tc) {
+  const Topo& Tp = net->topo;
+  const int V = Tp.V;
+  EvalPlan plan = make_plan(Tp);
+  const int nroots = (int)plan.roots.size();
+  size_t out_elem = out_kind == TNFA_OUT_F64 ? 8 : out_kind == TNFA_OUT_F32 ? 4
+                    : out_kind == TNFA_OUT_F32_SCALED ? 8 : 16;
+  size_t per_point = (size_t)plan.nslots * (plan.chimax * sizeof(T) + sizeof(int)) + V + 4 +
+                     (xmem == TNFA_MEM_HOST ? ncols * 8 : 0) + nroots * (sizeof(T) + 4) +
+                     (out_mem == TNFA_MEM_HOST ? out_elem : 0);
+  int64_t Pc_max = (int64_t)(ctx->eval_budget / per_point);
+  Pc_max = std::max<int64_t>(256, std::min<int64_t>(Pc_max, int64_t(1) << 30));
+  Pc_max = (Pc_max / 256) * 256;
+  const int64_t Pc_alloc = std::min<int64_t>(P, Pc_max);
+  const int Pcap = (int)std::max<int64_t>(Pc_alloc, 1);
+
+  DBuf dprog(ctx, prog.size() * sizeof(DigitEntry));
+  if (!prog.empty())
+    TNFA_CUDA(cudaMemcpyAsync(dprog.p, prog.data(), prog.size() * sizeof(DigitEntry),
+                              cudaMemcpyHostToDevice, ctx->stream));
+  DBuf dS(ctx, (size_t)V * Pcap);
+  DBuf dperm(ctx, (size_t)Pcap * 4);
+  int maxsd = 1;
+  for (int v = 0; v < V; ++v) maxsd = std::max(maxsd, Tp.site_dim[v]);
+  DBuf dmeta(ctx, group_meta_ints(maxsd) * 4);
+  DBuf derr(ctx, 4);
+  TNFA_CUDA(cudaMemsetAsync(derr.p, 0, 4, ctx->stream));
+  const size_t slot_vals = (size_t)Pcap * plan.chimax;
+  DBuf dslots(ctx, (size_t)plan.nslots * slot_vals * sizeof(T));
+  DBuf dslote(ctx, (size_t)plan.nslots * Pcap * sizeof(int));
+  DBuf droot(ctx, (size_t)nroots * Pcap * sizeof(T));
+  DBuf droote(ctx, (size_t)nroots * Pcap * sizeof(int));
+  DBuf dX(ctx, xmem == TNFA_MEM_HOST ? (size_t)Pcap * ncols * 8 : 0);
+  DBuf dout(ctx, out_mem == TNFA_MEM_HOST ? (size_t)Pcap * out_elem : 0);
+  std::vector<int> root_index(V, -1);
+  for (int r = 0; r < nroots; ++r) root_index[plan.roots[r]] = r;
+
+  for (int64_t p0 = 0; p0 < P; p0 += Pcap) {
+    const int Pc = (int)std::min<int64_t>(Pcap, P - p0);
+    const double* Xc;
+    if (xmem == TNFA_MEM_HOST) {
+      TNFA_CUDA(cudaMemcpyAsync(dX.p, X + p0 * ncols, (size_t)Pc * ncols * 8,
+                                cudaMemcpyHostToDevice, ctx->stream));
+      Xc = dX.as<double>();
+    } else {
+      Xc = X + p0 * ncols;
+    }
+    TNFA_CUDA(cudaMemsetAsync(dS.p, 0, (size_t)V * Pcap, ctx->stream));
+    if (!prog.empty()) {
+      KernelScope ks(ctx, "digitize", 0.0, (double)Pc * (ncols * 8.0 + V));
+      k_digitize<<<grid_for(Pc, 256, 8 * 152 * 8), 256, 0, ctx->stream>>>(
+          Xc, ncols, Pc, dprog.as<DigitEntry>(), (int)prog.size(), dS.as<uint8_t>(), (int64_t)Pcap,
+          derr.as<int>());
+      TNFA_LAUNCH_CHECK();
+    }
+    for (int v : plan.order) {
+      VertexJob<T> j{};
+      j.nchild = (int)Tp.children[v].size();
+      TNFA_CHECK(j.nchild <= EVAL_MAXC, TNFA_ERR_UNSUPPORTED,
+                 "vertex degree above " + std::to_string(EVAL_MAXC) + " children");
+      int64_t K = 1;
+      int sumdim = 0;
+      int cdims[EVAL_MAXC];
+      for (int i = 0; i < j.nchild; ++i) {
+        int c = Tp.children[v][i];
+        ChildSrc<T>& s = j.ch[i];
+        s.dim = Tp.link[c];
+        cdims[i] = s.dim;
+        sumdim += s.dim;
+        K *= s.dim;
+        if (plan.fused_leaf[c]) {
+          s.ptr = tensors + Tp.off[c];
+          s.exps = nullptr;
+          s.S = dS.as<uint8_t>() + (int64_t)c * Pcap;
+        } else {
+          s.ptr = (const T*)dslots.p + (size_t)plan.slot[c] * slot_vals;
+          s.exps = dslote.as<int>() + (size_t)plan.slot[c] * Pcap;
+          s.S = nullptr;
+        }
+      }
+      TNFA_CHECK(K < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "contraction too large");
+      j.K = (int)K;
+      j.chi_a = Tp.link[v];
+      j.site_dim = Tp.site_dim[v];
+      j.B = tensors + Tp.off[v];
+      j.Pc = Pc;
+      if (Tp.parent[v] < 0) {
+        j.out = (T*)droot.p + (size_t)root_index[v] * Pcap;
+        j.out_exp = droote.as<int>() + (size_t)root_index[v] * Pcap;
+      } else {
+        j.out = (T*)dslots.p + (size_t)plan.slot[v] * slot_vals;
+        j.out_exp = dslote.as<int>() + (size_t)plan.slot[v] * Pcap;
+      }
+      const bool tc = use_tc && j.site_dim <= 256 && tc_vertex_eligible(j.nchild, cdims, j.chi_a);
+      const int tp = tc ? tc_tile_rows() : contract_tile_rows(j.chi_a, sumdim, sizeof(T));
+      const int ng = j.site_dim;
+      int* meta = dmeta.as<int>();
+      j.ngroups = ng;
+      j.grp_off = meta;
+      j.grp_cnt = meta + ng;
+      j.tile_start = meta + 2 * ng;
+      if (ng == 1) {
+        KernelScope ks(ctx, "group", 0.0, 0.0);
+        k_group_identity<<<1, 1, 0, ctx->stream>>>(meta, Pc, tp);
+        TNFA_LAUNCH_CHECK();
+        j.perm = nullptr;
+      } else {
+        TNFA_CHECK(ng <= 256, TNFA_ERR_UNSUPPORTED, "site dimension above 256 per vertex");
+        const uint8_t* Sv = dS.as<uint8_t>() + (int64_t)v * Pcap;
+        TNFA_CUDA(cudaMemsetAsync(meta + ng, 0, ng * sizeof(int), ctx->stream));
+        KernelScope ks(ctx, "group", 0.0, (double)Pc * 6.0);
+        k_group_count<<<grid_for(Pc, 256, 4 * 152), 256, 0, ctx->stream>>>(Sv, Pc, ng, meta + ng);
+        k_group_scan<<<1, 1, 0, ctx->stream>>>(meta, ng, tp);
+        unsigned gs = (unsigned)((Pc + 256 * SCATTER_ITEMS - 1) / (256 * SCATTER_ITEMS));
+        k_group_scatter<<<gs, 256, 0, ctx->stream>>>(Sv, Pc, ng, meta + 3 * ng + 1, dperm.as<int>());
+        TNFA_LAUNCH_CHECK();
+        j.perm = dperm.as<int>();
+      }
+      if constexpr (std::is_same<T, float>::value) {
+        if (tc) {
+          tc_contract_vertex(ctx, net, v, j, tp);
+          continue;
+        }
+      }
+      launch_contract<T>(ctx, j, Pc);
+    }
+    void* o = out_mem == TNFA_MEM_HOST ? dout.p : out;
+    int64_t Pout = out_mem == TNFA_MEM_HOST ? Pc : P;
+    int64_t pofs = out_mem == TNFA_MEM_HOST ? 0 : p0;
+    KernelScope ksc(ctx, "combine", 0.0, (double)Pc * nroots * (sizeof(T) + 4.0));
+    k_combine<T><<<grid_for(Pc, 256, 8192), 256, 0, ctx->stream>>>(
+        (const T*)droot.p, droote.as<int>(), nroots, Pc, o, out_kind, Pout, pofs);
+    TNFA_LAUNCH_CHECK();
+    if (out_mem == TNFA_MEM_HOST) {
+      if (out_kind == TNFA_OUT_F32_SCALED) {
+        TNFA_CUDA(cudaMemcpyAsync((float*)out + p0, dout.p, (size_t)Pc * 4, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+        TNFA_CUDA(cudaMemcpyAsync((int*)((float*)out + P) + p0, (float*)dout.p + Pc, (size_t)Pc * 4,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+      } else {
+        TNFA_CUDA(cudaMemcpyAsync((char*)out + p0 * out_elem, dout.p, (size_t)Pc * out_elem,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+      }
+    }
+  }
+  int herr = 0;
+  TNFA_CUDA(cudaMemcpyAsync(&herr, derr.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  TNFA_CHECK(herr == 0, TNFA_ERR_DOMAIN,
+             "a coordinate is negative or not finite (the digit map needs x >= 0)");
+}
+
+// Digit program of a network for the given variable list.
+static std::vector<DigitEntry> make_digit_program(const Topo& T, int n_dims, const int32_t* dims,
+                                                  int* ncols_out) {
+  bool has_imag = false;
+  int L = T.leg_off[T.V];
+  for (int l = 0; l < L; ++l) {
+    TNFA_CHECK(T.leg_kind[l] != TNFA_LEG_OPERATOR, TNFA_ERR_INVALID_ARGUMENT,
+               "evaluate needs a function network, got an operator");
+    if (T.leg_kind[l] == TNFA_LEG_IMAG) has_imag = true;
+  }
+  const int ncols = has_imag ? 2 * n_dims : n_dims;
+  *ncols_out = ncols;
+  struct LegRef {
+    int var, kind, digit, leg, vertex, stride;
+  };
+  std::vector<LegRef> refs;
+  for (int v = 0; v < T.V; ++v) {
+    int stride = 1;
+    for (int l = T.leg_off[v + 1] - 1; l >= T.leg_off[v]; --l) {
+      refs.push_back({T.leg_var[l], T.leg_kind[l], T.leg_digit[l], l, v, stride});
+      stride *= T.leg_dim[l];
+    }
+  }
+  std::sort(refs.begin(), refs.end(), [](const LegRef& a, const LegRef& b) {
+    if (a.var != b.var) return a.var < b.var;
+    if (a.kind != b.kind) return a.kind < b.kind;
+    return a.digit < b.digit;
+  });
+  std::vector<DigitEntry> prog;
+  for (size_t i = 0; i < refs.size(); ++i) {
+    const LegRef& r = refs[i];
+    bool start = (i == 0 || refs[i - 1].var != r.var || refs[i - 1].kind != r.kind);
+    int expect = start ? 1 : refs[i - 1].digit + 1;
+    TNFA_CHECK(r.digit == expect, TNFA_ERR_TOPOLOGY,
+               "digits of variable " + std::to_string(r.var) +
+                   " are not 1..L (missing or repeated digit " + std::to_string(expect) + ")");
+    int col = -1;
+    for (int j = 0; j < n_dims; ++j)
+      if (dims[j] == r.var) col = j;
+    TNFA_CHECK(col >= 0, TNFA_ERR_INVALID_ARGUMENT,
+               "variable " + std::to_string(r.var) + " has digits but is not listed in dims");
+    int base = T.leg_dim[r.leg];
+    TNFA_CHECK(base >= 2 && base <= 255, TNFA_ERR_UNSUPPORTED, "digit base outside 2..255");
+    double bk = 1.0;
+    for (int k = 0; k < r.digit; ++k) bk *= base;
+    TNFA_CHECK(bk < 9007199254740992.0, TNFA_ERR_UNSUPPORTED, "base^digit above 2^53");
+    DigitEntry d;
+    d.col = has_imag ? 2 * col + (r.kind == TNFA_LEG_IMAG ? 1 : 0) : col;
+    d.base = base;
+    d.vertex = r.vertex;
+    d.stride = r.stride;
+    d.invb = 1.0 / bk;
+    d.start = start ? 1 : 0;
+    prog.push_back(d);
+  }
+  return prog;
+}
+
+void contract_scalar(tnfa_ctx* ctx, const tnfa_net* net, double* out_host) {
+  for (int v = 0; v < net->topo.V; ++v)
+    TNFA_CHECK(net->topo.site_dim[v] == 1, TNFA_ERR_INVALID_ARGUMENT,
+               "contract_scalar needs a network without site legs");
+  double dummy = 0.0;
+  std::vector<DigitEntry> prog;
+  if (net->dtype == TNFA_C128)
+    evaluate_impl<cplx>(ctx, net, (const cplx*)net->d, &dummy, 1, 0, prog, TNFA_MEM_HOST, out_host,
+                        TNFA_OUT_C128, TNFA_MEM_HOST, false);
+  else if (net->dtype == TNFA_F64)
+    evaluate_impl<double>(ctx, net, (const double*)net->d, &dummy, 1, 0, prog, TNFA_MEM_HOST,
+                          out_host, TNFA_OUT_F64, TNFA_MEM_HOST, false);
+  else
+    evaluate_impl<float>(ctx, net, (const float*)net->d, &dummy, 1, 0, prog, TNFA_MEM_HOST,
+                         out_host, TNFA_OUT_F64, TNFA_MEM_HOST, false);
+}
+
+}  // namespace tnfa
+
+using namespace tnfa;
+
+extern "C" int tnfa_evaluate(tnfa_ctx* ctx, const tnfa_net* net, const double* X, int64_t n_points,
+                             int32_t n_dims, const int32_t* dims, int x_memory, void* out,
+                             int out_kind, int out_memory, int precision) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(net, "evaluate");
+  TNFA_CHECK(n_points >= 0, TNFA_ERR_INVALID_ARGUMENT, "n_points < 0");
+  if (n_points == 0) return TNFA_OK;
+  TNFA_CHECK(X && out && (n_dims == 0 || dims), TNFA_ERR_INVALID_ARGUMENT, "null X, out or dims");
+  TNFA_CHECK(n_dims >= 0 && n_dims <= 64, TNFA_ERR_INVALID_ARGUMENT, "n_dims out of range");
+  TNFA_CHECK(x_memory == TNFA_MEM_HOST || x_memory == TNFA_MEM_DEVICE, TNFA_ERR_INVALID_ARGUMENT,
+             "bad x_memory");
+  TNFA_CHECK(out_memory == TNFA_MEM_HOST || out_memory == TNFA_MEM_DEVICE,
+             TNFA_ERR_INVALID_ARGUMENT, "bad out_memory");
+  for (int v = 0; v < net->topo.V; ++v)
+    TNFA_CHECK(net->topo.site_dim[v] <= 256, TNFA_ERR_UNSUPPORTED, "site dimension above 256");
+  int ncols = 0;
+  std::vector<DigitEntry> prog = make_digit_program(net->topo, n_dims, dims, &ncols);
+  if (net->dtype == TNFA_C128) {
+    TNFA_CHECK(out_kind == TNFA_OUT_C128, TNFA_ERR_DTYPE, "complex networks need TNFA_OUT_C128");
+    TNFA_CHECK(precision == TNFA_PREC_F64, TNFA_ERR_UNSUPPORTED,
+               "complex networks evaluate in TNFA_PREC_F64 only");
+    evaluate_impl<cplx>(ctx, net, (const cplx*)net->d, X, n_points, ncols, prog, x_memory, out,
+                        out_kind, out_memory, false);
+  } else {
+    TNFA_CHECK(out_kind == TNFA_OUT_F64 || out_kind == TNFA_OUT_F32 ||
+                   out_kind == TNFA_OUT_F32_SCALED,
+               TNFA_ERR_DTYPE, "real networks need a real output kind");
+    if (precision == TNFA_PREC_F64) {
+      TNFA_CHECK(net->dtype == TNFA_F64, TNFA_ERR_DTYPE, "TNFA_PREC_F64 needs an FP64 network");
+      evaluate_impl<double>(ctx, net, (const double*)net->d, X, n_points, ncols, prog, x_memory,
+                            out, out_kind, out_memory, false);
+    } else if (precision == TNFA_PREC_F32 || precision == TNFA_PREC_MIXED) {
+      const float* t32;
+      if (net->dtype == TNFA_F32) {
+        t32 = (const float*)net->d;
+      } else {
+        if (!net->d_f32) {
+          net->d_f32 = dalloc(ctx, (size_t)net->topo.n_elem * 4);
+          convert_f64_to_f32(ctx, (const double*)net->d, (float*)net->d_f32, net->topo.n_elem);
+        }
+        t32 = (const float*)net->d_f32;
+      }
+      if (precision == TNFA_PREC_MIXED) tc_prepare_net(ctx, net);
+      evaluate_impl<float>(ctx, net, t32, X, n_points, ncols, prog, x_memory, out, out_kind,
+                           out_memory, precision == TNFA_PREC_MIXED);
+    } else {
+      fail(TNFA_ERR_INVALID_ARGUMENT, "unknown precision");
+    }
+  }
+  TNFA_API_END
+}

@@ -1,0 +1,308 @@
+"""Finite-difference operators, operator application and products.
+
+Mirrors src/elementary_operators.jl.  An operator is a tree network whose
+site legs fuse (out, in) into one leg of dimension base^2 (out = the primed
+index of the reference's ITensors).  Operators are built from the
+reference's OpSums -- sums of products of the digit operators
+D+, D-, Dup, Ddn (src/digit_inds.jl:35-58) -- as a block-diagonal direct sum
+of their terms, then compressed on the device by truncation, which is what
+ITensorNetworks' ttn(OpSum; cutoff) produces up to gauge.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib
+from .indexmap import IndsNetworkMap
+from .network import ITensorNetworkFunction
+
+default_boundary = "Dirichlet"
+
+# Digit operators as matrices M[out, in] (src/digit_inds.jl:35-58: the
+# reference writes ITensor(o, s, s') so o[in, out]).
+_OPS = {
+    "D+": np.array([[0.0, 1.0], [0.0, 0.0]]),
+    "D-": np.array([[0.0, 0.0], [1.0, 0.0]]),
+    "Ddn": np.array([[1.0, 0.0], [0.0, 0.0]]),
+    "Dup": np.array([[0.0, 0.0], [0.0, 1.0]]),
+}
+
+
+def _op_matrix(name: str, base: int) -> np.ndarray:
+    if name == "I":
+        return np.eye(base)
+    if base != 2:
+        raise ValueError("digit shift operators are defined for base 2")
+    return _OPS[name]
+
+
+def operator_legs(s: IndsNetworkMap):
+    """Leg arrays of an operator on s: every digit leg becomes (out, in)."""
+    nlegs, ldim, lvar, ldig, lkind = s.leg_arrays()
+    return nlegs, [d * d for d in ldim], lvar, ldig, [_lib.LEG_OPERATOR] * len(ldim)
+
+
+class ITensorNetworkOperator(ITensorNetworkFunction):
+    """A tree tensor network operator (a TreeTensorNetwork of the reference)."""
+
+    def evaluate_batch(self, *a, **k):
+        raise TypeError("an operator is not a function; apply it with operate()")
+
+    def _wrap(self, handle, s=None, legs="same"):
+        return ITensorNetworkOperator(s or self.s, handle, self._ctx,
+                                      self._legs if legs == "same" else legs)
+
+    def __add__(self, other):
+        if not isinstance(other, ITensorNetworkOperator):
+            return NotImplemented
+        a, b = self._promote(other)
+        h = C.c_void_p()
+        self._ctx.call("tnfa_add", a._h, b._h, C.byref(h))
+        return self._wrap(h)
+
+    def __repr__(self):
+        return f"ITensorNetworkOperator(nv={self.s.nv()}, maxlinkdim={self.maxlinkdim()})"
+
+
+# ------------------------------------------------------------ OpSums ----
+class OpSum:
+    """Sum of products of digit operators; a term maps (dim, digit) -> op name."""
+
+    def __init__(self, terms=None):
+        self.terms: list[tuple[complex, dict]] = list(terms or [])
+
+    def add(self, coef, ops: dict) -> None:
+        self.terms.append((coef, dict(ops)))
+
+    def __add__(self, other: "OpSum") -> "OpSum":
+        return OpSum(self.terms + other.terms)
+
+    def __rmul__(self, c) -> "OpSum":
+        return OpSum([(c * k, ops) for k, ops in self.terms])
+
+    __mul__ = __rmul__
+
+
+def boundary_term(s: IndsNetworkMap, boundary: str, dim: int, isfwd: bool, n: int = 0) -> OpSum:
+    """src/elementary_operators.jl:32-57: Neumann adds Dup.. (fwd) / Ddn.. (bwd)
+    on the top L-n digits, Periodic adds D-.. (fwd) / D+.. (bwd)."""
+    L = s.ndigits(dim)
+    out = OpSum()
+    if boundary == "Neumann":
+        out.add(1.0, {(dim, j): ("Dup" if isfwd else "Ddn") for j in range(1, L - n + 1)})
+    elif boundary == "Periodic":
+        out.add(1.0, {(dim, j): ("D-" if isfwd else "D+") for j in range(1, L - n + 1)})
+    elif boundary != "Dirichlet":
+        raise ValueError(f"unknown boundary {boundary!r}")
+    return out
+
+
+def _shift_opsum(s, dim, boundary, n, up: str, down: str, isfwd: bool) -> OpSum:
+    if not s.is_tree():
+        raise ValueError("shift operators need a tree")
+    if s.base() != 2:
+        raise ValueError("shift operators need base 2")
+    L = s.ndigits(dim)
+    out = OpSum()
+    string = {(dim, L - n): up}
+    out.add(1.0, string)
+    for i in range(L - n, 1, -1):
+        string = dict(string)
+        string[(dim, i)] = down
+        string[(dim, i - 1)] = up
+        out.add(1.0, string)
+    return out + boundary_term(s, boundary, dim, isfwd, n)
+
+
+def forward_shift_opsum(s, dim=1, boundary=default_boundary, n: int = 0):
+    """f(x + (n+1) delta) with carries (src/elementary_operators.jl:59-80)."""
+    return _shift_opsum(s, dim, boundary, n, "D+", "D-", True)
+
+
+def backward_shift_opsum(s, dim=1, boundary=default_boundary, n: int = 0):
+    """f(x - (n+1) delta) with borrows (src/elementary_operators.jl:82-103)."""
+    return _shift_opsum(s, dim, boundary, n, "D-", "D+", False)
+
+
+def no_shift_opsum(s) -> OpSum:
+    """Identity (src/elementary_operators.jl:105-110)."""
+    return OpSum([(1.0, {})])
+
+
+def _site_op(s: IndsNetworkMap, v, ops: dict) -> np.ndarray:
+    """Fused (out, in) site tensor of one OpSum term at vertex v."""
+    t = np.ones(())
+    for l in s.legs[v]:
+        m = _op_matrix(ops.get((l.dim, l.digit), "I"), l.base)
+        t = np.multiply.outer(t, m.reshape(-1))
+    return t
+
+
+def opsum_to_operator(s: IndsNetworkMap, opsum: OpSum, cutoff: float = 1e-15,
+                      scale_dims: dict | None = None, compress: bool = True):
+    """Block-diagonal direct sum of the OpSum's product terms (bond = number of
+    terms), coefficients on the first vertex, then compressed on the device."""
+    lay = s.layout
+    terms = opsum.terms
+    T = len(terms)
+    real = all(np.isreal(c) for c, _ in terms)
+    dtype = float if real else complex
+    ts = {}
+    for i, v in enumerate(lay.order):
+        site = [_site_op(s, v, ops) for _, ops in terms]
+        sshape = site[0].shape
+        nch = len(lay.children[i])
+        root = lay.parent[i] < 0
+        out = np.zeros(sshape + ((1,) if root else (T,)) + (T,) * nch, dtype=dtype)
+        for t, (coef, _) in enumerate(terms):
+            idx = (0 if root else t,) + (t,) * nch
+            # += : a lone root (no bonds at all) sums the terms in place
+            out[(Ellipsis,) + idx] += site[t] * (coef if i == 0 else 1.0)
+        ts[v] = out
+    op = ITensorNetworkOperator.from_tensors(s, ts, legs=operator_legs(s))
+    if scale_dims:
+        for v, f in scale_dims.items():
+            op.scale_vertex(v, f)
+    if compress and T > 1:
+        op = _compress(op, cutoff)
+    return op
+
+
+def _compress(op: ITensorNetworkOperator, cutoff: float) -> ITensorNetworkOperator:
+    try:
+        from .truncation import truncate
+    except ImportError:
+        return op
+    try:
+        return truncate(op, cutoff=cutoff)
+    except _lib.TnfaError as e:
+        if e.status == _lib.ERR_UNSUPPORTED:
+            return op
+        raise
+
+
+def forward_shift_op(s, truncate_kwargs=None, **kw):
+    """src/elementary_operators.jl:117-120."""
+    return opsum_to_operator(s, forward_shift_opsum(s, **kw), **_tk(truncate_kwargs))
+
+
+def backward_shift_op(s, truncate_kwargs=None, **kw):
+    """src/elementary_operators.jl:112-115."""
+    return opsum_to_operator(s, backward_shift_opsum(s, **kw), **_tk(truncate_kwargs))
+
+
+def _tk(truncate_kwargs):
+    tk = dict(truncate_kwargs or {})
+    return {"cutoff": tk.get("cutoff", 1e-15)}
+
+
+def stencil(s: IndsNetworkMap, shifts: Sequence[float], delta_power: int, dim: int = 1,
+            left_boundary=default_boundary, right_boundary=default_boundary, scale: bool = True,
+            cutoff: float = 1e-15, **_ignored):
+    """shifts = [x+2d, x+d, x, x-d, x-2d] weights; scaled by base^power per
+    vertex of `dim` (src/elementary_operators.jl:122-160)."""
+    if len(shifts) != 5:
+        raise ValueError("stencil needs 5 weights")
+    b = s.base()
+    ops = shifts[2] * no_shift_opsum(s)
+    for i in (0, 1):
+        if shifts[i] != 0:
+            ops = ops + shifts[i] * forward_shift_opsum(s, dim, right_boundary, 1 if i == 0 else 0)
+    for i in (3, 4):
+        if shifts[i] != 0:
+            ops = ops + shifts[i] * backward_shift_opsum(s, dim, left_boundary, 1 if i == 4 else 0)
+    scale_dims = {v: float(b) ** delta_power for v in s.dimension_vertices(dim)} if scale else None
+    return opsum_to_operator(s, ops, cutoff=cutoff, scale_dims=scale_dims)
+
+
+def first_derivative_operator(s, **kw):
+    """(f(x+d) - f(x-d)) / 2d (src/elementary_operators.jl:162-164)."""
+    return stencil(s, [0.0, 0.5, 0.0, -0.5, 0.0], 1, **kw)
+
+
+def second_derivative_operator(s, **kw):
+    """(f(x+d) - 2f(x) + f(x-d)) / d^2 (src/elementary_operators.jl:166-168)."""
+    return stencil(s, [0.0, 1.0, -2.0, 1.0, 0.0], 2, **kw)
+
+
+def third_derivative_operator(s, **kw):
+    """src/elementary_operators.jl:170-172."""
+    return stencil(s, [0.5, -1.0, 0.0, 1.0, -0.5], 3, **kw)
+
+
+def fourth_derivative_operator(s, **kw):
+    """src/elementary_operators.jl:174-176."""
+    return stencil(s, [1.0, -4.0, 6.0, -4.0, 1.0], 4, **kw)
+
+
+def laplacian_operator(s, boundary: str | None = None, dims=None, **kw):
+    """Sum of second derivatives over dims (direct sum, not recompressed)
+    (src/elementary_operators.jl:178-189)."""
+    if boundary is not None:
+        kw = dict(kw, left_boundary=boundary, right_boundary=boundary)
+    dims = list(dims) if dims is not None else list(range(1, s.dimension() + 1))
+    op = second_derivative_operator(s, dim=dims[0], **kw)
+    for d in dims[1:]:
+        op = op + second_derivative_operator(s, dim=d, **kw)
+    return op
+
+
+def identity_operator(s) -> ITensorNetworkOperator:
+    """src/elementary_operators.jl:191-194."""
+    return opsum_to_operator(s, no_shift_opsum(s), compress=False)
+
+
+def operator_proj(f: ITensorNetworkFunction) -> ITensorNetworkOperator:
+    """|f> -> diag(f) (src/elementary_operators.jl:247-258)."""
+    h = C.c_void_p()
+    f.ctx.call("tnfa_operator_proj", f.handle, C.byref(h))
+    return ITensorNetworkOperator(f.s, h, f.ctx, operator_legs(f.s))
+
+
+def multiply(g: ITensorNetworkFunction, f: ITensorNetworkFunction, *more) -> ITensorNetworkFunction:
+    """Pointwise product (src/elementary_operators.jl:260-292): bond dims
+    multiply on shared vertices; functions on disjoint vertex sets form a forest."""
+    if more:
+        return multiply(multiply(g, f), *more)
+    if g.s.same_structure(f.s):
+        a, b = g._promote(f)
+        h = C.c_void_p()
+        g.ctx.call("tnfa_multiply", a.handle, b.handle, C.byref(h))
+        return type(g)(g.s, h, g.ctx)
+    if not set(g.s.vertices()) & set(f.s.vertices()):
+        a, b = g._promote(f)
+        h = C.c_void_p()
+        g.ctx.call("tnfa_net_concat", a.handle, b.handle, C.byref(h))
+        return type(g)(g.s.union(f.s), h, g.ctx)
+    raise NotImplementedError("multiply of functions on partially overlapping vertex sets")
+
+
+def point_to_opsum(s, x, dim: int) -> OpSum:
+    """src/elementary_operators.jl:197-206."""
+    iv = s.calculate_ind_values([x], [dim])
+    out = OpSum()
+    out.add(1.0, {(l.dim, l.digit): ("Dup" if val == 1 else "Ddn") for l, val in iv.items()})
+    return out
+
+
+def map_to_zero_operator(s, xs, dims=None, **truncate_kwargs):
+    """diag(1 - sum_x delta_x + overlaps) (src/elementary_operators.jl:209-227)."""
+    from .elementary_functions import delta_kernel
+
+    xs = [xs] if np.isscalar(xs) else list(xs)
+    dims = [1] * len(xs) if dims is None else ([dims] if isinstance(dims, int) else list(dims))
+    k = delta_kernel(s, [[x] for x in xs], [[d] for d in dims], remove_overlap=True, coeff=-1.0,
+                     include_identity=True)
+    return operator_proj(k)
+
+
+def map_to_zeros(f, xs, dims=None, truncate_kwargs=None, **kw):
+    """src/elementary_operators.jl:230-244."""
+    from .operate import operate
+
+    op = map_to_zero_operator(f.s, xs, dims, **(truncate_kwargs or {}))
+    return operate(op, f, **kw)
+

@@ -1,0 +1,317 @@
+"""Digit site legs and their map to continuous coordinates.
+
+Mirrors src/digit_inds.jl (digit legs on graph vertices),
+src/IndexMaps/{abstract,real,complex}indexmap.jl (digit k of variable d has
+weight value * base^-k, digit 1 most significant) and src/indsnetworkmap.jl
+(IndsNetworkMap = graph + legs + map).  Legs are plain records here; the
+device never sees names, only the layout built in :class:`TreeLayout`.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from functools import cached_property
+from typing import Hashable, Sequence
+
+import numpy as np
+
+from .graphs import NamedGraph
+
+REAL, IMAG = "real", "imag"
+
+
+@dataclass(frozen=True)
+class SiteLeg:
+    """One digit index: variable `dim` (1-based), digit (1 = most significant)."""
+
+    vertex: Hashable
+    dim: int
+    digit: int
+    base: int = 2
+    kind: str = REAL  # REAL or IMAG (complex index maps)
+
+    def value_to_scalar(self, value: int):
+        """index_value_to_scalar (src/IndexMaps/realindexmap.jl:13-15,
+        src/IndexMaps/complexindexmap.jl:25-32)."""
+        w = value * float(self.base) ** (-self.digit)
+        return 1j * w if self.kind == IMAG else w
+
+    def values_to_scalars(self) -> list:
+        return [self.value_to_scalar(i) for i in range(self.base)]
+
+
+def default_dimension_vertices(g: NamedGraph, map_dimension: int = 1) -> list[list]:
+    """Round-robin assignment of the graph's vertices to dimensions
+    (src/digit_inds.jl:17-21)."""
+    vs = g.vertices()
+    return [vs[i::map_dimension] for i in range(map_dimension)]
+
+
+class TreeLayout:
+    """Device order of a forest: roots are the first vertex (graph order) of
+    each component; vertices are numbered breadth first so that
+    parent[v] < v and the children of a vertex have increasing numbers."""
+
+    def __init__(self, g: NamedGraph):
+        if not g.is_forest():
+            raise ValueError(
+                "tensor network functions on this engine live on trees (or forests); "
+                "the graph has a cycle"
+            )
+        self.order: list = []
+        self.parent: list[int] = []
+        pos: dict = {}
+        for comp in g.components():
+            root = comp[0]
+            pos[root] = len(self.order)
+            self.order.append(root)
+            self.parent.append(-1)
+            head = pos[root]
+            while head < len(self.order):
+                v = self.order[head]
+                for w in g.neighbors(v):
+                    if w not in pos:
+                        pos[w] = len(self.order)
+                        self.order.append(w)
+                        self.parent.append(head)
+                head += 1
+        self.pos = pos
+        self.children: list[list[int]] = [[] for _ in self.order]
+        for i, p in enumerate(self.parent):
+            if p >= 0:
+                self.children[p].append(i)
+
+    @property
+    def n(self) -> int:
+        return len(self.order)
+
+    def neighbours_in_layout_order(self, i: int) -> list[int]:
+        """[parent (if any), children...] of layout vertex i."""
+        return ([self.parent[i]] if self.parent[i] >= 0 else []) + self.children[i]
+
+
+class IndsNetworkMap:
+    """A graph whose vertices carry digit legs, plus the digit -> coordinate map."""
+
+    def __init__(self, graph: NamedGraph, legs: dict, is_complex: bool = False):
+        self.graph = graph
+        self.legs = {v: list(legs.get(v, [])) for v in graph.vertices()}
+        self.is_complex = is_complex
+
+    # -- structure ----------------------------------------------------------
+    @cached_property
+    def layout(self) -> TreeLayout:
+        return TreeLayout(self.graph)
+
+    def vertices(self) -> list:
+        return self.graph.vertices()
+
+    def nv(self) -> int:
+        return self.graph.nv()
+
+    def inds(self, v=None) -> list[SiteLeg]:
+        if v is None:
+            return [l for w in self.vertices() for l in self.legs[w]]
+        return list(self.legs[v])
+
+    def __getitem__(self, v) -> list[SiteLeg]:
+        return self.inds(v)
+
+    def base(self) -> int:
+        bases = {l.base for l in self.inds()}
+        if len(bases) != 1:
+            raise ValueError("site legs have different bases")
+        return bases.pop()
+
+    def is_tree(self) -> bool:
+        return self.graph.is_tree()
+
+    # -- dimensions ---------------------------------------------------------
+    def dimensions(self) -> list[int]:
+        seen = []
+        for l in self.inds():
+            if l.dim not in seen:
+                seen.append(l.dim)
+        return seen
+
+    def dimension(self, leg: SiteLeg | None = None) -> int:
+        if leg is not None:
+            return leg.dim
+        return max(self.dimensions())
+
+    def dimension_inds(self, dims) -> list[SiteLeg]:
+        dims = [dims] if isinstance(dims, int) else list(dims)
+        return [l for l in self.inds() if l.dim in dims]
+
+    def dimension_vertices(self, dims) -> list:
+        dims = [dims] if isinstance(dims, int) else list(dims)
+        return [v for v in self.vertices() if any(l.dim in dims for l in self.legs[v])]
+
+    def vertex(self, dim: int, digit: int, kind: str = REAL):
+        hits = [
+            v for v in self.vertices()
+            for l in self.legs[v] if l.dim == dim and l.digit == digit and l.kind == kind
+        ]
+        if len(hits) != 1:
+            raise KeyError(f"no unique vertex for dim={dim} digit={digit}")
+        return hits[0]
+
+    def vertex_dimension(self, v) -> int:
+        (leg,) = self.legs[v]
+        return leg.dim
+
+    def vertex_digit(self, v) -> int:
+        (leg,) = self.legs[v]
+        return leg.digit
+
+    def vertices_dimensions(self, verts) -> list[int]:
+        return [l.dim for v in verts for l in self.legs[v]]
+
+    def vertices_digits(self, verts) -> list[int]:
+        return [l.digit for v in verts for l in self.legs[v]]
+
+    def ndigits(self, dim: int, kind: str = REAL) -> int:
+        return sum(1 for l in self.inds() if l.dim == dim and l.kind == kind)
+
+    # -- digit map ----------------------------------------------------------
+    def calculate_ind_values(self, xs, dims=None) -> dict:
+        """Digits of the point xs (src/IndexMaps/realindexmap.jl:67-76 with the
+        greedy subtraction of src/IndexMaps/abstractindexmap.jl:121-138)."""
+        xs = [xs] if np.isscalar(xs) else list(xs)
+        if dims is None:
+            dims = list(range(1, len(xs) + 1))
+        dims = [dims] if isinstance(dims, int) else list(dims)
+        if len(xs) != len(dims):
+            raise ValueError("xs and dims differ in length")
+        out = {}
+        parts = [(REAL, lambda z: float(np.real(z)))]
+        if self.is_complex:
+            parts.append((IMAG, lambda z: float(np.imag(z))))
+        for d, x in zip(dims, xs):
+            for kind, part in parts:
+                legs = sorted(
+                    (l for l in self.inds() if l.dim == d and l.kind == kind), key=lambda l: l.digit
+                )
+                rem = part(x)
+                if not (rem >= 0.0 and np.isfinite(rem)):
+                    raise ValueError(f"coordinate {x} outside the digit map's domain [0, inf)")
+                for l in legs:
+                    invb = 1.0 / float(l.base) ** l.digit
+                    val = 0
+                    for cand in range(l.base - 1, 0, -1):
+                        t = cand * invb
+                        if rem >= t:
+                            val, rem = cand, rem - t
+                            break
+                    out[l] = val
+        return out
+
+    def calculate_p(self, ind_values: dict, dims=None) -> list:
+        """Coordinates from digit values (src/IndexMaps/abstractindexmap.jl:103-119)."""
+        dims = self.dimensions() if dims is None else ([dims] if isinstance(dims, int) else dims)
+        return [sum(l.value_to_scalar(v) for l, v in ind_values.items() if l.dim == d) for d in dims]
+
+    def grid_points(self, N: int, d: int) -> list:
+        """N uniform grid points of dimension d (src/IndexMaps/realindexmap.jl:78-86)."""
+        legs = [l for l in self.inds() if l.dim == d and l.kind == REAL]
+        base = float(legs[0].base)
+        L = len(legs)
+        a = round(base**L / N)
+        pts = [i * (a / base**L) for i in range(N + 2)]
+        return [x for x in pts if x < 1]
+
+    # -- derived maps -------------------------------------------------------
+    def reduced(self, dims) -> "IndsNetworkMap":
+        """reduced_indsnetworkmap (src/indsnetworkmap.jl:29-46)."""
+        dims = [dims] if isinstance(dims, int) else list(dims)
+        legs = {v: [l for l in self.legs[v] if l.dim in dims] for v in self.vertices()}
+        keep = [v for v in self.vertices() if legs[v]]
+        return IndsNetworkMap(self.graph.induced_subgraph(keep), legs, self.is_complex)
+
+    def union(self, other: "IndsNetworkMap") -> "IndsNetworkMap":
+        g = self.graph.copy()
+        for v in other.vertices():
+            g.add_vertex(v)
+        for u, w in other.graph.edges():
+            g.add_edge(u, w)
+        legs = dict(self.legs)
+        for v in other.vertices():
+            if v not in legs:
+                legs[v] = other.legs[v]
+        return IndsNetworkMap(g, legs, self.is_complex or other.is_complex)
+
+    def same_structure(self, other: "IndsNetworkMap") -> bool:
+        return (
+            self.graph.vertices() == other.graph.vertices()
+            and set(self.graph.edges()) == set(other.graph.edges())
+            and all(self.legs[v] == other.legs[v] for v in self.vertices())
+        )
+
+    # -- device topology ------------------------------------------------------
+    def leg_arrays(self):
+        """Per layout vertex: n_legs, and flattened leg dim/var/digit/kind."""
+        lay = self.layout
+        nlegs, ldim, lvar, ldig, lkind = [], [], [], [], []
+        for v in lay.order:
+            legs = self.legs[v]
+            nlegs.append(len(legs))
+            for l in legs:
+                ldim.append(l.base)
+                lvar.append(l.dim)
+                ldig.append(l.digit)
+                lkind.append(1 if l.kind == IMAG else 0)
+        return nlegs, ldim, lvar, ldig, lkind
+
+    def __repr__(self) -> str:
+        return f"IndsNetworkMap(nv={self.nv()}, dims={self.dimensions()}, complex={self.is_complex})"
+
+
+def digit_siteinds(g: NamedGraph, dimension_vertices=None, base: int = 2, map_dimension: int = 1):
+    """Legs of a real map (src/digit_inds.jl:72-86)."""
+    if not dimension_vertices or not dimension_vertices[0]:
+        dimension_vertices = default_dimension_vertices(g, map_dimension)
+    legs: dict = {v: [] for v in g.vertices()}
+    for d, verts in enumerate(dimension_vertices, start=1):
+        for k, v in enumerate(verts, start=1):
+            legs[v].append(SiteLeg(v, d, k, base, REAL))
+    return legs
+
+
+def continuous_siteinds(
+    g: NamedGraph, dimension_vertices=None, *, base: int = 2, map_dimension: int = 1
+) -> IndsNetworkMap:
+    """RealIndsNetworkMap (src/indsnetworkmap.jl:53-64, alias :83)."""
+    return IndsNetworkMap(g, digit_siteinds(g, dimension_vertices, base, map_dimension), False)
+
+
+real_continuous_siteinds = continuous_siteinds
+
+
+def complex_continuous_siteinds(
+    g: NamedGraph,
+    real_dimension_vertices=None,
+    imag_dimension_vertices=None,
+    *,
+    base: int = 2,
+    map_dimension: int = 1,
+) -> IndsNetworkMap:
+    """ComplexIndsNetworkMap (src/indsnetworkmap.jl:66-81; legs src/digit_inds.jl:88-115)."""
+    if not real_dimension_vertices or not real_dimension_vertices[0]:
+        real_dimension_vertices = default_dimension_vertices(g, map_dimension)
+    if not imag_dimension_vertices or not imag_dimension_vertices[0]:
+        imag_dimension_vertices = default_dimension_vertices(g, map_dimension)
+    legs: dict = {v: [] for v in g.vertices()}
+    for d, verts in enumerate(real_dimension_vertices, start=1):
+        for k, v in enumerate(verts, start=1):
+            legs[v].append(SiteLeg(v, d, k, base, REAL))
+    for d, verts in enumerate(imag_dimension_vertices, start=1):
+        for k, v in enumerate(verts, start=1):
+            legs[v].append(SiteLeg(v, d, k, base, IMAG))
+    return IndsNetworkMap(g, legs, True)
+
+
+def reduced_indsnetworkmap(s: IndsNetworkMap, dims) -> IndsNetworkMap:
+    return s.reduced(dims)
+
+
+def grid_points(s: IndsNetworkMap, N: int, d: int) -> list:
+    return s.grid_points(N, d)

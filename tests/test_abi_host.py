@@ -1,0 +1,124 @@
+"""CPU tests: the C-ABI library loads and exports every declared symbol; the
+host-side graph / digit-map / constructor logic agrees with the oracle."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared_symbols():
+    text = (ROOT / "include" / "tnfa.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tnfa_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import itensornumericalanalysis._build as b
+
+    if not b.LIB_PATH.exists():
+        b.build()
+    return C.CDLL(str(b.LIB_PATH))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    syms = _declared_symbols()
+    assert len(syms) >= 25
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_ctypes_signatures_cover_the_header():
+    from itensornumericalanalysis import _lib
+
+    assert set(_declared_symbols()) == set(_lib.SIGNATURES)
+
+
+def test_version_and_null_arguments(lib):
+    from itensornumericalanalysis import _lib
+
+    L = _lib.load()
+    assert L.tnfa_version().decode().startswith("tnfa ")
+    # null handles are rejected without touching a device
+    assert L.tnfa_net_destroy(None) == _lib.ERR_INVALID_ARGUMENT
+    assert L.tnfa_ctx_destroy(None) == _lib.ERR_INVALID_ARGUMENT
+    assert L.tnfa_net_info(None, None, None, None, None) == _lib.ERR_INVALID_ARGUMENT
+    assert L.tnfa_last_error_string(None) == b"null context"
+
+
+def test_graph_generators_match_oracle():
+    import itensornumericalanalysis as ina
+
+    for g, (ov, oe) in [
+        (ina.named_grid((4, 3)), O.grid_graph((4, 3))),
+        (ina.named_comb_tree((3, 4)), O.comb_tree_graph((3, 4))),
+        (ina.named_binary_tree(60), O.binary_tree_graph(60)),
+    ]:
+        assert g.vertices() == ov
+        assert set(map(frozenset, g.edges())) == set(map(frozenset, oe))
+    assert ina.named_comb_tree((2, 16)).is_tree()
+    assert not ina.named_grid((3, 3)).is_forest()
+    t = ina.uniform_tree(30, 0)
+    assert t.is_tree() and t.nv() == 30
+
+
+def test_tree_layout_is_topological():
+    import itensornumericalanalysis as ina
+
+    for g in [ina.named_comb_tree((4, 3)), ina.named_binary_tree(60), ina.uniform_tree(40, 3)]:
+        lay = ina.continuous_siteinds(g).layout
+        assert lay.parent[0] == -1
+        assert all(p < i for i, p in enumerate(lay.parent) if p >= 0)
+        for i, ch in enumerate(lay.children):
+            assert ch == sorted(ch)
+            assert all(lay.parent[c] == i for c in ch)
+    with pytest.raises(ValueError):
+        ina.continuous_siteinds(ina.named_grid((3, 3))).layout
+
+
+def test_host_digit_map_matches_oracle():
+    import itensornumericalanalysis as ina
+
+    rng = np.random.default_rng(0)
+    for base in (2, 3):
+        g = ina.named_comb_tree((3, 4))
+        s = ina.continuous_siteinds(g, base=base, map_dimension=2)
+        so = O.siteinds(O.comb_tree_graph((3, 4)), base=base, map_dimension=2)
+        for _ in range(50):
+            xs = list(rng.random(2))
+            iv = s.calculate_ind_values(xs, [1, 2])
+            ivo = O.calculate_ind_values(so, xs, [1, 2])
+            a = sorted((l.dim, l.digit, v) for l, v in iv.items())
+            b = sorted((so.info[i][0], so.info[i][1], v) for i, v in ivo.items())
+            assert a == b
+        pts = s.calculate_p(s.calculate_ind_values([0.625, 0.25], [1, 2]), [1, 2])
+        if base == 2:
+            assert pts == [0.625, 0.25]
+    with pytest.raises(ValueError):
+        s.calculate_ind_values([-0.5, 0.1], [1, 2])
+
+
+def test_grid_points():
+    import itensornumericalanalysis as ina
+
+    s = ina.continuous_siteinds(ina.named_grid((8, 1)))
+    pts = s.grid_points(16, 1)
+    assert pts[0] == 0.0 and all(p < 1 for p in pts)
+    assert np.allclose(np.diff(pts), 1 / 16)
+
+
+def test_reduced_maps():
+    import itensornumericalanalysis as ina
+
+    g = ina.named_comb_tree((3, 5))
+    s = ina.continuous_siteinds(g, [[(i, j) for j in range(1, 6)] for i in range(1, 4)])
+    s2 = ina.reduced_indsnetworkmap(s, 2)
+    assert s2.dimensions() == [2]
+    assert s2.vertices() == [(2, j) for j in range(1, 6)]
+    assert s2.is_tree()

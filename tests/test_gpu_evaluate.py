@@ -1,0 +1,246 @@
+"""Batched evaluation and integration on the GPU (through the C ABI) against
+the CPU oracle and the reference's analytic known answers."""
+import numpy as np
+import pytest
+
+import oracle as O
+from _helpers import product_map, rel_err, upload_oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL_F64 = 1e-12  # plain FP64 path vs the FP64 oracle
+TOL_F32 = 2e-5   # FP32 CUDA-core path
+
+
+GRAPHS = {
+    "path12": O.path_graph(12),
+    "comb3x4": O.comb_tree_graph((3, 4)),
+    "binary15": O.binary_tree_graph(15),
+}
+
+
+def _points(rng, n, ndim):
+    return rng.random((n, ndim))
+
+
+@pytest.mark.parametrize("gname", list(GRAPHS))
+@pytest.mark.parametrize("chi", [1, 3, 16])
+def test_random_network_f64(ina, gname, chi):
+    graph = GRAPHS[gname]
+    rng = np.random.default_rng(chi)
+    s_or = O.siteinds(graph, map_dimension=2)
+    net = O.random_net(s_or, chi, rng, normalize=True)
+    f, _ = upload_oracle(ina, graph, net)
+    X = _points(rng, 257, 2)
+    got = f.evaluate_batch(X, [1, 2], precision="f64")
+    ref = np.array([O.evaluate(net, list(x), [1, 2]) for x in X[:64]])
+    assert rel_err(got[:64], ref) < TOL_F64
+    # per-point calls agree with the batch
+    for p in (0, 100, 256):
+        assert abs(f.evaluate(list(X[p]), [1, 2]) - got[p]) <= 1e-14 * max(1.0, abs(got[p]))
+
+
+@pytest.mark.parametrize("precision", ["f32", "mixed"])
+def test_random_network_f32_paths(ina, precision):
+    graph = O.binary_tree_graph(31)
+    rng = np.random.default_rng(5)
+    s_or = O.siteinds(graph, map_dimension=3)
+    net = O.random_net(s_or, 8, rng, normalize=True)
+    f, _ = upload_oracle(ina, graph, net)
+    X = _points(rng, 1000, 3)
+    ref = f.evaluate_batch(X, [1, 2, 3], precision="f64")
+    m, e = f.evaluate_batch(X, [1, 2, 3], precision=precision, out="f32_scaled")
+    got = np.ldexp(m, e)
+    err = np.abs(got - ref) / np.abs(ref)
+    assert np.median(err) < TOL_F32
+    # values underflow plain FP32 here; the scaled output keeps them
+    assert np.all(np.isfinite(got)) and np.all(got != 0)
+
+
+FUNCS = [
+    ("cosh", "cosh_itn", O.cosh_itn, np.cosh),
+    ("sinh", "sinh_itn", O.sinh_itn, np.sinh),
+    ("exp", "exp_itn", O.exp_itn, np.exp),
+    ("cos", "cos_itn", O.cos_itn, np.cos),
+    ("sin", "sin_itn", O.sin_itn, np.sin),
+]
+
+
+@pytest.mark.parametrize("name,pname,onet,fn", FUNCS)
+@pytest.mark.parametrize("base", [2, 3])
+def test_constructors_match_oracle(ina, name, pname, onet, fn, base):
+    """test/test_realitensorfunction.jl:65-104 on the GPU."""
+    rng = np.random.default_rng(3)
+    a, k, c = rng.random(3)
+    graph = O.comb_tree_graph((2, 3))
+    s_or = O.siteinds(graph, base=base)
+    s = product_map(ina, graph, s_or)
+    f = getattr(ina, pname)(s, k=k, a=a, c=c)
+    x = 0.625 if base == 2 else 5.0 / 9.0
+    val = f.evaluate(x)
+    assert abs(val - c * fn(k * x + a)) <= np.sqrt(np.finfo(float).eps) * abs(c * fn(k * x + a))
+    X = rng.random((50, 1))
+    got = f.evaluate_batch(X)
+    ref = np.array([O.evaluate(onet(s_or, k=k, a=a, c=c), [x0]) for x0 in X[:, 0]])
+    assert rel_err(got, ref.real if not np.iscomplexobj(got) else ref) < TOL_F64
+
+
+def test_tanh_and_poly(ina):
+    """test/test_realitensorfunction.jl:106-144."""
+    rng = np.random.default_rng(4)
+    a, k, c = rng.random(3)
+    s = ina.continuous_siteinds(ina.named_grid((10, 1)))
+    f = ina.tanh_itn(s, k=k, a=a, c=c, nterms=50)
+    assert abs(f.evaluate(0.625) - c * np.tanh(k * 0.625 + a)) < 1e-8
+    for deg in range(1, 12):
+        g = ina.uniform_tree(6, rng)
+        s = ina.continuous_siteinds(g)
+        k, c = rng.random(2)
+        coeffs = rng.random(deg + 1)
+        p = ina.poly_itn(s, list(coeffs), k=k, c=c)
+        x = 0.875
+        exact = c * sum(coeffs[i] * (k * x) ** i for i in range(deg + 1))
+        assert abs(p.evaluate(x) - exact) <= 1e-4
+
+
+def test_poly_matches_oracle_tensors_values(ina):
+    graph = O.comb_tree_graph((3, 3))
+    s_or = O.siteinds(graph, map_dimension=2)
+    s = product_map(ina, graph, s_or)
+    coeffs = [1.0, 0.5, 0.25]
+    f = ina.poly_itn(s, coeffs, dim=1)
+    onet = O.poly_itn(s_or, coeffs, dim=1)
+    rng = np.random.default_rng(8)
+    X = rng.random((40, 2))
+    ref = np.array([O.evaluate(onet, list(x), [1, 2]) for x in X]).real
+    assert rel_err(f.evaluate_batch(X, [1, 2]), ref) < TOL_F64
+
+
+def test_const_and_sums(ina):
+    """test/test_realitensorfunction.jl:147-189."""
+    s = ina.continuous_siteinds(ina.named_comb_tree((3, 3)), map_dimension=3)
+    assert abs(ina.const_itn(s, c=1.5).evaluate([0.5, 0.25, 0.0], [1, 2, 3]) - 1.5) < 1e-14
+    assert abs(ina.const_itn(s, c=-2.0, linkdim=4).evaluate([0.5, 0.25, 0.0], [1, 2, 3]) + 2.0) < 1e-13
+    s = ina.continuous_siteinds(ina.named_grid((10, 1)), map_dimension=2)
+    rng = np.random.default_rng(9)
+    for _, pname, _, fn in FUNCS:
+        a, k, c = rng.random(3)
+        f = getattr(ina, pname)(s, k=k, a=a, c=c, dim=1) + getattr(ina, pname)(s, k=k, a=a, c=c, dim=2)
+        x, y = 0.625, 0.25
+        assert abs(f.evaluate([x, y], [1, 2]) - (c * fn(k * x + a) + c * fn(k * y + a))) < 1e-12
+
+
+def test_delta_p(ina):
+    """test/test_realitensorfunction.jl:210-259."""
+    L = 10
+    s = ina.continuous_siteinds(ina.named_grid((L, 1)), map_dimension=2)
+    x0, y0 = 0.625, 0.25
+    d = 2.0**-L
+    xs = [0.0, d, 0.25, 0.5, 0.625, 0.875, 1 - d]
+    psi = ina.delta_p(s, [x0, y0])
+    assert abs(psi.evaluate([x0, y0], [1, 2]) - 1) < 1e-14
+    assert abs(psi.evaluate([y0, x0], [1, 2])) < 1e-14
+    plane = ina.delta_p(s, [y0], [2])
+    X = np.array([[x, y0] for x in xs] + [[x, 0.5] for x in xs])
+    v = plane.evaluate_batch(X, [1, 2])
+    assert np.allclose(v[: len(xs)], 1.0) and np.allclose(v[len(xs):], 0.0)
+    both = ina.delta_p(s, [[x0, y0], [0.5]], [[1, 2], [2]])
+    assert abs(both.evaluate([x0, y0], [1, 2]) - 1) < 1e-14
+    for x in xs:
+        assert abs(both.evaluate([x, 0.5], [1, 2]) - 1) < 1e-14
+    assert abs(both.evaluate([0.0, 0.0], [1, 2])) < 1e-14
+
+
+def test_complex_map_functions(ina):
+    """test/test_complexitensorfunction.jl:57-80 (complex k, a, c and map)."""
+    rng = np.random.default_rng(10)
+    graph = O.comb_tree_graph((2, 3))
+    rdv, idv = [[(1, 1), (1, 2), (1, 3)]], [[(2, 1), (2, 2), (2, 3)]]
+    s_or = O.complex_siteinds(graph, rdv, idv)
+    s = product_map(ina, graph, s_or)
+    for _, pname, onet, fn in FUNCS:
+        a, k, c = rng.random(3) + 1j * rng.random(3)
+        f = getattr(ina, pname)(s, k=k, a=a, c=c)
+        z = 0.625 + 0.25j
+        assert abs(f.evaluate(z) - c * fn(k * z + a)) <= 1e-7 * abs(c * fn(k * z + a))
+        Z = rng.random(20) + 1j * rng.random(20)
+        got = f.evaluate_batch(Z.reshape(-1, 1))
+        ref = np.array([O.evaluate(onet(s_or, k=k, a=a, c=c), [z0]) for z0 in Z])
+        assert rel_err(got, ref) < TOL_F64
+
+
+def test_integrate(ina):
+    """test/test_integration.jl:15-38 plus oracle parity."""
+    s = ina.continuous_siteinds(ina.named_comb_tree((2, 10)))
+    f = ina.exp_itn(s, dim=1)
+    assert abs(ina.integrate(f * f) - 0.5 * (np.e**2 - 1)) <= 1e-4
+    s = ina.continuous_siteinds(ina.named_comb_tree((3, 10)), map_dimension=2)
+    g = ina.exp_itn(s, dim=1) * ina.exp_itn(s, dim=2)
+    assert abs(ina.integrate(g) - (np.e - 1) ** 2) <= 1e-4
+    graph = O.binary_tree_graph(20)
+    rng = np.random.default_rng(12)
+    s_or = O.siteinds(graph, map_dimension=2)
+    net = O.random_net(s_or, 6, rng)
+    fp, _ = upload_oracle(ina, graph, net)
+    assert abs(fp.integrate() - O.integrate(net)) <= TOL_F64 * abs(O.integrate(net))
+    assert abs(fp.integrate(take_sum=True) - O.integrate(net, take_sum=True)) <= TOL_F64 * abs(
+        O.integrate(net, take_sum=True))
+
+
+def test_sum_and_product_algebra(ina):
+    graph = O.comb_tree_graph((3, 3))
+    rng = np.random.default_rng(13)
+    s_or = O.siteinds(graph, map_dimension=2)
+    n1 = O.random_net(s_or, 3, rng)
+    n2 = O.random_net(s_or, 2, rng)
+    f1, _ = upload_oracle(ina, graph, n1)
+    f2, _ = upload_oracle(ina, graph, n2)
+    X = rng.random((30, 2))
+    r1 = np.array([O.evaluate(n1, list(x), [1, 2]) for x in X])
+    r2 = np.array([O.evaluate(n2, list(x), [1, 2]) for x in X])
+    assert rel_err((f1 + f2).evaluate_batch(X, [1, 2]), r1 + r2) < TOL_F64
+    assert rel_err((f1 * f2).evaluate_batch(X, [1, 2]), r1 * r2) < TOL_F64
+    assert rel_err((2.5 * f1).evaluate_batch(X, [1, 2]), 2.5 * r1) < TOL_F64
+    assert (f1 + f2).maxlinkdim() == 5 and (f1 * f2).maxlinkdim() == 6
+
+
+def test_edge_cases(ina):
+    s = ina.continuous_siteinds(ina.named_grid((8, 1)))
+    f = ina.exp_itn(s)
+    d = 2.0**-8
+    # x >= 1 saturates to the last grid point, as the reference's greedy loop does
+    assert abs(f.evaluate(1.0) - np.exp(1 - d)) < 1e-12
+    assert abs(f.evaluate(7.5) - np.exp(1 - d)) < 1e-12
+    with pytest.raises(ina.TnfaError) as e:
+        f.evaluate(-0.25)
+    assert e.value.status == ina._lib.ERR_DOMAIN
+    with pytest.raises(ina.TnfaError):
+        f.evaluate(float("nan"))
+    assert f.evaluate_batch(np.zeros((0, 1))).shape == (0,)
+    # a single-vertex network
+    s1 = ina.continuous_siteinds(ina.named_grid((1, 1)))
+    g = ina.exp_itn(s1, k=2.0)
+    assert abs(g.evaluate(0.5) - np.exp(1.0)) < 1e-14
+    # a forest: product of functions on disjoint vertex sets
+    s2 = ina.continuous_siteinds(ina.named_comb_tree((2, 4)), [[(1, j) for j in range(1, 5)],
+                                                             [(2, j) for j in range(1, 5)]])
+    sa, sb = ina.reduced_indsnetworkmap(s2, 1), ina.reduced_indsnetworkmap(s2, 2)
+    h = ina.exp_itn(sa, dim=1) * ina.cos_itn(sb, dim=2)
+    x, y = 0.5, 0.25
+    assert abs(h.evaluate([x, y], [1, 2]) - np.exp(x) * np.cos(y)) < 1e-12
+
+
+def test_deep_tree_underflow_is_scaled(ina):
+    """60-vertex binary tree with unit-norm tensors: |f| ~ 1e-40..1e-60, far
+    below FP32's range; the FP32 path carries a base-2 exponent per point."""
+    graph = O.binary_tree_graph(60)
+    rng = np.random.default_rng(14)
+    s_or = O.siteinds(graph, map_dimension=3)
+    net = O.random_net(s_or, 16, rng, normalize=True)
+    f, _ = upload_oracle(ina, graph, net)
+    X = rng.random((256, 3))
+    ref = np.array([O.evaluate(net, list(x), [1, 2, 3]) for x in X[:16]])
+    got = f.evaluate_batch(X, [1, 2, 3], precision="f64")
+    assert rel_err(got[:16], ref) < 1e-11
+    m, e = f.evaluate_batch(X, [1, 2, 3], precision="f32", out="f32_scaled")
+    assert np.median(np.abs(np.ldexp(m, e) - got) / np.abs(got)) < TOL_F32
