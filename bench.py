@@ -364,6 +364,7 @@ def main():
         "fp64_plain": {"value": f64_rate, "unit": "points/s", "sample_points": nf,
                        "speedup_of_value": value / ws / f64_rate},
         "rel_err_vs_fp64": {"median": float(np.median(rel)), "max": float(np.max(rel)),
+                            "normwise": float(np.linalg.norm(got - ref64) / np.linalg.norm(ref64)),
                             "points": nf},
         "kernels": {k: {"launches_per_step": v["launches"] // args.steps,
                         "ms_per_step": v["ms"] / args.steps} for k, v in stats.items()},

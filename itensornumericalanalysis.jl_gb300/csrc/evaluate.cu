@@ -607,7 +607,7 @@ static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, 
       }
       if constexpr (std::is_same<T, float>::value) {
         if (tc) {
-          tc_contract_vertex(ctx, net, v, j, tp);
+          tc_contract_vertex(ctx, net, v, j, tp, derr.as<int>());
           continue;
         }
       }
@@ -635,6 +635,8 @@ static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, 
   int herr = 0;
   TNFA_CUDA(cudaMemcpyAsync(&herr, derr.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
   TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  TNFA_CHECK((herr & 2) == 0, TNFA_ERR_TIMEOUT,
+             "a tensor-core pipeline wait ran out of its iteration budget");
   TNFA_CHECK(herr == 0, TNFA_ERR_DOMAIN,
              "a coordinate is negative or not finite (the digit map needs x >= 0)");
 }

@@ -49,7 +49,7 @@ inline size_t group_meta_ints(int ng) { return (size_t)4 * ng + 1; }
 bool tc_vertex_eligible(int nchild, const int* child_dims, int chi_a);
 void tc_prepare_net(tnfa_ctx* ctx, const tnfa_net* net);  // BF16 hi/lo copies
 void tc_contract_vertex(tnfa_ctx* ctx, const tnfa_net* net, int v, const VertexJob<float>& job,
-                        int tile_rows);
+                        int tile_rows, int* err);
 int tc_tile_rows();
 
 }  // namespace tnfa

@@ -1,13 +1,541 @@
-// Tensor-core (tcgen05) vertex contraction for batched evaluation.
+// Tensor-core (tcgen05) vertex contraction for batched evaluation, sm_103a.
+//
+// One CTA computes a tile of 128 points (rows) of one vertex:
+//   out[p, a] = sum_{b, c} m1[p, b] m2[p, c] T_s[a][b * chi2 + c]
+// i.e. D[128 x N] = A[128 x K] * B[N x K]^T with K = chi1 * chi2, A the row-wise
+// Kronecker product of the two child messages (never stored in global memory)
+// and B the slice T_s of the vertex tensor (canonical layout, K-major).
+//
+// Precision: split BF16.  A = A_hi + A_lo, B = B_hi + B_lo (each BF16), and
+// D = A_hi B_hi + A_hi B_lo + A_lo B_hi accumulated in FP32 in tensor memory;
+// the dropped A_lo B_lo term is ~2^-16 relative.
+//
+// Roles (320 threads):
+//   warps 0-7  producers: thread (row m, half h) keeps half of its m2 row in
+//              registers and writes 32 of the 64 columns of every A chunk (hi and
+//              lo) into 128B-swizzled shared memory; afterwards they run the
+//              epilogue (TMEM -> registers, power-of-two row rescaling, store).
+//   warp 8     TMA: streams the B_hi / B_lo chunk [N x 64] of every K step.
+//   warp 9     MMA: one lane issues tcgen05.mma (M=128, N, K=16) x 12 per chunk.
+// Stages are guarded by mbarriers; every wait is bounded and a timeout sets an
+// error bit and unwinds (TMEM is always released).
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "evaluate.cuh"
 
 namespace tnfa {
 
-bool tc_vertex_eligible(int, const int*, int) { return false; }
-void tc_prepare_net(tnfa_ctx*, const tnfa_net*) {}
-int tc_tile_rows() { return 128; }
-void tc_contract_vertex(tnfa_ctx*, const tnfa_net*, int, const VertexJob<float>&, int) {
-  fail(TNFA_ERR_UNSUPPORTED, "tensor-core evaluation not built");
+namespace {
+
+constexpr int TC_M = 128;         // rows per tile (points)
+constexpr int TC_KC = 64;         // K elements per chunk (128 bytes of BF16)
+constexpr int TC_PRODUCERS = 256; // warps 0-7
+constexpr int TC_THREADS = 320;
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 26;  // try_wait iterations before giving up
+constexpr int TC_ERR_TIMEOUT = 2;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t addr = smem_u32(bar);
+  for (uint32_t it = 0; it < TC_WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
+// 1024 bytes (SBO), version 1.
+__device__ __forceinline__ uint64_t sw128_desc(const void* base) {
+  uint64_t a = smem_u32(base);
+  uint64_t d = (a & 0x3FFFFull) >> 4;
+  d |= (uint64_t)1 << 16;            // leading byte offset (unused for this layout)
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
+  d |= (uint64_t)1 << 46;            // descriptor version
+  d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: BF16 x BF16 -> FP32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+struct TcParams {
+  const float* m1_ptr;   // child 1 rows (message or leaf tensor); null: chi1 = 1
+  const int* m1_exp;
+  const uint8_t* m1_S;
+  const float* m2_ptr;   // child 2 rows
+  const int* m2_exp;
+  const uint8_t* m2_S;
+  int chi1, chi2, N, K;
+  float* out;
+  int* out_exp;
+  const int* perm;
+  const int* grp_off;
+  const int* grp_cnt;
+  const int* tile_start;
+  int ngroups;
+  int* err;
+};
+
+// BILIN = false: Kronecker mode above (output N = chi_a columns).
+// BILIN = true : root of two children (chi_a = 1): A = m2 rows (K = chi2),
+//                N = chi1, and the epilogue contracts D[p, :] with m1[p, :].
+template <int N, int CHI2, int STAGES, bool BILIN>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_contract_tc(const __grid_constant__ CUtensorMap map_hi,
+                  const __grid_constant__ CUtensorMap map_lo, const TcParams P) {
+  constexpr int A_BYTES = TC_M * TC_KC * 2;  // 16 KB
+  constexpr int B_BYTES = N * TC_KC * 2;
+  constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+  constexpr int HALF = CHI2 / 2;  // m2 values per producer thread
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], acc_bar;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ float rowmax[2][TC_M];
+  __shared__ int sh_abort;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  unsigned char* smem =
+      (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+
+  // ---- tile lookup (same grouping as the SIMT kernels) ----
+  const int b = blockIdx.x;
+  const int ng = P.ngroups;
+  if (b >= P.tile_start[ng]) return;
+  int g = 0;
+  while (g + 1 < ng && P.tile_start[g + 1] <= b) ++g;
+  const int row0 = P.grp_off[g] + (b - P.tile_start[g]) * TC_M;
+  const int nrows = min(TC_M, P.grp_off[g] + P.grp_cnt[g] - row0);
+  if (nrows <= 0) return;
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full_bar[s], TC_PRODUCERS + 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(&acc_bar, 1);
+    sh_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 8) {  // TMEM allocation: N fp32 columns (power of two >= 32)
+    constexpr uint32_t ncols = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_sh)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base_sh;
+  const int nk = P.K / TC_KC;
+
+  if (warp < 8) {
+    // ------------------------------------------------------ producers ----
+    const int m = (warp & 3) * 32 + lane;
+    const int h = warp >> 2;
+    const bool valid = m < nrows;
+    const int p = valid ? (P.perm ? P.perm[row0 + m] : row0 + m) : 0;
+    float m2r[HALF];
+    const float* m2row = P.m2_S ? P.m2_ptr + (int64_t)P.m2_S[p] * CHI2
+                                : P.m2_ptr + (int64_t)p * CHI2;
+#pragma unroll
+    for (int j = 0; j < HALF; ++j) {
+      // columns [32h, 32h+32) of every 64-wide block of c
+      int c = (j / 32) * 64 + 32 * h + (j % 32);
+      m2r[j] = valid ? m2row[c] : 0.0f;
+    }
+    const float* m1row = nullptr;
+    if (P.m1_ptr)
+      m1row = P.m1_S ? P.m1_ptr + (int64_t)P.m1_S[p] * P.chi1 : P.m1_ptr + (int64_t)p * P.chi1;
+    const int nb = BILIN ? 1 : P.chi1;
+    const int e_in = valid ? ((P.m1_exp ? P.m1_exp[p] : 0) + (P.m2_exp ? P.m2_exp[p] : 0)) : 0;
+    constexpr int CPB = CHI2 / TC_KC;  // chunks per value of b
+    bool ok = true;
+    for (int bb = 0; bb < nb && ok; ++bb) {
+      const float a1 = (!BILIN && m1row && valid) ? m1row[bb] : (valid ? 1.0f : 0.0f);
+#pragma unroll
+      for (int cblk = 0; cblk < CPB; ++cblk) {
+        const int kc = bb * CPB + cblk;
+        const int s = kc % STAGES, use = kc / STAGES;
+        if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        unsigned char* Ahi = smem + s * STAGE_BYTES;
+        unsigned char* Alo = Ahi + A_BYTES;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {  // 4 x 16-byte chunks of 8 values
+          uint32_t hw[4], lw[4];
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            float x0 = a1 * m2r[cblk * 32 + q * 8 + 2 * t];
+            float x1 = a1 * m2r[cblk * 32 + q * 8 + 2 * t + 1];
+            __nv_bfloat162 hh = __floats2bfloat162_rn(x0, x1);
+            float2 hf = __bfloat1622float2(hh);
+            hw[t] = *reinterpret_cast<uint32_t*>(&hh);
+            lw[t] = pack_bf16(x0 - hf.x, x1 - hf.y);
+          }
+          const int chunk = (4 * h + q) ^ (m & 7);
+          const int off = m * 128 + chunk * 16;
+          *reinterpret_cast<uint4*>(Ahi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+          *reinterpret_cast<uint4*>(Alo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+        fence_proxy_async();
+        mbar_arrive(&full_bar[s]);
+      }
+    }
+    if (!ok) {
+      atomicOr(P.err, TC_ERR_TIMEOUT);
+      sh_abort = 1;
+    }
+    // ------------------------------------------------------- epilogue ----
+    const bool acc_ok = mbar_wait(&acc_bar, 0);
+    if (!acc_ok) {
+      atomicOr(P.err, TC_ERR_TIMEOUT);
+      sh_abort = 1;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    float v[N / 2];
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+#pragma unroll
+    for (int cc = 0; cc < N / 2; cc += 32)
+      tmem_ld32(tmem + lane_base + (uint32_t)(h * (N / 2) + cc), v + cc);
+    if constexpr (BILIN) {
+      // out[p] = sum_b D[p, b] m1[p, b]
+      float part = 0.f;
+      if (valid) {
+        const float* mrow = m1row + h * (N / 2);
+#pragma unroll
+        for (int i = 0; i < N / 2; ++i) part = fmaf(v[i], mrow[i], part);
+      }
+      rowmax[h][m] = part;
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (h == 0 && valid && acc_ok) {
+        const float tot = rowmax[0][m] + rowmax[1][m];
+        int ex = 0;
+        if (tot != 0.f) frexpf(tot, &ex);
+        P.out[p] = scalbnf(tot, -ex);
+        P.out_exp[p] = e_in + ex;
+      }
+    } else {
+      float mx = 0.f;
+#pragma unroll
+      for (int i = 0; i < N / 2; ++i) mx = fmaxf(mx, fabsf(v[i]));
+      rowmax[h][m] = mx;
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      mx = fmaxf(rowmax[0][m], rowmax[1][m]);
+      int ex = 0;
+      if (mx > 0.f) frexpf(mx, &ex);
+      if (valid && acc_ok) {
+        float* dst = P.out + (int64_t)p * N + h * (N / 2);
+#pragma unroll
+        for (int i = 0; i < N / 2; i += 4)
+          *reinterpret_cast<float4*>(dst + i) =
+              make_float4(scalbnf(v[i], -ex), scalbnf(v[i + 1], -ex), scalbnf(v[i + 2], -ex),
+                          scalbnf(v[i + 3], -ex));
+        if (h == 0) P.out_exp[p] = e_in + ex;
+      }
+    }
+  } else if (warp == 8) {
+    // ------------------------------------------------------------ TMA ----
+    if (lane == 0) {
+      bool ok = true;
+      for (int kc = 0; kc < nk; ++kc) {
+        const int s = kc % STAGES, use = kc / STAGES;
+        if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        unsigned char* Bhi = smem + s * STAGE_BYTES + 2 * A_BYTES;
+        unsigned char* Blo = Bhi + B_BYTES;
+        mbar_arrive_expect_tx(&full_bar[s], 2 * B_BYTES);
+        tma_load_2d(Bhi, &map_hi, &full_bar[s], kc * TC_KC, g * N);
+        tma_load_2d(Blo, &map_lo, &full_bar[s], kc * TC_KC, g * N);
+      }
+      if (!ok) atomicOr(P.err, TC_ERR_TIMEOUT);
+    }
+  } else {
+    // ------------------------------------------------------------ MMA ----
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16(TC_M, N);
+      bool ok = true;
+      for (int kc = 0; kc < nk; ++kc) {
+        const int s = kc % STAGES, use = kc / STAGES;
+        if (!mbar_wait(&full_bar[s], use & 1)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        unsigned char* Ahi = smem + s * STAGE_BYTES;
+        unsigned char* Alo = Ahi + A_BYTES;
+        unsigned char* Bhi = Alo + A_BYTES;
+        unsigned char* Blo = Bhi + B_BYTES;
+        const uint64_t dah = sw128_desc(Ahi), dal = sw128_desc(Alo);
+        const uint64_t dbh = sw128_desc(Bhi), dbl = sw128_desc(Blo);
+#pragma unroll
+        for (int k = 0; k < TC_KC / 16; ++k) {
+          const uint64_t adv = (uint64_t)(k * 32) >> 4;  // 16 BF16 along K
+          mma_bf16(tmem, dah + adv, dbh + adv, idesc, (kc | k) != 0);
+          mma_bf16(tmem, dah + adv, dbl + adv, idesc, 1);
+          mma_bf16(tmem, dal + adv, dbh + adv, idesc, 1);
+        }
+        mma_commit(&empty_bar[s]);
+      }
+      if (!ok) atomicOr(P.err, TC_ERR_TIMEOUT);
+      mma_commit(&acc_bar);  // arrives once every issued MMA has completed
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 8) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    constexpr uint32_t ncols = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+  }
+}
+
+// BF16 hi / lo split of the FP32 tensors, per-vertex offsets padded to 64
+// elements so every vertex base is 128-byte aligned for TMA.
+__global__ void k_split_bf16(const float* __restrict__ src, __nv_bfloat16* __restrict__ hi,
+                             __nv_bfloat16* __restrict__ lo, const int64_t* __restrict__ soff,
+                             const int64_t* __restrict__ doff, int V) {
+  const int v = blockIdx.y;
+  const int64_t n = soff[v + 1] - soff[v];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float x = src[soff[v] + i];
+    __nv_bfloat16 h = __float2bfloat16_rn(x);
+    hi[doff[v] + i] = h;
+    lo[doff[v] + i] = __float2bfloat16_rn(x - __bfloat162float(h));
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int box_rows) {
+  auto enc = get_encode();
+  TNFA_CHECK(enc != nullptr, TNFA_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  CUtensorMap m;
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+  cuuint32_t box[2] = {(cuuint32_t)TC_KC, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  TNFA_CHECK(r == CUDA_SUCCESS, TNFA_ERR_CUDA,
+             "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
+  return m;
+}
+
+template <int N, int CHI2, int STAGES, bool BILIN>
+void launch_tc(tnfa_ctx* ctx, const CUtensorMap& mh, const CUtensorMap& ml, const TcParams& p,
+               unsigned grid) {
+  constexpr int STAGE_BYTES = 2 * TC_M * TC_KC * 2 + 2 * N * TC_KC * 2;
+  const int smem = STAGES * STAGE_BYTES + 1024;
+  TNFA_CUDA(cudaFuncSetAttribute(k_contract_tc<N, CHI2, STAGES, BILIN>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  k_contract_tc<N, CHI2, STAGES, BILIN><<<grid, TC_THREADS, smem, ctx->stream>>>(mh, ml, p);
+  TNFA_LAUNCH_CHECK();
+}
+
+struct TcCache {
+  std::vector<int64_t> doff;  // padded offsets of the BF16 copies
+};
+
+}  // namespace
+
+bool tc_vertex_eligible(int nchild, const int* child_dims, int chi_a) {
+  if (nchild < 1 || nchild > 2) return false;
+  const int chi2 = child_dims[nchild - 1];
+  if (chi2 != 64 && chi2 != 128) return false;
+  if (chi_a == 1)  // root of two children: bilinear mode, N = chi1
+    return nchild == 2 && (child_dims[0] == 64 || child_dims[0] == 128);
+  if (chi_a != 64 && chi_a != 128) return false;
+  if (nchild == 2 && (child_dims[0] < 1 || child_dims[0] > 4096)) return false;
+  return true;
+}
+
+int tc_tile_rows() { return TC_M; }
+
+static std::vector<int64_t> padded_offsets(const Topo& T) {
+  std::vector<int64_t> d(T.V + 1, 0);
+  for (int v = 0; v < T.V; ++v) d[v + 1] = d[v] + ((T.size(v) + 63) / 64) * 64;
+  return d;
+}
+
+void tc_prepare_net(tnfa_ctx* ctx, const tnfa_net* net) {
+  if (net->d_bhi) return;
+  const Topo& T = net->topo;
+  const float* src = net->dtype == TNFA_F32 ? (const float*)net->d : (const float*)net->d_f32;
+  TNFA_CHECK(src != nullptr, TNFA_ERR_INVALID_ARGUMENT, "no FP32 tensors for the split");
+  std::vector<int64_t> doff = padded_offsets(T);
+  std::vector<int64_t> soff(T.off.begin(), T.off.end());
+  DBuf ds(ctx, soff.size() * 8), dd(ctx, doff.size() * 8);
+  TNFA_CUDA(cudaMemcpyAsync(ds.p, soff.data(), soff.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  TNFA_CUDA(cudaMemcpyAsync(dd.p, doff.data(), doff.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  net->d_bhi = dalloc(ctx, (size_t)doff[T.V] * 2);
+  net->d_blo = dalloc(ctx, (size_t)doff[T.V] * 2);
+  int64_t maxn = 1;
+  for (int v = 0; v < T.V; ++v) maxn = std::max<int64_t>(maxn, T.size(v));
+  dim3 grid(grid_for(maxn, 256, 2048), T.V);
+  k_split_bf16<<<grid, 256, 0, ctx->stream>>>(src, (__nv_bfloat16*)net->d_bhi,
+                                               (__nv_bfloat16*)net->d_blo, ds.as<int64_t>(),
+                                               dd.as<int64_t>(), T.V);
+  TNFA_LAUNCH_CHECK();
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+void tc_contract_vertex(tnfa_ctx* ctx, const tnfa_net* net, int v, const VertexJob<float>& j,
+                        int tile_rows, int* err) {
+  TNFA_CHECK(tile_rows == TC_M, TNFA_ERR_INVALID_ARGUMENT, "tile rows mismatch");
+  const Topo& T = net->topo;
+  std::vector<int64_t> doff = padded_offsets(T);
+  const __nv_bfloat16* hi = (const __nv_bfloat16*)net->d_bhi + doff[v];
+  const __nv_bfloat16* lo = (const __nv_bfloat16*)net->d_blo + doff[v];
+  const bool bilin = j.chi_a == 1;
+  const int N = bilin ? j.ch[0].dim : j.chi_a;
+  const int K = bilin ? j.ch[1].dim : j.K;
+  CUtensorMap mh = make_map(hi, K, (int64_t)j.site_dim * N, N);
+  CUtensorMap ml = make_map(lo, K, (int64_t)j.site_dim * N, N);
+  TcParams p{};
+  const ChildSrc<float>& c2 = j.ch[j.nchild - 1];
+  p.m2_ptr = c2.ptr;
+  p.m2_exp = c2.exps;
+  p.m2_S = c2.S;
+  p.chi2 = c2.dim;
+  if (j.nchild == 2) {
+    p.m1_ptr = j.ch[0].ptr;
+    p.m1_exp = j.ch[0].exps;
+    p.m1_S = j.ch[0].S;
+    p.chi1 = j.ch[0].dim;
+  } else {
+    p.chi1 = 1;
+  }
+  p.N = N;
+  p.K = K;
+  p.out = j.out;
+  p.out_exp = j.out_exp;
+  p.perm = j.perm;
+  p.grp_off = j.grp_off;
+  p.grp_cnt = j.grp_cnt;
+  p.tile_start = j.tile_start;
+  p.ngroups = j.ngroups;
+  p.err = err;
+  const unsigned grid = (unsigned)((j.Pc + TC_M - 1) / TC_M + j.ngroups);
+  KernelScope ks(ctx, "contract_tc", 2.0 * j.Pc * (double)j.K * j.chi_a,
+                 4.0 * ((double)j.Pc * (p.chi1 + p.chi2 + j.chi_a)) +
+                     4.0 * j.site_dim * (double)j.chi_a * j.K);
+  if (!bilin) {
+    if (N == 128 && p.chi2 == 128) launch_tc<128, 128, 3, false>(ctx, mh, ml, p, grid);
+    else if (N == 128 && p.chi2 == 64) launch_tc<128, 64, 3, false>(ctx, mh, ml, p, grid);
+    else if (N == 64 && p.chi2 == 128) launch_tc<64, 128, 4, false>(ctx, mh, ml, p, grid);
+    else if (N == 64 && p.chi2 == 64) launch_tc<64, 64, 4, false>(ctx, mh, ml, p, grid);
+    else fail(TNFA_ERR_UNSUPPORTED, "tensor-core shape");
+  } else {
+    if (N == 128 && p.chi2 == 128) launch_tc<128, 128, 3, true>(ctx, mh, ml, p, grid);
+    else if (N == 128 && p.chi2 == 64) launch_tc<128, 64, 3, true>(ctx, mh, ml, p, grid);
+    else if (N == 64 && p.chi2 == 128) launch_tc<64, 128, 4, true>(ctx, mh, ml, p, grid);
+    else if (N == 64 && p.chi2 == 64) launch_tc<64, 64, 4, true>(ctx, mh, ml, p, grid);
+    else fail(TNFA_ERR_UNSUPPORTED, "tensor-core shape");
+  }
 }
 
 }  // namespace tnfa

@@ -53,7 +53,7 @@ def test_random_network_f32_paths(ina, precision):
     got = np.ldexp(m, e)
     err = np.abs(got - ref) / np.abs(ref)
     assert np.median(err) < TOL_F32
-    # values underflow plain FP32 here; the scaled output keeps them
+    # the scaled output is finite and nonzero for every point
     assert np.all(np.isfinite(got)) and np.all(got != 0)
 
 
@@ -244,3 +244,32 @@ def test_deep_tree_underflow_is_scaled(ina):
     assert rel_err(got[:16], ref) < 1e-11
     m, e = f.evaluate_batch(X, [1, 2, 3], precision="f32", out="f32_scaled")
     assert np.median(np.abs(np.ldexp(m, e) - got) / np.abs(got)) < TOL_F32
+
+
+@pytest.mark.parametrize("graph_name,chi", [("binary7", 128), ("binary15", 64), ("path6", 128)])
+def test_tensor_core_path(ina, graph_name, chi):
+    """The tcgen05 split-BF16 contraction (chi in {64, 128}; the binary trees'
+    roots use the bilinear mode) against the FP64 path on the same tensors.
+    Split BF16 x3 leaves ~2^-17 per product; random trees amplify it by their
+    depth, so the norm-wise bound is 3e-4."""
+    graph = {"binary7": O.binary_tree_graph(7), "binary15": O.binary_tree_graph(15),
+             "path6": O.path_graph(6)}[graph_name]
+    rng = np.random.default_rng(chi)
+    s_or = O.siteinds(graph, map_dimension=3 if graph_name != "path6" else 1)
+    net = O.random_net(s_or, chi, rng, normalize=True)
+    f, _ = upload_oracle(ina, graph, net)
+    nd = len(s_or.dims())
+    X = rng.random((3000, nd))
+    dims = list(range(1, nd + 1))
+    ctx = f.ctx
+    ctx.kernel_stats(reset=True)
+    m, e = f.evaluate_batch(X, dims, precision="mixed", out="f32_scaled")
+    st = ctx.kernel_stats(reset=True)
+    assert st.get("contract_tc", {}).get("launches", 0) > 0, st
+    got = np.ldexp(m, e)
+    ref = f.evaluate_batch(X, dims, precision="f64")
+    nrm = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert nrm < 3e-4, nrm
+    assert np.median(np.abs(got - ref) / np.abs(ref)) < 3e-4
+    if graph_name != "path6":
+        assert st.get("contract_f32", {}).get("launches", 0) == 0, st
