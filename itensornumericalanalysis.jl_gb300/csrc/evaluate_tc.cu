@@ -234,8 +234,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int e_in = valid ? ((P.m1_exp ? P.m1_exp[p] : 0) + (P.m2_exp ? P.m2_exp[p] : 0)) : 0;
     constexpr int CPB = CHI2 / TC_KC;  // chunks per value of b
     bool ok = true;
+    // m1[p, b] is consumed once per b; it is loaded four at a time one group
+    // ahead so the global-load latency hides behind the previous group.
+    const bool use_m1 = !BILIN && m1row && valid;
+    const bool vec4 = use_m1 && (P.chi1 % 4 == 0);
+    float4 grp = make_float4(1.f, 1.f, 1.f, 1.f), nxt = grp;
+    if (vec4) nxt = *reinterpret_cast<const float4*>(m1row);
     for (int bb = 0; bb < nb && ok; ++bb) {
-      const float a1 = (!BILIN && m1row && valid) ? m1row[bb] : (valid ? 1.0f : 0.0f);
+      float a1;
+      if (vec4) {
+        if ((bb & 3) == 0) {
+          grp = nxt;
+          if (bb + 4 < nb) nxt = *reinterpret_cast<const float4*>(m1row + bb + 4);
+        }
+        const int q4 = bb & 3;
+        a1 = q4 == 0 ? grp.x : q4 == 1 ? grp.y : q4 == 2 ? grp.z : grp.w;
+      } else {
+        a1 = use_m1 ? m1row[bb] : (valid ? 1.0f : 0.0f);
+      }
 #pragma unroll
       for (int cblk = 0; cblk < CPB; ++cblk) {
         const int kc = bb * CPB + cblk;

@@ -1,0 +1,465 @@
+// Batched dense linear algebra kernels (FP64 real and complex128).
+//
+//   permute  : general tensor transpose (up to 10 axes)
+//   gemm     : tiled SIMT GEMM, 64x64 tiles, op(A) op(B) with N/T/C
+//   qr       : Householder QR, one CTA per matrix, column-major workspace
+//   svd      : one-sided Jacobi (Hestenes) SVD, round-robin pair ordering,
+//              one CTA per matrix, columns contiguous in the workspace
+// Every problem of a batch may have its own shape; one launch covers them all.
+#include <algorithm>
+#include <cmath>
+
+#include "linalg.cuh"
+
+namespace tnfa {
+namespace la {
+
+// ---------------------------------------------------------- scalar ops --
+__host__ __device__ inline double re(double x) { return x; }
+__host__ __device__ inline double re(cplx x) { return x.re; }
+__host__ __device__ inline double abs2(double x) { return x * x; }
+__host__ __device__ inline double abs2(cplx x) { return x.re * x.re + x.im * x.im; }
+__host__ __device__ inline double conj(double x) { return x; }
+__host__ __device__ inline cplx conj(cplx x) { return {x.re, -x.im}; }
+__host__ __device__ inline double scal(double x, double a) { return x * a; }
+__host__ __device__ inline cplx scal(cplx x, double a) { return {x.re * a, x.im * a}; }
+template <class T> __host__ __device__ inline T from_real(double a);
+template <> __host__ __device__ inline double from_real<double>(double a) { return a; }
+template <> __host__ __device__ inline cplx from_real<cplx>(double a) { return {a, 0.0}; }
+__device__ inline double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ inline cplx shfl_xor(cplx v, int o) {
+  return {__shfl_xor_sync(0xffffffffu, v.re, o), __shfl_xor_sync(0xffffffffu, v.im, o)};
+}
+template <class T>
+__device__ inline T warp_sum(T v) {
+  for (int o = 16; o; o >>= 1) v = v + shfl_xor(v, o);
+  return v;
+}
+// x / |x| (1 for x = 0)
+__device__ inline double phase(double x) { return x < 0 ? -1.0 : 1.0; }
+__device__ inline cplx phase(cplx x) {
+  double a = sqrt(abs2(x));
+  return a > 0 ? cplx{x.re / a, x.im / a} : cplx{1.0, 0.0};
+}
+
+template <class Job>
+static DBuf upload(tnfa_ctx* ctx, const std::vector<Job>& jobs) {
+  DBuf d(ctx, jobs.size() * sizeof(Job));
+  TNFA_CUDA(cudaMemcpyAsync(d.p, jobs.data(), jobs.size() * sizeof(Job), cudaMemcpyHostToDevice,
+                            ctx->stream));
+  return d;
+}
+
+// ------------------------------------------------------------- permute --
+template <class T>
+__global__ void k_permute(const PermJob* __restrict__ jobs) {
+  const PermJob& jb = jobs[blockIdx.y];
+  int64_t sstride[MAXD];
+  int64_t st = 1;
+  for (int a = jb.nd - 1; a >= 0; --a) {
+    sstride[a] = st;
+    st *= jb.shape[a];
+  }
+  const T* src = (const T*)jb.src;
+  T* dst = (T*)jb.dst;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < jb.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = i, si = 0;
+    for (int a = jb.nd - 1; a >= 0; --a) {
+      const int sa = jb.perm[a];
+      const int64_t x = r % jb.shape[sa];
+      r /= jb.shape[sa];
+      si += x * sstride[sa];
+    }
+    dst[i] = src[si];
+  }
+}
+
+template <class T>
+void permute(tnfa_ctx* ctx, const std::vector<PermJob>& jobs) {
+  if (jobs.empty()) return;
+  int64_t nmax = 1;
+  for (const auto& j : jobs) nmax = std::max(nmax, j.n);
+  TNFA_CHECK(jobs.size() <= 65535, TNFA_ERR_UNSUPPORTED, "permute batch too large");
+  DBuf d = upload(ctx, jobs);
+  dim3 grid(grid_for(nmax, 256, 2048), (unsigned)jobs.size());
+  KernelScope ks(ctx, "permute", 0.0, 2.0 * sizeof(T) * nmax * jobs.size());
+  k_permute<T><<<grid, 256, 0, ctx->stream>>>(d.as<PermJob>());
+  TNFA_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------- gemm --
+template <class T>
+__device__ inline T opget(const T* X, int ld, int op, int r, int c) {
+  // element (r, c) of op(X)
+  if (op == 0) return X[(int64_t)r * ld + c];
+  T v = X[(int64_t)c * ld + r];
+  return op == 2 ? conj(v) : v;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_gemm(const GemmJob* __restrict__ jobs) {
+  constexpr int BM = 64, BN = 64, BK = 16;
+  const GemmJob& jb = jobs[blockIdx.z];
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  if (m0 >= jb.m || n0 >= jb.n) return;
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
+  const T* A = (const T*)jb.A;
+  const T* B = (const T*)jb.B;
+  T* C = (T*)jb.C;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = from_real<T>(0.0);
+  for (int k0 = 0; k0 < jb.k; k0 += BK) {
+    for (int idx = threadIdx.x; idx < BM * BK; idx += 256) {
+      int r, kk;
+      if (jb.opA == 0) { r = idx / BK; kk = idx % BK; }   // contiguous along k
+      else { kk = idx / BM; r = idx % BM; }              // contiguous along m
+      const int gr = m0 + r, gk = k0 + kk;
+      As[kk][r] = (gr < jb.m && gk < jb.k) ? opget(A, jb.lda, jb.opA, gr, gk) : from_real<T>(0.0);
+    }
+    for (int idx = threadIdx.x; idx < BN * BK; idx += 256) {
+      int c, kk;
+      if (jb.opB == 0) { kk = idx / BN; c = idx % BN; }   // contiguous along n
+      else { c = idx / BK; kk = idx % BK; }              // contiguous along k
+      const int gc = n0 + c, gk = k0 + kk;
+      Bs[kk][c] = (gc < jb.n && gk < jb.k) ? opget(B, jb.ldb, jb.opB, gk, gc) : from_real<T>(0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = Sc<T>::fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = m0 + ty + 16 * i;
+    if (r >= jb.m) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = n0 + tx + 16 * j;
+      if (c >= jb.n) continue;
+      T v = scal(acc[i][j], jb.alpha);
+      T* cp = C + (int64_t)r * jb.ldc + c;
+      *cp = jb.beta == 0.0 ? v : v + scal(*cp, jb.beta);
+    }
+  }
+}
+
+template <class T>
+void gemm(tnfa_ctx* ctx, const std::vector<GemmJob>& jobs) {
+  if (jobs.empty()) return;
+  int mt = 1, nt = 1;
+  double fl = 0;
+  for (const auto& j : jobs) {
+    mt = std::max(mt, (j.m + 63) / 64);
+    nt = std::max(nt, (j.n + 63) / 64);
+    fl += 2.0 * j.m * j.n * j.k;
+  }
+  TNFA_CHECK(jobs.size() <= 65535 && mt <= 65535, TNFA_ERR_UNSUPPORTED, "gemm batch too large");
+  DBuf d = upload(ctx, jobs);
+  dim3 grid(nt, mt, (unsigned)jobs.size());
+  KernelScope ks(ctx, sizeof(T) == 8 ? "gemm_f64" : "gemm_c128", fl, 0.0);
+  k_gemm<T><<<grid, 256, 0, ctx->stream>>>(d.as<GemmJob>());
+  TNFA_LAUNCH_CHECK();
+}
+
+// ------------------------------------------------------------------ qr --
+template <class T>
+__device__ inline T block_sum(T v, T* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    T t = lane < nw ? red[lane] : from_real<T>(0.0);
+    t = warp_sum(t);
+    if (lane == 0) red[0] = t;
+  }
+  __syncthreads();
+  T r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// Workspace per job: A copied column-major into W (m*n), Q column-major
+// into Qw (m*kq); reflector j is stored in W column j rows j..m-1.
+template <class T>
+__global__ void __launch_bounds__(512) k_qr(const QrJob* __restrict__ jobs, T* __restrict__ work,
+                                            const int64_t* __restrict__ woff) {
+  const QrJob jb = jobs[blockIdx.x];
+  const int m = jb.m, n = jb.n, kq = min(m, n);
+  T* W = work + woff[blockIdx.x];
+  T* Qw = W + (int64_t)m * n;
+  T* tau = (T*)jb.tau;
+  const T* A = (const T*)jb.A;
+  __shared__ T red[32];
+  __shared__ T alpha_sh;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) {
+    const int r = (int)(i / n), c = (int)(i % n);
+    W[(int64_t)c * m + r] = A[i];
+  }
+  __syncthreads();
+  T* R = (T*)jb.R;
+  for (int j = 0; j < kq; ++j) {
+    T* x = W + (int64_t)j * m;
+    double part = 0.0;
+    for (int r = j + threadIdx.x; r < m; r += blockDim.x) part += abs2(x[r]);
+    const double nrm2 = re(block_sum<T>(from_real<T>(part), red));
+    if (threadIdx.x == 0) {
+      const T x0 = x[j];
+      const double nrm = sqrt(nrm2);
+      const T alpha = scal(phase(x0), -nrm);
+      const T v0 = x0 - alpha;
+      const double vn2 = nrm2 - abs2(x0) + abs2(v0);
+      tau[j] = from_real<T>(vn2 > 0.0 ? 2.0 / vn2 : 0.0);
+      x[j] = v0;
+      alpha_sh = alpha;
+    }
+    __syncthreads();
+    const double beta = re(tau[j]);
+    const T alpha = alpha_sh;
+    if (beta != 0.0) {
+      for (int c = j + 1 + warp; c < n; c += nw) {
+        T* y = W + (int64_t)c * m;
+        T w = from_real<T>(0.0);
+        for (int r = j + lane; r < m; r += 32) w = Sc<T>::fma(conj(x[r]), y[r], w);
+        w = warp_sum(w);
+        const T bw = scal(w, beta);
+        for (int r = j + lane; r < m; r += 32) y[r] = y[r] - x[r] * bw;
+      }
+    }
+    __syncthreads();
+    // R row j: diagonal alpha, then the updated row j of the trailing block
+    for (int c = threadIdx.x; c < n; c += blockDim.x)
+      R[(int64_t)j * n + c] = c < j ? from_real<T>(0.0) : (c == j ? alpha : W[(int64_t)c * m + j]);
+    __syncthreads();
+  }
+  // Q = H_0 ... H_{kq-1} [I; 0]
+  for (int64_t i = threadIdx.x; i < (int64_t)m * kq; i += blockDim.x) {
+    const int c = (int)(i / m), r = (int)(i % m);
+    Qw[i] = from_real<T>(r == c ? 1.0 : 0.0);
+  }
+  __syncthreads();
+  for (int j = kq - 1; j >= 0; --j) {
+    const double beta = re(tau[j]);
+    if (beta != 0.0) {
+      const T* x = W + (int64_t)j * m;
+      for (int c = j + warp; c < kq; c += nw) {
+        T* y = Qw + (int64_t)c * m;
+        T w = from_real<T>(0.0);
+        for (int r = j + lane; r < m; r += 32) w = Sc<T>::fma(conj(x[r]), y[r], w);
+        w = warp_sum(w);
+        const T bw = scal(w, beta);
+        for (int r = j + lane; r < m; r += 32) y[r] = y[r] - x[r] * bw;
+      }
+    }
+    __syncthreads();
+  }
+  T* Q = (T*)jb.Q;
+  for (int64_t i = threadIdx.x; i < (int64_t)m * kq; i += blockDim.x) {
+    const int r = (int)(i / kq), c = (int)(i % kq);
+    Q[i] = Qw[(int64_t)c * m + r];
+  }
+}
+
+template <class T>
+void qr(tnfa_ctx* ctx, const std::vector<QrJob>& jobs) {
+  if (jobs.empty()) return;
+  std::vector<int64_t> woff(jobs.size() + 1, 0);
+  double fl = 0;
+  for (size_t i = 0; i < jobs.size(); ++i) {
+    const int64_t m = jobs[i].m, n = jobs[i].n, k = std::min(m, n);
+    woff[i + 1] = woff[i] + m * n + m * k;
+    fl += 4.0 * m * n * k;
+  }
+  DBuf work(ctx, (size_t)woff.back() * sizeof(T));
+  DBuf dw = upload(ctx, woff);
+  DBuf d = upload(ctx, jobs);
+  KernelScope ks(ctx, sizeof(T) == 8 ? "qr_f64" : "qr_c128", fl, 0.0);
+  k_qr<T><<<(unsigned)jobs.size(), 512, 0, ctx->stream>>>(d.as<QrJob>(), work.as<T>(),
+                                                          dw.as<int64_t>());
+  TNFA_LAUNCH_CHECK();
+}
+
+// ----------------------------------------------------------------- svd --
+// Round-robin pairing of n2 (even) players: round r, slot i.
+__device__ inline void rr_pair(int n2, int r, int i, int& p, int& q) {
+  if (i == 0) {
+    p = n2 - 1;
+    q = r;
+  } else {
+    p = (r + i) % (n2 - 1);
+    q = (r - i + (n2 - 1)) % (n2 - 1);
+  }
+  if (p > q) {
+    int t = p;
+    p = q;
+    q = t;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(512) k_svd(const SvdJob* __restrict__ jobs, T* __restrict__ work,
+                                             const int64_t* __restrict__ woff, int max_sweeps) {
+  const SvdJob jb = jobs[blockIdx.x];
+  const int m = jb.m, n = jb.n;
+  T* U = work + woff[blockIdx.x];     // column-major m x n (columns contiguous)
+  T* V = U + (int64_t)m * n;          // column-major n x n
+  double* sig = (double*)(V + (int64_t)n * n);
+  int* rank = (int*)(sig + n);
+  const T* A = (const T*)jb.A;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __shared__ int rotated;
+  for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) {
+    const int r = (int)(i / n), c = (int)(i % n);
+    U[(int64_t)c * m + r] = A[i];
+  }
+  for (int64_t i = threadIdx.x; i < (int64_t)n * n; i += blockDim.x)
+    V[i] = from_real<T>((i / n) == (i % n) ? 1.0 : 0.0);
+  __syncthreads();
+  const int n2 = (n + 1) & ~1;
+  int sweep = 0;
+  bool converged = (n < 2);
+  const double tol = 1e-15;
+  while (!converged && sweep < max_sweeps) {
+    if (threadIdx.x == 0) rotated = 0;
+    __syncthreads();
+    for (int r = 0; r < n2 - 1; ++r) {
+      for (int slot = warp; slot < n2 / 2; slot += nw) {
+        int p, q;
+        rr_pair(n2, r, slot, p, q);
+        if (q >= n) continue;
+        T* up = U + (int64_t)p * m;
+        T* uq = U + (int64_t)q * m;
+        double a = 0.0, b = 0.0;
+        T g = from_real<T>(0.0);
+        for (int i = lane; i < m; i += 32) {
+          a += abs2(up[i]);
+          b += abs2(uq[i]);
+          g = Sc<T>::fma(conj(up[i]), uq[i], g);
+        }
+        a = warp_sum(a);
+        b = warp_sum(b);
+        g = warp_sum(g);
+        const double ag = sqrt(abs2(g));
+        if (ag <= tol * sqrt(a * b) || ag == 0.0) continue;
+        const double zeta = (b - a) / (2.0 * ag);
+        const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+        const T e = phase(g);  // g / |g|
+        const T se = scal(e, s), sec = scal(conj(e), s);
+        for (int i = lane; i < m; i += 32) {
+          const T xp = up[i], xq = uq[i];
+          up[i] = scal(xp, c) - sec * xq;
+          uq[i] = se * xp + scal(xq, c);
+        }
+        T* vp = V + (int64_t)p * n;
+        T* vq = V + (int64_t)q * n;
+        for (int i = lane; i < n; i += 32) {
+          const T xp = vp[i], xq = vq[i];
+          vp[i] = scal(xp, c) - sec * xq;
+          vq[i] = se * xp + scal(xq, c);
+        }
+        if (lane == 0) rotated = 1;
+      }
+      __syncthreads();
+    }
+    ++sweep;
+    converged = (rotated == 0);
+    __syncthreads();
+  }
+  // singular values, ranks (descending, stable), normalised outputs
+  for (int c = warp; c < n; c += nw) {
+    double s2 = 0.0;
+    for (int i = lane; i < m; i += 32) s2 += abs2(U[(int64_t)c * m + i]);
+    s2 = warp_sum(s2);
+    if (lane == 0) sig[c] = sqrt(s2);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+    int rk = 0;
+    for (int d = 0; d < n; ++d) rk += (sig[d] > sig[c]) || (sig[d] == sig[c] && d < c);
+    rank[c] = rk;
+    jb.S[rk] = sig[c];
+  }
+  __syncthreads();
+  T* Uo = (T*)jb.U;
+  T* Vo = (T*)jb.V;
+  for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) {
+    const int c = (int)(i / m), r = (int)(i % m);
+    const double s = sig[c];
+    Uo[(int64_t)r * n + rank[c]] = s > 0 ? scal(U[i], 1.0 / s) : from_real<T>(0.0);
+  }
+  for (int64_t i = threadIdx.x; i < (int64_t)n * n; i += blockDim.x) {
+    const int c = (int)(i / n), r = (int)(i % n);
+    Vo[(int64_t)r * n + rank[c]] = V[i];
+  }
+  if (threadIdx.x == 0 && jb.sweeps) *jb.sweeps = converged ? sweep : -1;
+}
+
+template <class T>
+void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
+  if (jobs.empty()) return;
+  std::vector<int64_t> woff(jobs.size() + 1, 0);
+  double fl = 0;
+  for (size_t i = 0; i < jobs.size(); ++i) {
+    TNFA_CHECK(jobs[i].m >= jobs[i].n, TNFA_ERR_INVALID_ARGUMENT, "svd needs m >= n");
+    const int64_t m = jobs[i].m, n = jobs[i].n;
+    // U, V in T; sig (n doubles) and rank (n ints) rounded up to T slots
+    woff[i + 1] = woff[i] + m * n + n * n + (int64_t)((n * 12 + sizeof(T) - 1) / sizeof(T)) + 1;
+    fl += 6.0 * m * n * n * 8;  // ~8 sweeps
+  }
+  DBuf work(ctx, (size_t)woff.back() * sizeof(T));
+  DBuf dw = upload(ctx, woff);
+  DBuf d = upload(ctx, jobs);
+  KernelScope ks(ctx, sizeof(T) == 8 ? "svd_f64" : "svd_c128", fl, 0.0);
+  k_svd<T><<<(unsigned)jobs.size(), 512, 0, ctx->stream>>>(d.as<SvdJob>(), work.as<T>(),
+                                                           dw.as<int64_t>(), max_sweeps);
+  TNFA_LAUNCH_CHECK();
+}
+
+int truncation_rank(const double* s, int n, double cutoff, int maxdim, int mindim) {
+  if (n <= 0) return 0;
+  double total = 0.0;
+  for (int i = 0; i < n; ++i) total += s[i] * s[i];
+  int r = n;
+  if (total > 0.0 && cutoff > 0.0) {
+    double dropped = 0.0;
+    while (r > 1 && dropped + s[r - 1] * s[r - 1] <= cutoff * total) {
+      dropped += s[r - 1] * s[r - 1];
+      --r;
+    }
+  }
+  if (maxdim > 0) r = std::min(r, maxdim);
+  r = std::max(r, std::min(std::max(mindim, 1), n));
+  return r;
+}
+
+template void permute<double>(tnfa_ctx*, const std::vector<PermJob>&);
+template void permute<cplx>(tnfa_ctx*, const std::vector<PermJob>&);
+template void permute<float>(tnfa_ctx*, const std::vector<PermJob>&);
+template void gemm<double>(tnfa_ctx*, const std::vector<GemmJob>&);
+template void gemm<cplx>(tnfa_ctx*, const std::vector<GemmJob>&);
+template void qr<double>(tnfa_ctx*, const std::vector<QrJob>&);
+template void qr<cplx>(tnfa_ctx*, const std::vector<QrJob>&);
+template void svd<double>(tnfa_ctx*, const std::vector<SvdJob>&, int);
+template void svd<cplx>(tnfa_ctx*, const std::vector<SvdJob>&, int);
+
+}  // namespace la
+}  // namespace tnfa

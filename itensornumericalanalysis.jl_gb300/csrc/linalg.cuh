@@ -1,0 +1,69 @@
+// Batched dense linear algebra on the device (row-major matrices).  Every
+// routine takes a vector of independent problems of possibly different sizes
+// and runs them in one launch (one CTA, or one CTA tile set, per problem).
+#pragma once
+#include "common.cuh"
+
+namespace tnfa {
+namespace la {
+
+constexpr int MAXD = 10;  // tensor order handled by permute
+
+// dst = transpose of src: dst axis i is src axis perm[i].
+struct PermJob {
+  const void* src;
+  void* dst;
+  int nd;
+  int shape[MAXD];  // src shape
+  int perm[MAXD];
+  int64_t n;
+};
+template <class T>
+void permute(tnfa_ctx* ctx, const std::vector<PermJob>& jobs);
+
+// C = alpha * op(A) * op(B) + beta * C; op(X) = X, X^T or X^H (conj).
+struct GemmJob {
+  const void* A;
+  const void* B;
+  void* C;
+  int m, n, k;
+  int lda, ldb, ldc;
+  int opA, opB;  // 0: N, 1: T, 2: C (conjugate transpose)
+  double alpha, beta;
+};
+template <class T>
+void gemm(tnfa_ctx* ctx, const std::vector<GemmJob>& jobs);
+
+// Householder QR of A (m x n, lda = n, destroyed): Q (m x kq, kq = min(m, n))
+// and R (kq x n) written to separate buffers.
+struct QrJob {
+  void* A;
+  void* Q;
+  void* R;
+  void* tau;  // kq scalars of workspace
+  int m, n;
+};
+template <class T>
+void qr(tnfa_ctx* ctx, const std::vector<QrJob>& jobs);
+
+// One-sided Jacobi SVD of A (m x n, m >= n, lda = n, destroyed):
+// A = U diag(S) V^H with U (m x n, orthonormal columns where S > 0), S (n,
+// real, descending), V (n x n).  conv receives the sweep count, or -1 when
+// the sweep cap was reached.
+struct SvdJob {
+  void* A;
+  void* U;
+  double* S;
+  void* V;
+  int m, n;
+  int* sweeps;
+};
+template <class T>
+void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps = 60);
+
+// Rank kept by the reference truncation rule: smallest r >= mindim with
+// sum_{i >= r} s_i^2 <= cutoff * sum s_i^2, capped by maxdim (> 0).
+int truncation_rank(const double* s, int n, double cutoff, int maxdim, int mindim);
+
+}  // namespace la
+}  // namespace tnfa

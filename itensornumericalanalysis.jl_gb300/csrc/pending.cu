@@ -12,30 +12,9 @@ using namespace tnfa;
 
 extern "C" {
 
-int tnfa_integrate_operator(tnfa_ctx* ctx, const tnfa_net*, const tnfa_net*, int, double*) {
-  TNFA_PENDING("tnfa_integrate_operator")
-}
 int tnfa_partial_integrate(tnfa_ctx* ctx, const tnfa_net*, int32_t, const int32_t*, int,
                            tnfa_net**) {
   TNFA_PENDING("tnfa_partial_integrate")
-}
-int tnfa_apply(tnfa_ctx* ctx, const tnfa_net*, const tnfa_net*, const tnfa_trunc_params*,
-               tnfa_net**) {
-  TNFA_PENDING("tnfa_apply")
-}
-int tnfa_apply_batched(tnfa_ctx* ctx, int32_t, const tnfa_net* const*, const tnfa_net* const*,
-                       const tnfa_trunc_params*, tnfa_net**) {
-  TNFA_PENDING("tnfa_apply_batched")
-}
-int tnfa_truncate(tnfa_ctx* ctx, const tnfa_net*, const tnfa_trunc_params*, tnfa_net**) {
-  TNFA_PENDING("tnfa_truncate")
-}
-int tnfa_truncate_batched(tnfa_ctx* ctx, int32_t, const tnfa_net* const*, const tnfa_trunc_params*,
-                          tnfa_net**) {
-  TNFA_PENDING("tnfa_truncate_batched")
-}
-int tnfa_inner(tnfa_ctx* ctx, const tnfa_net*, const tnfa_net*, double*) {
-  TNFA_PENDING("tnfa_inner")
 }
 int tnfa_linsolve(tnfa_ctx* ctx, const tnfa_net*, const tnfa_net*, const tnfa_net*,
                   const tnfa_linsolve_params*, tnfa_net**, double*) {

@@ -1,0 +1,745 @@
+// Tree tensor network algorithms on the device: operator application,
+// orthogonalisation and truncation, inner products, integral of O f.
+//
+// Reference: operate (src/elementary_operators.jl:294-319) hands O and f to
+// ITensorNetworks.contract(...; alg="fit", init=f), a variational fit that
+// starts from f's bond dimensions; truncate (src/itensornetworkfunction.jl:
+// 114-118) calls ITensorNetworks.truncate (QR toward a root, SVD per bond with
+// a relative discarded-weight cutoff).  Here O f is formed exactly (bond dims
+// multiply) and then truncated -- the result the fit converges to.
+//
+// Truncation of a tree: (1) QR every vertex toward its root, children first;
+// (2) depth-first from the root: at vertex v (the orthogonality centre) SVD
+// the bond to child c, keep the rank allowed by cutoff / maxdim, move the
+// centre into c (S V^H absorbed), recurse, then QR c back toward v.  Every
+// SVD therefore sees the exact Schmidt spectrum of its bond.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "evaluate.cuh"
+#include "linalg.cuh"
+
+namespace tnfa {
+
+tnfa_net* site_reduced_net(tnfa_ctx* ctx, const tnfa_net* net, int take_sum);  // integrate.cu
+
+namespace {
+
+inline double habs2(double x) { return x * x; }
+inline double habs2(cplx x) { return x.re * x.re + x.im * x.im; }
+template <class T> inline T hreal(double a);
+template <> inline double hreal<double>(double a) { return a; }
+template <> inline cplx hreal<cplx>(double a) { return {a, 0.0}; }
+__device__ inline double dconj(double x) { return x; }
+__device__ inline cplx dconj(cplx x) { return {x.re, -x.im}; }
+
+template <class T>
+__global__ void k_copy2d(T* __restrict__ dst, int ldd, const T* __restrict__ src, int lds,
+                         int rows, int cols, int conjugate) {
+  const int64_t n = (int64_t)rows * cols;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / cols, c = i % cols;
+    T v = src[r * lds + c];
+    dst[r * ldd + c] = conjugate ? dconj(v) : v;
+  }
+}
+
+template <class T>
+void copy2d(tnfa_ctx* ctx, void* dst, int ldd, const void* src, int lds, int rows, int cols,
+            bool conjugate) {
+  k_copy2d<T><<<grid_for((int64_t)rows * cols, 256, 4096), 256, 0, ctx->stream>>>(
+      (T*)dst, ldd, (const T*)src, lds, rows, cols, conjugate ? 1 : 0);
+  TNFA_LAUNCH_CHECK();
+}
+
+__device__ inline double dmul(double x, double s) { return x * s; }
+__device__ inline cplx dmul(cplx x, double s) { return {x.re * s, x.im * s}; }
+
+template <class T>
+__global__ void k_scale_by(T* x, int64_t n, double s) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = dmul(x[i], s);
+}
+
+template <class T>
+struct Work {
+  tnfa_ctx* ctx;
+  Topo topo;
+  std::vector<DBuf> t;  // per-vertex tensors, canonical layout
+
+  std::vector<int> shape(int v) const {
+    std::vector<int> s{topo.site_dim[v], topo.link[v]};
+    for (int c : topo.children[v]) s.push_back(topo.link[c]);
+    return s;
+  }
+  int64_t size(int v) const {
+    int64_t n = 1;
+    for (int d : shape(v)) n *= d;
+    return n;
+  }
+  int child_axis(int v, int c) const {
+    const auto& ch = topo.children[v];
+    return 2 + (int)(std::find(ch.begin(), ch.end(), c) - ch.begin());
+  }
+};
+
+template <class T>
+Work<T> load_work(tnfa_ctx* ctx, const tnfa_net* net) {
+  Work<T> w{ctx, net->topo, {}};
+  w.t.reserve(net->topo.V);
+  for (int v = 0; v < net->topo.V; ++v) {
+    const int64_t n = net->topo.size(v);
+    w.t.emplace_back(ctx, (size_t)n * sizeof(T));
+    TNFA_CUDA(cudaMemcpyAsync(w.t.back().p, (const T*)net->d + net->topo.off[v], n * sizeof(T),
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  return w;
+}
+
+template <class T>
+tnfa_net* store_work(Work<T>& w, int dtype) {
+  w.topo.finalize();
+  tnfa_net* out = new_net(w.ctx, w.topo, dtype);
+  for (int v = 0; v < w.topo.V; ++v)
+    TNFA_CUDA(cudaMemcpyAsync((T*)out->d + w.topo.off[v], w.t[v].p, w.size(v) * sizeof(T),
+                              cudaMemcpyDeviceToDevice, w.ctx->stream));
+  return out;
+}
+
+// dst = src with axis `ax` moved to position `to` (dims `shp`).
+template <class T>
+void move_axis(tnfa_ctx* ctx, const void* src, void* dst, const std::vector<int>& shp, int ax,
+               int to) {
+  la::PermJob j{};
+  j.src = src;
+  j.dst = dst;
+  j.nd = (int)shp.size();
+  TNFA_CHECK(j.nd <= la::MAXD, TNFA_ERR_UNSUPPORTED, "tensor order above 10");
+  std::vector<int> order(j.nd);
+  std::iota(order.begin(), order.end(), 0);
+  order.erase(order.begin() + ax);
+  order.insert(order.begin() + to, ax);
+  j.n = 1;
+  for (int a = 0; a < j.nd; ++a) {
+    j.shape[a] = shp[a];
+    j.perm[a] = order[a];
+    j.n *= shp[a];
+  }
+  if (ax == to) {
+    TNFA_CUDA(cudaMemcpyAsync(dst, src, j.n * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+    return;
+  }
+  la::permute<T>(ctx, {j});
+}
+
+// T_v <- M x_ax T_v : contract axis `ax` of v's tensor with the columns of M
+// (newdim x shape[ax]).
+template <class T>
+void absorb(Work<T>& w, int v, int ax, const void* M, int newdim) {
+  tnfa_ctx* ctx = w.ctx;
+  std::vector<int> shp = w.shape(v);
+  const int old = shp[ax];
+  const int64_t rest = w.size(v) / old;
+  DBuf a(ctx, (size_t)w.size(v) * sizeof(T));
+  move_axis<T>(ctx, w.t[v].p, a.p, shp, ax, 0);  // [old][rest]
+  DBuf b(ctx, (size_t)newdim * rest * sizeof(T));
+  la::GemmJob g{M, a.p, b.p, newdim, (int)rest, old, old, (int)rest, (int)rest, 0, 0, 1.0, 0.0};
+  la::gemm<T>(ctx, {g});
+  std::vector<int> nshp = shp;
+  nshp.erase(nshp.begin() + ax);
+  nshp.insert(nshp.begin(), newdim);  // current layout [newdim][rest...]
+  DBuf c(ctx, (size_t)newdim * rest * sizeof(T));
+  move_axis<T>(ctx, b.p, c.p, nshp, 0, ax);
+  w.t[v] = std::move(c);
+}
+
+// Thin QR of v's tensor with axis `ax` as the columns: T = Q R.  v keeps Q
+// (axis ax now of dim k = min(rows, cols)); R (k x cols) is returned.
+template <class T>
+int qr_axis(Work<T>& w, int v, int ax, DBuf& R) {
+  tnfa_ctx* ctx = w.ctx;
+  std::vector<int> shp = w.shape(v);
+  const int cols = shp[ax];
+  const int64_t rows = w.size(v) / cols;
+  TNFA_CHECK(rows < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "matrix too large");
+  const int k = (int)std::min<int64_t>(rows, cols);
+  DBuf M(ctx, (size_t)w.size(v) * sizeof(T));
+  move_axis<T>(ctx, w.t[v].p, M.p, shp, ax, (int)shp.size() - 1);  // [rest][cols]
+  DBuf Q(ctx, (size_t)rows * k * sizeof(T));
+  R = DBuf(ctx, (size_t)k * cols * sizeof(T));
+  DBuf tau(ctx, (size_t)k * sizeof(T));
+  la::qr<T>(ctx, {la::QrJob{M.p, Q.p, R.p, tau.p, (int)rows, cols}});
+  std::vector<int> qshp = shp;
+  qshp.erase(qshp.begin() + ax);
+  qshp.push_back(k);
+  DBuf back(ctx, (size_t)rows * k * sizeof(T));
+  move_axis<T>(ctx, Q.p, back.p, qshp, (int)qshp.size() - 1, ax);
+  w.t[v] = std::move(back);
+  return k;
+}
+
+template <class T>
+void orthogonalize_to_roots(Work<T>& w) {
+  for (int v = w.topo.V - 1; v >= 0; --v) {
+    const int p = w.topo.parent[v];
+    if (p < 0) continue;
+    DBuf R;
+    const int ax_p = w.child_axis(p, v);
+    const int k = qr_axis(w, v, 1, R);
+    absorb(w, p, ax_p, R.p, k);
+    w.topo.link[v] = k;
+  }
+}
+
+struct TruncStats {
+  double max_discarded = 0.0;  // largest relative discarded weight of a bond
+  int max_sweeps = 0;
+  bool nonconv = false;
+};
+
+// SVD of v's tensor across the bond to child c, truncated; the centre moves
+// into c.
+template <class T>
+void split_bond(Work<T>& w, int v, int c, const tnfa_trunc_params& prm, TruncStats& st) {
+  tnfa_ctx* ctx = w.ctx;
+  const int ax = w.child_axis(v, c);
+  const std::vector<int> shp = w.shape(v);
+  const int cols = shp[ax];
+  const int64_t rows64 = w.size(v) / cols;
+  TNFA_CHECK(rows64 < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "matrix too large");
+  const int rows = (int)rows64;
+  DBuf M(ctx, (size_t)w.size(v) * sizeof(T));
+  move_axis<T>(ctx, w.t[v].p, M.p, shp, ax, (int)shp.size() - 1);  // [rows][cols]
+  const bool tall = rows >= cols;
+  const int n = tall ? cols : rows;  // number of singular values
+  DBuf S(ctx, (size_t)n * sizeof(double)), sw(ctx, sizeof(int));
+  DBuf U, Vm, left;
+  if (tall) {
+    // M = Q R, R = U S V^H  =>  left = Q U, right = S V^H
+    DBuf Q(ctx, (size_t)rows * cols * sizeof(T)), R(ctx, (size_t)cols * cols * sizeof(T));
+    DBuf tau(ctx, (size_t)cols * sizeof(T));
+    la::qr<T>(ctx, {la::QrJob{M.p, Q.p, R.p, tau.p, rows, cols}});
+    U = DBuf(ctx, (size_t)n * n * sizeof(T));
+    Vm = DBuf(ctx, (size_t)n * n * sizeof(T));
+    la::svd<T>(ctx, {la::SvdJob{R.p, U.p, S.as<double>(), Vm.p, n, n, sw.as<int>()}});
+    left = DBuf(ctx, (size_t)rows * n * sizeof(T));
+    la::gemm<T>(ctx, {la::GemmJob{Q.p, U.p, left.p, rows, n, n, n, n, n, 0, 0, 1.0, 0.0}});
+  } else {
+    // M^T = U S V^H  =>  M = conj(V) S U^T : left = conj(V), right = S U^T
+    DBuf MT(ctx, (size_t)rows * cols * sizeof(T));
+    move_axis<T>(ctx, M.p, MT.p, {rows, cols}, 1, 0);
+    U = DBuf(ctx, (size_t)cols * n * sizeof(T));
+    Vm = DBuf(ctx, (size_t)n * n * sizeof(T));
+    la::svd<T>(ctx, {la::SvdJob{MT.p, U.p, S.as<double>(), Vm.p, cols, n, sw.as<int>()}});
+  }
+  std::vector<double> s(n);
+  int sweeps = 0;
+  TNFA_CUDA(cudaMemcpyAsync(s.data(), S.p, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaMemcpyAsync(&sweeps, sw.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (sweeps < 0) st.nonconv = true;
+  st.max_sweeps = std::max(st.max_sweeps, sweeps);
+  const int r = la::truncation_rank(s.data(), n, prm.cutoff, prm.maxdim, prm.mindim);
+  double tot = 0, drop = 0;
+  for (int i = 0; i < n; ++i) {
+    tot += s[i] * s[i];
+    if (i >= r) drop += s[i] * s[i];
+  }
+  if (tot > 0) st.max_discarded = std::max(st.max_discarded, drop / tot);
+  // diag(s[:r]) on the device
+  DBuf sd(ctx, (size_t)r * r * sizeof(T));
+  {
+    std::vector<T> diag((size_t)r * r, hreal<T>(0.0));
+    for (int i = 0; i < r; ++i) diag[(size_t)i * r + i] = hreal<T>(s[i]);
+    TNFA_CUDA(cudaMemcpyAsync(sd.p, diag.data(), diag.size() * sizeof(T), cudaMemcpyHostToDevice,
+                              ctx->stream));
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  DBuf newv(ctx, (size_t)rows * r * sizeof(T));
+  DBuf X(ctx, (size_t)r * cols * sizeof(T));
+  if (tall) {
+    copy2d<T>(ctx, newv.p, r, left.p, n, rows, r, false);
+    // X[i][j] = s_i conj(V[j][i])
+    la::gemm<T>(ctx, {la::GemmJob{sd.p, Vm.p, X.p, r, cols, r, r, n, cols, 0, 2, 1.0, 0.0}});
+  } else {
+    copy2d<T>(ctx, newv.p, r, Vm.p, n, rows, r, true);
+    // X[i][j] = s_i U[j][i]
+    la::gemm<T>(ctx, {la::GemmJob{sd.p, U.p, X.p, r, cols, r, r, n, cols, 0, 1, 1.0, 0.0}});
+  }
+  std::vector<int> nshp = shp;
+  nshp.erase(nshp.begin() + ax);
+  nshp.push_back(r);
+  DBuf back(ctx, (size_t)rows * r * sizeof(T));
+  move_axis<T>(ctx, newv.p, back.p, nshp, (int)nshp.size() - 1, ax);
+  w.t[v] = std::move(back);
+  absorb(w, c, 1, X.p, r);
+  w.topo.link[c] = r;
+}
+
+template <class T>
+void truncate_from(Work<T>& w, int v, const tnfa_trunc_params& prm, TruncStats& st) {
+  const std::vector<int> kids = w.topo.children[v];
+  for (int c : kids) {
+    split_bond(w, v, c, prm, st);
+    truncate_from(w, c, prm, st);
+    DBuf R;  // move the centre back to v
+    const int ax = w.child_axis(v, c);
+    const int k = qr_axis(w, c, 1, R);
+    absorb(w, v, ax, R.p, k);
+    w.topo.link[c] = k;
+  }
+}
+
+// ------------------------------------------------------ exact apply ----
+constexpr int AP_MAXD = 10;
+// Y[s_out][(aO af)][(cO cf)...] = sum_{s_in} O[(s_out, s_in) fused per leg][aO][cO..] f[s_in][af][cf..]
+struct ApplyJob {
+  int64_t ooff, foff, yoff, n;
+  int nd;                 // axes: site + bonds
+  int dO[AP_MAXD], dF[AP_MAXD];
+  int nlegs;
+  int base[8];
+};
+
+template <class T>
+__global__ void k_apply_exact(const T* __restrict__ O, const T* __restrict__ F, T* __restrict__ Y,
+                              const ApplyJob* __restrict__ jobs) {
+  const ApplyJob& jb = jobs[blockIdx.y];
+  int64_t obond = 1, fbond = 1;
+  for (int a = 1; a < jb.nd; ++a) {
+    obond *= jb.dO[a];
+    fbond *= jb.dF[a];
+  }
+  const int sdim = jb.dF[0];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < jb.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = i, oi = 0, fi = 0, os = 1, fs = 1;
+    for (int a = jb.nd - 1; a >= 1; --a) {
+      const int64_t d = (int64_t)jb.dO[a] * jb.dF[a];
+      const int64_t x = r % d;
+      r /= d;
+      oi += (x / jb.dF[a]) * os;
+      fi += (x % jb.dF[a]) * fs;
+      os *= jb.dO[a];
+      fs *= jb.dF[a];
+    }
+    const int s_out = (int)r;
+    T acc = Sc<T>::zero();
+    for (int s_in = 0; s_in < sdim; ++s_in) {
+      // fused operator site index: per leg (out * b + in), first leg most significant
+      int so = s_out, si = s_in, osite = 0, mul = 1;
+      for (int l = jb.nlegs - 1; l >= 0; --l) {
+        const int b = jb.base[l];
+        const int o = so % b, in = si % b;
+        so /= b;
+        si /= b;
+        osite += (o * b + in) * mul;
+        mul *= b * b;
+      }
+      acc = Sc<T>::fma(O[jb.ooff + osite * obond + oi], F[jb.foff + s_in * fbond + fi], acc);
+    }
+    Y[jb.yoff + i] = acc;
+  }
+}
+
+// O'[s_in][rest] = w * sum_{s_out} O[(s_out, s_in)][rest]: the out legs of an
+// operator contracted with the uniform integration weights.
+struct RowJob {
+  int64_t ooff, doff, rest;
+  int nlegs;
+  int base[8];
+  double w;
+};
+
+template <class T>
+__global__ void k_reduce_out(const T* __restrict__ O, T* __restrict__ D,
+                             const RowJob* __restrict__ jobs) {
+  const RowJob& jb = jobs[blockIdx.y];
+  int sdim = 1;
+  for (int l = 0; l < jb.nlegs; ++l) sdim *= jb.base[l];
+  const int64_t n = (int64_t)sdim * jb.rest;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int s_in = (int)(i / jb.rest);
+    const int64_t q = i % jb.rest;
+    T acc = Sc<T>::zero();
+    for (int s_out = 0; s_out < sdim; ++s_out) {
+      int so = s_out, si = s_in, osite = 0, mul = 1;
+      for (int l = jb.nlegs - 1; l >= 0; --l) {
+        const int b = jb.base[l];
+        osite += ((so % b) * b + si % b) * mul;
+        so /= b;
+        si /= b;
+        mul *= b * b;
+      }
+      acc = acc + O[jb.ooff + (int64_t)osite * jb.rest + q];
+    }
+    D[jb.doff + i] = dmul(acc, jb.w);
+  }
+}
+
+template <class Job>
+DBuf upload_jobs(tnfa_ctx* ctx, const std::vector<Job>& jobs) {
+  DBuf d(ctx, jobs.size() * sizeof(Job));
+  TNFA_CUDA(cudaMemcpyAsync(d.p, jobs.data(), jobs.size() * sizeof(Job), cudaMemcpyHostToDevice,
+                            ctx->stream));
+  return d;
+}
+
+void check_same_tree(const Topo& A, const Topo& B, const char* what) {
+  TNFA_CHECK(A.V == B.V && A.parent == B.parent && A.nlegs == B.nlegs, TNFA_ERR_SHAPE,
+             std::string(what) + ": operator and function live on different trees");
+}
+
+template <class T>
+Work<T> apply_exact(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f) {
+  const Topo& A = op->topo;
+  const Topo& B = f->topo;
+  check_same_tree(A, B, "apply");
+  for (int l = 0; l < A.leg_off[A.V]; ++l) {
+    TNFA_CHECK(A.leg_kind[l] == TNFA_LEG_OPERATOR, TNFA_ERR_INVALID_ARGUMENT,
+               "apply: first argument is not an operator");
+    TNFA_CHECK(B.leg_kind[l] != TNFA_LEG_OPERATOR, TNFA_ERR_INVALID_ARGUMENT,
+               "apply: second argument is an operator");
+    TNFA_CHECK(A.leg_dim[l] == B.leg_dim[l] * B.leg_dim[l], TNFA_ERR_SHAPE,
+               "apply: operator leg dim must be base^2 of the function's");
+  }
+  Topo Y = B;
+  for (int v = 0; v < B.V; ++v) Y.link[v] = A.link[v] * B.link[v];
+  Y.finalize();
+  std::vector<ApplyJob> jobs;
+  int64_t nmax = 1;
+  Work<T> w{ctx, Y, {}};
+  DBuf ybuf(ctx, (size_t)Y.n_elem * sizeof(T));
+  for (int v = 0; v < B.V; ++v) {
+    ApplyJob j{};
+    j.ooff = A.off[v];
+    j.foff = B.off[v];
+    j.yoff = Y.off[v];
+    j.n = Y.size(v);
+    j.nd = 2 + (int)B.children[v].size();
+    TNFA_CHECK(j.nd <= AP_MAXD && B.nlegs[v] <= 8, TNFA_ERR_UNSUPPORTED, "vertex degree too high");
+    j.dO[0] = A.site_dim[v];
+    j.dF[0] = B.site_dim[v];
+    j.dO[1] = A.link[v];
+    j.dF[1] = B.link[v];
+    for (size_t i = 0; i < B.children[v].size(); ++i) {
+      j.dO[2 + i] = A.link[B.children[v][i]];
+      j.dF[2 + i] = B.link[B.children[v][i]];
+    }
+    j.nlegs = B.nlegs[v];
+    for (int l = 0; l < j.nlegs; ++l) j.base[l] = B.leg_dim[B.leg_off[v] + l];
+    jobs.push_back(j);
+    nmax = std::max(nmax, j.n);
+  }
+  DBuf dj = upload_jobs(ctx, jobs);
+  dim3 grid(grid_for(nmax, 256, 4096), B.V);
+  {
+    double fl = 0;
+    for (auto& j : jobs) fl += 2.0 * j.n * j.dF[0];
+    KernelScope ks(ctx, "apply_exact", fl, 0.0);
+    k_apply_exact<T><<<grid, 256, 0, ctx->stream>>>((const T*)op->d, (const T*)f->d, ybuf.as<T>(),
+                                                     dj.as<ApplyJob>());
+    TNFA_LAUNCH_CHECK();
+  }
+  w.t.reserve(Y.V);
+  for (int v = 0; v < Y.V; ++v) {
+    w.t.emplace_back(ctx, (size_t)Y.size(v) * sizeof(T));
+    TNFA_CUDA(cudaMemcpyAsync(w.t.back().p, ybuf.as<T>() + Y.off[v], Y.size(v) * sizeof(T),
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  return w;
+}
+
+template <class T>
+double host_norm(tnfa_ctx* ctx, const DBuf& b, int64_t n) {
+  std::vector<T> h(n);
+  TNFA_CUDA(cudaMemcpyAsync(h.data(), b.p, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  double s = 0;
+  for (auto& x : h) s += habs2(x);
+  return std::sqrt(s);
+}
+
+template <class T>
+tnfa_net* truncate_work(Work<T>& w, int dtype, const tnfa_trunc_params& prm) {
+  orthogonalize_to_roots(w);
+  TruncStats st;
+  for (int r : w.topo.roots()) truncate_from(w, r, prm, st);
+  TNFA_CHECK(!st.nonconv, TNFA_ERR_NOT_CONVERGED, "Jacobi SVD hit its sweep cap");
+  if (prm.normalize) {
+    for (int r : w.topo.roots()) {
+      const double nrm = host_norm<T>(w.ctx, w.t[r], w.size(r));
+      if (nrm > 0) {
+        k_scale_by<T><<<grid_for(w.size(r), 256, 1024), 256, 0, w.ctx->stream>>>(
+            w.t[r].template as<T>(), w.size(r), 1.0 / nrm);
+        TNFA_LAUNCH_CHECK();
+      }
+    }
+  }
+  return store_work(w, dtype);
+}
+
+void check_params(const tnfa_trunc_params* p) {
+  TNFA_CHECK(p != nullptr, TNFA_ERR_INVALID_ARGUMENT, "null truncation parameters");
+  TNFA_CHECK(p->cutoff >= 0.0 && std::isfinite(p->cutoff), TNFA_ERR_INVALID_ARGUMENT,
+             "cutoff must be finite and >= 0");
+  TNFA_CHECK(p->maxdim >= 0 && p->mindim >= 0, TNFA_ERR_INVALID_ARGUMENT, "negative maxdim/mindim");
+}
+
+// ------------------------------------------------------------- inner ----
+// Message of vertex v toward its parent: M[ag][af] = sum conj?(F) G over the
+// site and children legs (children already contracted with their messages).
+template <class T>
+void contract_pair(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, bool conjF, double* out) {
+  const Topo& A = f->topo;
+  const Topo& B = g->topo;
+  check_same_tree(A, B, "inner");
+  TNFA_CHECK(A.site_dim == B.site_dim, TNFA_ERR_SHAPE, "inner: site dimensions differ");
+  std::vector<DBuf> msg(A.V);
+  T total = hreal<T>(1.0);
+  for (int v = A.V - 1; v >= 0; --v) {
+    // G with every child leg cg_j replaced by cf_j
+    std::vector<int> shp{B.site_dim[v], B.link[v]};
+    for (int c : B.children[v]) shp.push_back(B.link[c]);
+    int64_t n = B.size(v);
+    DBuf G(ctx, (size_t)n * sizeof(T));
+    TNFA_CUDA(cudaMemcpyAsync(G.p, (const T*)g->d + B.off[v], n * sizeof(T),
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+    for (size_t j = 0; j < B.children[v].size(); ++j) {
+      const int c = B.children[v][j];
+      const int ax = 2 + (int)j;
+      const int oldd = shp[ax], newd = A.link[c];
+      const int64_t rest = n / oldd;
+      DBuf a(ctx, (size_t)n * sizeof(T));
+      move_axis<T>(ctx, G.p, a.p, shp, ax, 0);  // [cg][rest]
+      DBuf b(ctx, (size_t)newd * rest * sizeof(T));
+      // b[cf][rest] = sum_cg M_c[cg][cf] a[cg][rest]  (M_c is cg x cf)
+      la::gemm<T>(ctx, {la::GemmJob{msg[c].p, a.p, b.p, newd, (int)rest, oldd, newd, (int)rest,
+                                    (int)rest, 1, 0, 1.0, 0.0}});
+      std::vector<int> nshp = shp;
+      nshp.erase(nshp.begin() + ax);
+      nshp.insert(nshp.begin(), newd);
+      shp[ax] = newd;
+      n = newd * rest;
+      G = DBuf(ctx, (size_t)n * sizeof(T));
+      move_axis<T>(ctx, b.p, G.p, nshp, 0, ax);
+      msg[c].reset();
+    }
+    // M[ag][af] = sum_R G[ag][R] conj?(F[af][R])
+    std::vector<int> fshp{A.site_dim[v], A.link[v]};
+    for (int c : A.children[v]) fshp.push_back(A.link[c]);
+    DBuf Fm(ctx, (size_t)A.size(v) * sizeof(T)), Gm(ctx, (size_t)n * sizeof(T));
+    move_axis<T>(ctx, (const T*)f->d + A.off[v], Fm.p, fshp, 1, 0);
+    move_axis<T>(ctx, G.p, Gm.p, shp, 1, 0);
+    const int ag = B.link[v], af = A.link[v];
+    const int64_t R = n / ag;
+    msg[v] = DBuf(ctx, (size_t)ag * af * sizeof(T));
+    la::gemm<T>(ctx, {la::GemmJob{Gm.p, Fm.p, msg[v].p, ag, af, (int)R, (int)R, (int)R, af, 0,
+                                  conjF ? 2 : 1, 1.0, 0.0}});
+    if (B.parent[v] < 0) {
+      T val;
+      TNFA_CUDA(cudaMemcpyAsync(&val, msg[v].p, sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+      TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+      total = total * val;
+      msg[v].reset();
+    }
+  }
+  if constexpr (sizeof(T) == 16) {
+    out[0] = ((cplx*)&total)->re;
+    out[1] = ((cplx*)&total)->im;
+  } else {
+    out[0] = (double)total;
+    out[1] = 0.0;
+  }
+}
+
+tnfa_net* reduce_out_legs(tnfa_ctx* ctx, const tnfa_net* op, int take_sum) {
+  const Topo& A = op->topo;
+  Topo D = A;
+  for (int l = 0; l < A.leg_off[A.V]; ++l) {
+    int b = 1;
+    while (b * b < A.leg_dim[l]) ++b;
+    TNFA_CHECK(b * b == A.leg_dim[l] && A.leg_kind[l] == TNFA_LEG_OPERATOR, TNFA_ERR_INVALID_ARGUMENT,
+               "integrate(O, f): O is not an operator network");
+    D.leg_dim[l] = b;
+    D.leg_kind[l] = TNFA_LEG_REAL;
+  }
+  D.finalize();
+  tnfa_net* out = new_net(ctx, D, op->dtype);
+  std::vector<RowJob> jobs;
+  int64_t nmax = 1;
+  for (int v = 0; v < A.V; ++v) {
+    RowJob j{};
+    j.ooff = A.off[v];
+    j.doff = D.off[v];
+    j.rest = A.size(v) / A.site_dim[v];
+    j.nlegs = A.nlegs[v];
+    TNFA_CHECK(j.nlegs <= 8, TNFA_ERR_UNSUPPORTED, "too many legs");
+    j.w = 1.0;
+    for (int l = 0; l < j.nlegs; ++l) {
+      j.base[l] = D.leg_dim[D.leg_off[v] + l];
+      if (!take_sum) j.w /= j.base[l];
+    }
+    jobs.push_back(j);
+    nmax = std::max<int64_t>(nmax, D.size(v));
+  }
+  DBuf dj = upload_jobs(ctx, jobs);
+  dim3 grid(grid_for(nmax, 256, 1024), A.V);
+  if (op->dtype == TNFA_F64)
+    k_reduce_out<double><<<grid, 256, 0, ctx->stream>>>((const double*)op->d, (double*)out->d,
+                                                         dj.as<RowJob>());
+  else if (op->dtype == TNFA_C128)
+    k_reduce_out<cplx><<<grid, 256, 0, ctx->stream>>>((const cplx*)op->d, (cplx*)out->d,
+                                                       dj.as<RowJob>());
+  else
+    fail(TNFA_ERR_DTYPE, "integrate(O, f) needs FP64 or complex128 networks");
+  TNFA_LAUNCH_CHECK();
+  return out;
+}
+
+}  // namespace
+
+tnfa_net* apply_truncate(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f,
+                         const tnfa_trunc_params& prm) {
+  TNFA_CHECK(op->dtype == f->dtype, TNFA_ERR_DTYPE, "apply: operator and function types differ");
+  if (f->dtype == TNFA_F64) {
+    Work<double> w = apply_exact<double>(ctx, op, f);
+    return truncate_work(w, TNFA_F64, prm);
+  }
+  if (f->dtype == TNFA_C128) {
+    Work<cplx> w = apply_exact<cplx>(ctx, op, f);
+    return truncate_work(w, TNFA_C128, prm);
+  }
+  fail(TNFA_ERR_DTYPE, "apply: FP64 or complex128 networks");
+}
+
+tnfa_net* truncate_net(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_trunc_params& prm) {
+  if (f->dtype == TNFA_F64) {
+    Work<double> w = load_work<double>(ctx, f);
+    return truncate_work(w, TNFA_F64, prm);
+  }
+  if (f->dtype == TNFA_C128) {
+    Work<cplx> w = load_work<cplx>(ctx, f);
+    return truncate_work(w, TNFA_C128, prm);
+  }
+  fail(TNFA_ERR_DTYPE, "truncate: FP64 or complex128 networks");
+}
+
+void inner_product(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, bool conjF, double* out) {
+  TNFA_CHECK(f->dtype == g->dtype, TNFA_ERR_DTYPE, "inner: element types differ");
+  if (f->dtype == TNFA_F64) contract_pair<double>(ctx, f, g, conjF, out);
+  else if (f->dtype == TNFA_C128) contract_pair<cplx>(ctx, f, g, conjF, out);
+  else fail(TNFA_ERR_DTYPE, "inner: FP64 or complex128 networks");
+}
+
+}  // namespace tnfa
+
+using namespace tnfa;
+
+extern "C" {
+
+int tnfa_apply(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f,
+               const tnfa_trunc_params* params, tnfa_net** out) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(op, "apply operator");
+  require_net(f, "apply function");
+  check_params(params);
+  TNFA_CHECK(out, TNFA_ERR_INVALID_ARGUMENT, "null out");
+  *out = apply_truncate(ctx, op, f, *params);
+  TNFA_API_END
+}
+
+int tnfa_apply_batched(tnfa_ctx* ctx, int32_t n, const tnfa_net* const* ops,
+                       const tnfa_net* const* fs, const tnfa_trunc_params* params,
+                       tnfa_net** outs) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  check_params(params);
+  TNFA_CHECK(n >= 0 && (n == 0 || (ops && fs && outs)), TNFA_ERR_INVALID_ARGUMENT, "null arrays");
+  for (int i = 0; i < n; ++i) outs[i] = nullptr;
+  try {
+    for (int i = 0; i < n; ++i) {
+      require_net(ops[i], "apply_batched operator");
+      require_net(fs[i], "apply_batched function");
+      outs[i] = apply_truncate(ctx, ops[i], fs[i], *params);
+    }
+  } catch (...) {
+    for (int i = 0; i < n; ++i)
+      if (outs[i]) {
+        tnfa_net_destroy(outs[i]);
+        outs[i] = nullptr;
+      }
+    throw;
+  }
+  TNFA_API_END
+}
+
+int tnfa_truncate(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_trunc_params* params,
+                  tnfa_net** out) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(f, "truncate");
+  check_params(params);
+  TNFA_CHECK(out, TNFA_ERR_INVALID_ARGUMENT, "null out");
+  *out = truncate_net(ctx, f, *params);
+  TNFA_API_END
+}
+
+int tnfa_truncate_batched(tnfa_ctx* ctx, int32_t n, const tnfa_net* const* fs,
+                          const tnfa_trunc_params* params, tnfa_net** outs) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  check_params(params);
+  TNFA_CHECK(n >= 0 && (n == 0 || (fs && outs)), TNFA_ERR_INVALID_ARGUMENT, "null arrays");
+  for (int i = 0; i < n; ++i) outs[i] = nullptr;
+  try {
+    for (int i = 0; i < n; ++i) {
+      require_net(fs[i], "truncate_batched");
+      outs[i] = truncate_net(ctx, fs[i], *params);
+    }
+  } catch (...) {
+    for (int i = 0; i < n; ++i)
+      if (outs[i]) {
+        tnfa_net_destroy(outs[i]);
+        outs[i] = nullptr;
+      }
+    throw;
+  }
+  TNFA_API_END
+}
+
+int tnfa_inner(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, double* out) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(f, "inner f");
+  require_net(g, "inner g");
+  TNFA_CHECK(out, TNFA_ERR_INVALID_ARGUMENT, "null out");
+  inner_product(ctx, f, g, true, out);
+  TNFA_API_END
+}
+
+int tnfa_integrate_operator(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f, int take_sum,
+                            double* out) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(op, "integrate operator");
+  require_net(f, "integrate function");
+  TNFA_CHECK(out, TNFA_ERR_INVALID_ARGUMENT, "null out");
+  TNFA_CHECK(op->dtype == f->dtype, TNFA_ERR_DTYPE, "integrate(O, f): element types differ");
+  tnfa_net* row = reduce_out_legs(ctx, op, take_sum);
+  try {
+    inner_product(ctx, row, f, false, out);
+  } catch (...) {
+    tnfa_net_destroy(row);
+    throw;
+  }
+  tnfa_net_destroy(row);
+  TNFA_API_END
+}
+
+}  // extern "C"

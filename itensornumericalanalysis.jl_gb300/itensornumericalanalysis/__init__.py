@@ -68,7 +68,7 @@ from .indexmap import (
     reduced_indsnetworkmap,
 )
 from .integration import integrate, partial_integrate
-from .network import ITensorNetworkFunction, calculate_fx, evaluate
+from .network import ITensorNetworkFunction, calculate_fx, evaluate, inner
 from .operate import operate
 from .truncation import truncate
 

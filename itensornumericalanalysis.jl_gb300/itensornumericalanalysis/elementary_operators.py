@@ -172,16 +172,10 @@ def opsum_to_operator(s: IndsNetworkMap, opsum: OpSum, cutoff: float = 1e-15,
 
 
 def _compress(op: ITensorNetworkOperator, cutoff: float) -> ITensorNetworkOperator:
-    try:
-        from .truncation import truncate
-    except ImportError:
-        return op
-    try:
-        return truncate(op, cutoff=cutoff)
-    except _lib.TnfaError as e:
-        if e.status == _lib.ERR_UNSUPPORTED:
-            return op
-        raise
+    """Recompress the term-by-term direct sum on the device (QR + SVD sweep)."""
+    from .truncation import truncate
+
+    return truncate(op, cutoff=cutoff)
 
 
 def forward_shift_op(s, truncate_kwargs=None, **kw):

@@ -209,6 +209,16 @@ class ITensorNetworkFunction:
         self._ctx.call("tnfa_integrate", self._h, int(take_sum), out)
         return complex(out[0], out[1]) if self.is_complex else out[0]
 
+    def inner(self, other: "ITensorNetworkFunction"):
+        """<self|other> = sum over the grid of conj(self) * other."""
+        a, b = self._promote(other)
+        out = (C.c_double * 2)()
+        self._ctx.call("tnfa_inner", a._h, b._h, out)
+        return complex(out[0], out[1]) if a.is_complex else out[0]
+
+    def norm(self) -> float:
+        return float(abs(self.inner(self)) ** 0.5)
+
     # -- algebra -------------------------------------------------------------
     def copy(self) -> "ITensorNetworkFunction":
         h = C.c_void_p()
@@ -280,6 +290,11 @@ def evaluate(f: ITensorNetworkFunction, xs, dims=None, **kw):
     if a.ndim == 2:
         return f.evaluate_batch(a, dims, **kw)
     return f.evaluate(xs, dims, **kw)
+
+
+def inner(f: ITensorNetworkFunction, g: ITensorNetworkFunction):
+    """<f|g> over the full grid (conjugating f)."""
+    return f.inner(g)
 
 
 def calculate_fx(f: ITensorNetworkFunction, X, dims=None, **kw) -> np.ndarray:
