@@ -133,6 +133,12 @@ struct KernelFamily {
 }  // namespace tnfa
 
 struct tnfa_ctx {
+  // One reference for the caller's handle plus one per live network: the
+  // context (and its stream) is released only when the last one goes, so a
+  // network may be destroyed after tnfa_ctx_destroy without touching freed
+  // memory.
+  int refs = 1;
+  bool closed = false;
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -189,6 +195,7 @@ struct DBuf {
 };
 
 tnfa_net* new_net(tnfa_ctx* ctx, const Topo& topo, int dtype);  // allocates d
+void ctx_release(tnfa_ctx* ctx);  // drop one reference (frees at zero)
 void require_net(const tnfa_net* net, const char* what);
 void require_ctx(const tnfa_ctx* ctx);
 

@@ -74,7 +74,24 @@ tnfa_net* new_net(tnfa_ctx* ctx, const Topo& topo, int dtype) {
     delete n;
     throw;
   }
+  ctx->refs += 1;
   return n;
+}
+
+static void ctx_free(tnfa_ctx* ctx) {
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& f : ctx->families)
+    for (auto& ev : f.events) {
+      cudaEventDestroy(ev.first);
+      cudaEventDestroy(ev.second);
+    }
+  for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+void ctx_release(tnfa_ctx* ctx) {
+  if (--ctx->refs == 0) ctx_free(ctx);
 }
 
 __global__ void k_f64_to_f32(const double* __restrict__ s, float* __restrict__ d, int64_t n) {
@@ -262,16 +279,10 @@ int tnfa_ctx_kernel_stats(tnfa_ctx* ctx, int32_t max, char* names, int64_t* laun
 }
 
 int tnfa_ctx_destroy(tnfa_ctx* ctx) {
-  if (!ctx) return TNFA_ERR_INVALID_ARGUMENT;
+  if (!ctx || ctx->closed) return TNFA_ERR_INVALID_ARGUMENT;
+  ctx->closed = true;
   cudaStreamSynchronize(ctx->stream);
-  for (auto& f : ctx->families)
-    for (auto& ev : f.events) {
-      cudaEventDestroy(ev.first);
-      cudaEventDestroy(ev.second);
-    }
-  for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
-  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
-  delete ctx;
+  ctx_release(ctx);
   return TNFA_OK;
 }
 
@@ -315,9 +326,11 @@ int tnfa_net_create(tnfa_ctx* ctx, const tnfa_topology* topo, int dtype, const v
 
 int tnfa_net_destroy(tnfa_net* net) {
   if (!net) return TNFA_ERR_INVALID_ARGUMENT;
+  tnfa_ctx* ctx = net->ctx;
   net->invalidate_caches();
-  if (net->d) dfree(net->ctx, net->d);
+  if (net->d) dfree(ctx, net->d);
   delete net;
+  if (ctx) ctx_release(ctx);
   return TNFA_OK;
 }
 

@@ -332,11 +332,18 @@ __global__ void __launch_bounds__(512) k_svd(const SvdJob* __restrict__ jobs, T*
   }
   for (int64_t i = threadIdx.x; i < (int64_t)n * n; i += blockDim.x)
     V[i] = from_real<T>((i / n) == (i % n) ? 1.0 : 0.0);
-  __syncthreads();
+  __shared__ double red[32];
+  double part = 0.0;
+  for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) part += abs2(A[i]);
+  const double fro2 = block_sum<double>(part, red);
+  // columns below this are rounding noise of the whole matrix
+  const double negl = 1e-30 * fro2;
   const int n2 = (n + 1) & ~1;
   int sweep = 0;
   bool converged = (n < 2);
-  const double tol = 1e-15;
+  // pairs count as orthogonal once |g| <= tol sqrt(a b); the rounding floor of
+  // a length-m dot product is ~sqrt(m) eps
+  const double tol = 8.0 * sqrt((double)m) * 2.220446049250313e-16;
   while (!converged && sweep < max_sweeps) {
     if (threadIdx.x == 0) rotated = 0;
     __syncthreads();
@@ -358,7 +365,7 @@ __global__ void __launch_bounds__(512) k_svd(const SvdJob* __restrict__ jobs, T*
         b = warp_sum(b);
         g = warp_sum(g);
         const double ag = sqrt(abs2(g));
-        if (ag <= tol * sqrt(a * b) || ag == 0.0) continue;
+        if (ag <= tol * sqrt(a * b) || ag == 0.0 || (a < negl && b < negl)) continue;
         const double zeta = (b - a) / (2.0 * ag);
         const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
         const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;

@@ -80,6 +80,8 @@ class ITensorNetworkFunction:
         return type(self)(s or self.s, handle, self._ctx, self._legs if legs == "same" else legs)
 
     def __del__(self):
+        # the library keeps the context alive while networks exist, so this
+        # is safe in any finalisation order
         try:
             if self._h:
                 self._ctx.lib.tnfa_net_destroy(self._h)
