@@ -365,9 +365,14 @@ __global__ void __launch_bounds__(512) k_svd(const SvdJob* __restrict__ jobs, T*
         b = warp_sum(b);
         g = warp_sum(g);
         const double ag = sqrt(abs2(g));
-        if (ag <= tol * sqrt(a * b) || ag == 0.0 || (a < negl && b < negl)) continue;
+        // a negligible column carries no singular value worth orthogonalising
+        // against; skipping it also avoids zeta^2 overflow on extreme ratios
+        if (ag <= tol * sqrt(a * b) || ag == 0.0 || a < negl || b < negl) continue;
         const double zeta = (b - a) / (2.0 * ag);
-        const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double t = fabs(zeta) > 1e150
+                             ? 0.5 / zeta
+                             : (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        if (t == 0.0) continue;
         const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
         const T e = phase(g);  // g / |g|
         const T se = scal(e, s), sec = scal(conj(e), s);
