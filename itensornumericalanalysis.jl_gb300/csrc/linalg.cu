@@ -8,6 +8,7 @@
 // Every problem of a batch may have its own shape; one launch covers them all.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "linalg.cuh"
 
@@ -224,12 +225,19 @@ __global__ void __launch_bounds__(512) k_qr(const QrJob* __restrict__ jobs, T* _
     if (threadIdx.x == 0) {
       const T x0 = x[j];
       const double nrm = sqrt(nrm2);
-      const T alpha = scal(phase(x0), -nrm);
-      const T v0 = x0 - alpha;
-      const double vn2 = nrm2 - abs2(x0) + abs2(v0);
-      tau[j] = from_real<T>(vn2 > 0.0 ? 2.0 / vn2 : 0.0);
-      x[j] = v0;
-      alpha_sh = alpha;
+      if (!(nrm > 1e-150)) {
+        // an (almost) eliminated column: no reflection.  A residue this small
+        // (rounding left by earlier steps) would make 2 / |v|^2 overflow.
+        tau[j] = from_real<T>(0.0);
+        alpha_sh = x0;
+      } else {
+        const T alpha = scal(phase(x0), -nrm);
+        const T v0 = x0 - alpha;
+        const double vn2 = nrm2 - abs2(x0) + abs2(v0);
+        tau[j] = from_real<T>(vn2 > 0.0 ? 2.0 / vn2 : 0.0);
+        x[j] = v0;
+        alpha_sh = alpha;
+      }
     }
     __syncthreads();
     const double beta = re(tau[j]);
@@ -440,10 +448,37 @@ void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
   DBuf work(ctx, (size_t)woff.back() * sizeof(T));
   DBuf dw = upload(ctx, woff);
   DBuf d = upload(ctx, jobs);
-  KernelScope ks(ctx, sizeof(T) == 8 ? "svd_f64" : "svd_c128", fl, 0.0);
-  k_svd<T><<<(unsigned)jobs.size(), 512, 0, ctx->stream>>>(d.as<SvdJob>(), work.as<T>(),
-                                                           dw.as<int64_t>(), max_sweeps);
-  TNFA_LAUNCH_CHECK();
+  {
+    KernelScope ks(ctx, sizeof(T) == 8 ? "svd_f64" : "svd_c128", fl, 0.0);
+    k_svd<T><<<(unsigned)jobs.size(), 512, 0, ctx->stream>>>(d.as<SvdJob>(), work.as<T>(),
+                                                             dw.as<int64_t>(), max_sweeps);
+    TNFA_LAUNCH_CHECK();
+  }
+  // Diagnostics: with TNFA_DEBUG_DIR set, the input of every SVD that hit the
+  // sweep cap is written there (int32 m, int32 n, element size, then data).
+  static const char* dbg = getenv("TNFA_DEBUG_DIR");
+  if (dbg && *dbg) {
+    static int counter = 0;
+    for (const auto& j : jobs) {
+      if (!j.sweeps) continue;
+      int sw = 0;
+      TNFA_CUDA(cudaMemcpyAsync(&sw, j.sweeps, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (sw >= 0) continue;
+      std::vector<T> h((size_t)j.m * j.n);
+      TNFA_CUDA(cudaMemcpyAsync(h.data(), j.A, h.size() * sizeof(T), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+      TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+      char path[1024];
+      snprintf(path, sizeof path, "%s/svd_nonconv_%d.bin", dbg, counter++);
+      if (FILE* fp = fopen(path, "wb")) {
+        int hdr[3] = {j.m, j.n, (int)sizeof(T)};
+        fwrite(hdr, sizeof(int), 3, fp);
+        fwrite(h.data(), sizeof(T), h.size(), fp);
+        fclose(fp);
+      }
+    }
+  }
 }
 
 int truncation_rank(const double* s, int n, double cutoff, int maxdim, int mindim) {

@@ -15,6 +15,7 @@
 // SVD therefore sees the exact Schmidt spectrum of its bond.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <numeric>
 
 #include "evaluate.cuh"
@@ -64,6 +65,28 @@ __global__ void k_scale_by(T* x, int64_t n, double s) {
     x[i] = dmul(x[i], s);
 }
 
+// Diagnostics: with TNFA_DEBUG_NAN set, every step of the truncation checks
+// its output for NaN / Inf and fails naming the first step that produced one.
+inline bool nan_debug() {
+  static const char* e = getenv("TNFA_DEBUG_NAN");
+  return e && *e;
+}
+
+template <class T>
+void nan_check(tnfa_ctx* ctx, const void* p, int64_t n, const char* what, int v) {
+  if (!nan_debug() || n <= 0) return;
+  std::vector<T> h(n);
+  TNFA_CUDA(cudaMemcpyAsync(h.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int64_t i = 0; i < n; ++i) {
+    double a = habs2(h[i]);
+    if (!std::isfinite(a))
+      fail(TNFA_ERR_CUDA, std::string("non-finite value after ") + what + " at vertex " +
+                              std::to_string(v) + ", element " + std::to_string(i) + " of " +
+                              std::to_string(n));
+  }
+}
+
 template <class T>
 struct Work {
   tnfa_ctx* ctx;
@@ -95,6 +118,7 @@ Work<T> load_work(tnfa_ctx* ctx, const tnfa_net* net) {
     w.t.emplace_back(ctx, (size_t)n * sizeof(T));
     TNFA_CUDA(cudaMemcpyAsync(w.t.back().p, (const T*)net->d + net->topo.off[v], n * sizeof(T),
                               cudaMemcpyDeviceToDevice, ctx->stream));
+    nan_check<T>(ctx, w.t.back().p, n, "load", v);
   }
   return w;
 }
@@ -151,8 +175,12 @@ void absorb(Work<T>& w, int v, int ax, const void* M, int newdim) {
   std::vector<int> nshp = shp;
   nshp.erase(nshp.begin() + ax);
   nshp.insert(nshp.begin(), newdim);  // current layout [newdim][rest...]
+  nan_check<T>(ctx, a.p, w.size(v), "absorb/permute-in", v);
+  nan_check<T>(ctx, M, (int64_t)newdim * old, "absorb/matrix", v);
+  nan_check<T>(ctx, b.p, newdim * rest, "absorb/gemm", v);
   DBuf c(ctx, (size_t)newdim * rest * sizeof(T));
   move_axis<T>(ctx, b.p, c.p, nshp, 0, ax);
+  nan_check<T>(ctx, c.p, newdim * rest, "absorb/permute-out", v);
   w.t[v] = std::move(c);
 }
 
@@ -171,7 +199,10 @@ int qr_axis(Work<T>& w, int v, int ax, DBuf& R) {
   DBuf Q(ctx, (size_t)rows * k * sizeof(T));
   R = DBuf(ctx, (size_t)k * cols * sizeof(T));
   DBuf tau(ctx, (size_t)k * sizeof(T));
+  nan_check<T>(ctx, M.p, w.size(v), "qr_axis/permute-in", v);
   la::qr<T>(ctx, {la::QrJob{M.p, Q.p, R.p, tau.p, (int)rows, cols}});
+  nan_check<T>(ctx, Q.p, rows * k, "qr_axis/Q", v);
+  nan_check<T>(ctx, R.p, (int64_t)k * cols, "qr_axis/R", v);
   std::vector<int> qshp = shp;
   qshp.erase(qshp.begin() + ax);
   qshp.push_back(k);
