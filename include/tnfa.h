@@ -162,6 +162,26 @@ int tnfa_evaluate(tnfa_ctx* ctx, const tnfa_net* net, const double* X, int64_t n
                   int32_t n_dims, const int32_t* dims, int x_memory, void* out, int out_kind,
                   int out_memory, int precision);
 
+/* Batched evaluation for callers that cannot allocate device memory during
+ * the call -- for example code whose GPU memory is wholly owned by another
+ * runtime's caching allocator (where cudaMalloc would fail or implicitly
+ * synchronise the device), or latency-bound serving loops that must not block
+ * on the allocator.  No counterpart in the reference (its evaluate allocates
+ * freely on the host).  It computes what tnfa_evaluate computes, with every
+ * scratch buffer taken from one fixed 32 MiB device array compiled into the
+ * library (each GPU that loads the library holds it until exit) and no
+ * cudaMalloc / cudaFree.  X (n_points x n_cols doubles) and out must be device
+ * pointers; precision must match the network's type (TNFA_PREC_F64 on FP64 or
+ * complex networks, TNFA_PREC_F32 on FP32 networks).  A request whose scratch
+ * does not fit is rejected with TNFA_ERR_INVALID_ARGUMENT, naming the number of
+ * points that fit.  The first call on a device looks up the array's device
+ * address; make that call before any stream capture.  All calls share the one
+ * array, so calls that overlap on the GPU (other streams, other host threads)
+ * race: serialise them. */
+int tnfa_evaluate_noalloc(tnfa_ctx* ctx, const tnfa_net* net, const double* X, int64_t n_points,
+                          int32_t n_dims, const int32_t* dims, void* out, int out_kind,
+                          int precision);
+
 /* ---- integration -------------------------------------------------------- */
 
 /* Left Riemann sum over [0,1)^n: contract every site leg with the uniform

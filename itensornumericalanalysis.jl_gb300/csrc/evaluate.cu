@@ -772,3 +772,209 @@ extern "C" int tnfa_evaluate(tnfa_ctx* ctx, const tnfa_net* net, const double* X
   }
   TNFA_API_END
 }
+
+// ------------------------------------------ evaluation without allocation ----
+// tnfa_evaluate_noalloc: the same digitize / group / contract / combine
+// kernels as tnfa_evaluate, with every scratch buffer carved out of one
+// file-scope device array instead of the stream-ordered allocator.
+#include <mutex>
+
+namespace tnfa {
+namespace {
+
+constexpr size_t NOALLOC_BYTES = (size_t)32 << 20;  // 32 MiB, held by every device
+__device__ __align__(256) unsigned char noalloc_scratch[NOALLOC_BYTES];
+
+// Host code cannot use the array's name as a device address; this looks the
+// address up once per device (with that device current) and caches it.
+unsigned char* noalloc_base(int device) {
+  static std::mutex mu;
+  static std::vector<unsigned char*> addr;
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)addr.size() <= device) addr.resize(device + 1, nullptr);
+  if (!addr[device]) {
+    TNFA_CUDA(cudaSetDevice(device));
+    void* p = nullptr;
+    TNFA_CUDA(cudaGetSymbolAddress(&p, noalloc_scratch));
+    addr[device] = (unsigned char*)p;
+  }
+  return addr[device];
+}
+
+struct Carve {
+  unsigned char* base;
+  size_t cap, used = 0;
+  size_t take_off(size_t bytes) {
+    const size_t off = (used + 255) & ~(size_t)255;
+    used = off + bytes;
+    return off;
+  }
+  void* take(size_t bytes) {
+    const size_t off = take_off(bytes);
+    TNFA_CHECK(used <= cap, TNFA_ERR_INVALID_ARGUMENT, "scratch overflow");
+    return base + off;
+  }
+};
+
+template <class T>
+void evaluate_noalloc_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, const double* X,
+                           int64_t P64, int ncols, const std::vector<DigitEntry>& prog, void* out,
+                           int out_kind) {
+  const Topo& Tp = net->topo;
+  const int V = Tp.V;
+  EvalPlan plan = make_plan(Tp);
+  const int nroots = (int)plan.roots.size();
+  int maxsd = 1;
+  for (int v = 0; v < V; ++v) maxsd = std::max(maxsd, Tp.site_dim[v]);
+  // Dry run of the carving to size the request before touching the device.
+  const int64_t P = P64;
+  const size_t slot_vals = (size_t)P * plan.chimax;
+  size_t sizes[] = {prog.size() * sizeof(DigitEntry),
+                    (size_t)V * P,
+                    (size_t)P * 4,
+                    group_meta_ints(maxsd) * 4,
+                    4,
+                    (size_t)plan.nslots * slot_vals * sizeof(T),
+                    (size_t)plan.nslots * P * sizeof(int),
+                    (size_t)nroots * P * sizeof(T),
+                    (size_t)nroots * P * sizeof(int)};
+  Carve dry{nullptr, NOALLOC_BYTES};
+  for (size_t s : sizes) dry.take_off(s);
+  if (dry.used > NOALLOC_BYTES) {
+    const size_t per_point = (dry.used - prog.size() * sizeof(DigitEntry)) / (size_t)std::max<int64_t>(P, 1) + 1;
+    fail(TNFA_ERR_INVALID_ARGUMENT,
+         "tnfa_evaluate_noalloc: " + std::to_string(P) + " points need " +
+             std::to_string(dry.used) + " bytes of scratch, above the fixed " +
+             std::to_string(NOALLOC_BYTES) + "; this network allows about " +
+             std::to_string(NOALLOC_BYTES / per_point) + " points per call");
+  }
+  Carve cv{noalloc_base(ctx->device), NOALLOC_BYTES};
+  DigitEntry* dprog = (DigitEntry*)cv.take(sizes[0]);
+  uint8_t* dS = (uint8_t*)cv.take(sizes[1]);
+  int* dperm = (int*)cv.take(sizes[2]);
+  int* meta = (int*)cv.take(sizes[3]);
+  int* derr = (int*)cv.take(sizes[4]);
+  T* slots = (T*)cv.take(sizes[5]);
+  int* slote = (int*)cv.take(sizes[6]);
+  T* rootv = (T*)cv.take(sizes[7]);
+  int* roote = (int*)cv.take(sizes[8]);
+  const int Pc = (int)P;
+  // the array keeps the previous call's contents: clear what must start at 0
+  TNFA_CUDA(cudaMemsetAsync(derr, 0, 4, ctx->stream));
+  TNFA_CUDA(cudaMemsetAsync(dS, 0, (size_t)V * P, ctx->stream));
+  if (!prog.empty()) {
+    TNFA_CUDA(cudaMemcpyAsync(dprog, prog.data(), sizes[0], cudaMemcpyHostToDevice, ctx->stream));
+    k_digitize<<<grid_for(Pc, 256, 8 * 152 * 8), 256, 0, ctx->stream>>>(
+        X, ncols, Pc, dprog, (int)prog.size(), dS, (int64_t)P, derr);
+    TNFA_LAUNCH_CHECK();
+  }
+  std::vector<int> root_index(V, -1);
+  for (int r = 0; r < nroots; ++r) root_index[plan.roots[r]] = r;
+  for (int v : plan.order) {
+    VertexJob<T> j{};
+    j.nchild = (int)Tp.children[v].size();
+    TNFA_CHECK(j.nchild <= EVAL_MAXC, TNFA_ERR_UNSUPPORTED, "vertex degree too high");
+    int64_t K = 1;
+    int sumdim = 0;
+    for (int i = 0; i < j.nchild; ++i) {
+      const int c = Tp.children[v][i];
+      ChildSrc<T>& s = j.ch[i];
+      s.dim = Tp.link[c];
+      sumdim += s.dim;
+      K *= s.dim;
+      if (plan.fused_leaf[c]) {
+        s.ptr = tensors + Tp.off[c];
+        s.exps = nullptr;
+        s.S = dS + (int64_t)c * P;
+      } else {
+        s.ptr = slots + (size_t)plan.slot[c] * slot_vals;
+        s.exps = slote + (size_t)plan.slot[c] * P;
+        s.S = nullptr;
+      }
+    }
+    TNFA_CHECK(K < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "contraction too large");
+    j.K = (int)K;
+    j.chi_a = Tp.link[v];
+    j.site_dim = Tp.site_dim[v];
+    j.B = tensors + Tp.off[v];
+    j.Pc = Pc;
+    if (Tp.parent[v] < 0) {
+      j.out = rootv + (size_t)root_index[v] * P;
+      j.out_exp = roote + (size_t)root_index[v] * P;
+    } else {
+      j.out = slots + (size_t)plan.slot[v] * slot_vals;
+      j.out_exp = slote + (size_t)plan.slot[v] * P;
+    }
+    const int tp = contract_tile_rows(j.chi_a, sumdim, sizeof(T));
+    const int ng = j.site_dim;
+    j.ngroups = ng;
+    j.grp_off = meta;
+    j.grp_cnt = meta + ng;
+    j.tile_start = meta + 2 * ng;
+    if (ng == 1) {
+      k_group_identity<<<1, 1, 0, ctx->stream>>>(meta, Pc, tp);
+      TNFA_LAUNCH_CHECK();
+      j.perm = nullptr;
+    } else {
+      TNFA_CHECK(ng <= 256, TNFA_ERR_UNSUPPORTED, "site dimension above 256 per vertex");
+      const uint8_t* Sv = dS + (int64_t)v * P;
+      TNFA_CUDA(cudaMemsetAsync(meta + ng, 0, ng * sizeof(int), ctx->stream));
+      k_group_count<<<grid_for(Pc, 256, 4 * 152), 256, 0, ctx->stream>>>(Sv, Pc, ng, meta + ng);
+      k_group_scan<<<1, 1, 0, ctx->stream>>>(meta, ng, tp);
+      const unsigned gs = (unsigned)((Pc + 256 * SCATTER_ITEMS - 1) / (256 * SCATTER_ITEMS));
+      k_group_scatter<<<gs, 256, 0, ctx->stream>>>(Sv, Pc, ng, meta + 3 * ng + 1, dperm);
+      TNFA_LAUNCH_CHECK();
+      j.perm = dperm;
+    }
+    launch_contract<T>(ctx, j, Pc);
+  }
+  k_combine<T><<<grid_for(Pc, 256, 8192), 256, 0, ctx->stream>>>(rootv, roote, nroots, Pc, out,
+                                                                   out_kind, P, 0);
+  TNFA_LAUNCH_CHECK();
+  int herr = 0;
+  TNFA_CUDA(cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  TNFA_CHECK(herr == 0, TNFA_ERR_DOMAIN,
+             "a coordinate is negative or not finite (the digit map needs x >= 0)");
+}
+
+}  // namespace
+}  // namespace tnfa
+
+extern "C" int tnfa_evaluate_noalloc(tnfa_ctx* ctx, const tnfa_net* net, const double* X,
+                                     int64_t n_points, int32_t n_dims, const int32_t* dims,
+                                     void* out, int out_kind, int precision) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(net, "evaluate_noalloc");
+  TNFA_CHECK(n_points >= 0, TNFA_ERR_INVALID_ARGUMENT, "n_points < 0");
+  if (n_points == 0) return TNFA_OK;
+  TNFA_CHECK(X && out && (n_dims == 0 || dims), TNFA_ERR_INVALID_ARGUMENT, "null X, out or dims");
+  TNFA_CHECK(n_dims >= 0 && n_dims <= 64, TNFA_ERR_INVALID_ARGUMENT, "n_dims out of range");
+  TNFA_CHECK(n_points < (int64_t(1) << 31), TNFA_ERR_INVALID_ARGUMENT, "too many points");
+  for (int v = 0; v < net->topo.V; ++v)
+    TNFA_CHECK(net->topo.site_dim[v] <= 256, TNFA_ERR_UNSUPPORTED, "site dimension above 256");
+  int ncols = 0;
+  std::vector<DigitEntry> prog = make_digit_program(net->topo, n_dims, dims, &ncols);
+  if (net->dtype == TNFA_C128) {
+    TNFA_CHECK(out_kind == TNFA_OUT_C128 && precision == TNFA_PREC_F64, TNFA_ERR_DTYPE,
+               "complex networks: TNFA_OUT_C128 and TNFA_PREC_F64");
+    evaluate_noalloc_impl<cplx>(ctx, net, (const cplx*)net->d, X, n_points, ncols, prog, out,
+                                out_kind);
+  } else {
+    TNFA_CHECK(out_kind == TNFA_OUT_F64 || out_kind == TNFA_OUT_F32 ||
+                   out_kind == TNFA_OUT_F32_SCALED,
+               TNFA_ERR_DTYPE, "real networks need a real output kind");
+    if (precision == TNFA_PREC_F64 && net->dtype == TNFA_F64)
+      evaluate_noalloc_impl<double>(ctx, net, (const double*)net->d, X, n_points, ncols, prog, out,
+                                    out_kind);
+    else if (precision == TNFA_PREC_F32 && net->dtype == TNFA_F32)
+      evaluate_noalloc_impl<float>(ctx, net, (const float*)net->d, X, n_points, ncols, prog, out,
+                                   out_kind);
+    else
+      fail(TNFA_ERR_UNSUPPORTED,
+           "tnfa_evaluate_noalloc computes in the network's own type: TNFA_PREC_F64 on FP64 "
+           "networks or TNFA_PREC_F32 on FP32 networks");
+  }
+  TNFA_API_END
+}

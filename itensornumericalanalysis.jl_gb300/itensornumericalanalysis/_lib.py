@@ -127,6 +127,10 @@ SIGNATURES = {
         C.c_int,
         [_P, _P, _P, _I64, _I32, _PI32, C.c_int, _P, C.c_int, C.c_int, C.c_int],
     ),
+    "tnfa_evaluate_noalloc": (
+        C.c_int,
+        [_P, _P, _P, _I64, _I32, _PI32, _P, C.c_int, C.c_int],
+    ),
     "tnfa_integrate": (C.c_int, [_P, _P, C.c_int, _PD]),
     "tnfa_integrate_operator": (C.c_int, [_P, _P, _P, C.c_int, _PD]),
     "tnfa_partial_integrate": (C.c_int, [_P, _P, _I32, _PI32, C.c_int, _PP]),
