@@ -271,9 +271,12 @@ int tnfa_linsolve(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnf
 /* ---- differentiation ----------------------------------------------------- */
 
 /* Vector-Jacobian product of batched evaluation: dtensors += sum_p dout[p] *
- * d f(x_p) / d tensors, canonical layout, real networks, FP64 or FP32 per
- * the network dtype.  No reference counterpart (the reference has no AD);
- * it backs the rrule of evaluate. */
+ * d f(x_p) / d tensors (dout: n_points doubles; dtensors: n_elements scalars of
+ * the network's type in canonical layout, accumulated into).  Computed in the
+ * network's type (FP64, FP32 or complex128; for complex networks the result is
+ * the holomorphic derivative sum_p dout_p d f_p / d T, not conjugated).  No
+ * reference counterpart (the reference has no AD); it backs the rrule of
+ * evaluate. */
 int tnfa_evaluate_vjp(tnfa_ctx* ctx, const tnfa_net* net, const double* X, int64_t n_points,
                       int32_t n_dims, const int32_t* dims, int x_memory, const double* dout,
                       int dout_memory, void* dtensors, int dtensors_memory);

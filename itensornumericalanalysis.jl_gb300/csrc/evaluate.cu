@@ -978,3 +978,351 @@ extern "C" int tnfa_evaluate_noalloc(tnfa_ctx* ctx, const tnfa_net* net, const d
   }
   TNFA_API_END
 }
+
+// ----------------------------------------------- vector-Jacobian product ----
+// d/dT of sum_p dout_p f(x_p).  For vertex v with outside message E_v (the
+// contraction of everything but v's subtree, as a vector over v's parent
+// bond) and inside messages m_c of its children,
+//   dT_v[s][a][c1..ck] += sum_{p: s_v(p) = s} dout_p E_v[p][a] prod_j m_cj[p][c_j].
+// Inside messages come from the forward contraction (kept for every vertex);
+// E of a child is the same contraction with that child's bond as the output
+// (the vertex tensor with the child's axis moved first, E_v as one more input);
+// the accumulation treats E_v as one more Kronecker factor and reduces over
+// the points of each digit group (split over point tiles, atomics per tile).
+#include "linalg.cuh"
+
+namespace tnfa {
+namespace {
+
+template <class T>
+__device__ inline void atomic_add_T(T* a, T v);
+template <>
+__device__ inline void atomic_add_T<double>(double* a, double v) { atomicAdd(a, v); }
+template <>
+__device__ inline void atomic_add_T<float>(float* a, float v) { atomicAdd(a, v); }
+template <>
+__device__ inline void atomic_add_T<cplx>(cplx* a, cplx v) {
+  atomicAdd(&a->re, v.re);
+  atomicAdd(&a->im, v.im);
+}
+
+template <class T, int TP>
+__global__ void __launch_bounds__(256) k_grad_acc(const VertexJob<T> j, T* __restrict__ dT) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int row0, nrows, g;
+  if (!locate_tile(j, TP, blockIdx.x, row0, nrows, g)) return;
+  int sumdim = 0;
+  for (int c = 0; c < j.nchild; ++c) sumdim += j.ch[c].dim;
+  T* rows = (T*)smem_raw;
+  T* scale = rows + (int64_t)sumdim * TP;
+  int* pts = (int*)(scale + TP);
+  int* eacc = pts + TP;
+  for (int r = threadIdx.x; r < TP; r += blockDim.x) {
+    pts[r] = r < nrows ? (j.perm ? j.perm[row0 + r] : row0 + r) : 0;
+    eacc[r] = 0;
+  }
+  __syncthreads();
+  load_children(j, pts, nrows, TP, rows, eacc);
+  for (int r = threadIdx.x; r < nrows; r += blockDim.x) scale[r] = Sc<T>::scale2(Sc<T>::one(), eacc[r]);
+  __syncthreads();
+  const int k = blockIdx.y * blockDim.x + threadIdx.x;
+  if (k >= j.K) return;
+  T acc = Sc<T>::zero();
+  for (int r = 0; r < nrows; ++r) acc = Sc<T>::fma(scale[r], kr_entry(j, rows, TP, r, k), acc);
+  atomic_add_T<T>(dT + (int64_t)g * j.K + k, acc);
+}
+
+template <class T>
+__global__ void k_vjp_seed(const double* __restrict__ dout, const T* __restrict__ rootv,
+                           const int* __restrict__ roote, int nroots, int r, int Pc, T* __restrict__ E,
+                           int* __restrict__ Eexp) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < Pc; p += gridDim.x * blockDim.x) {
+    T v = Sc<T>::one();
+    if constexpr (sizeof(T) == 16)
+      v = T{dout[p], 0.0};
+    else
+      v = (T)dout[p];
+    int e = 0;
+    for (int q = 0; q < nroots; ++q) {
+      if (q == r) continue;
+      v = v * rootv[(int64_t)q * Pc + p];
+      e += roote[(int64_t)q * Pc + p];
+    }
+    E[p] = v;
+    Eexp[p] = e;
+  }
+}
+
+// Group the points of a chunk by the site value of vertex v (fills the job's
+// group fields; tp = tile rows of the kernel that will consume them).
+template <class T>
+void group_by_site(tnfa_ctx* ctx, VertexJob<T>& j, const uint8_t* Sv, int Pc, int ng, int tp,
+                   int* meta, int* perm) {
+  j.ngroups = ng;
+  j.grp_off = meta;
+  j.grp_cnt = meta + ng;
+  j.tile_start = meta + 2 * ng;
+  if (ng == 1) {
+    k_group_identity<<<1, 1, 0, ctx->stream>>>(meta, Pc, tp);
+    TNFA_LAUNCH_CHECK();
+    j.perm = nullptr;
+    return;
+  }
+  TNFA_CHECK(ng <= 256, TNFA_ERR_UNSUPPORTED, "site dimension above 256 per vertex");
+  TNFA_CUDA(cudaMemsetAsync(meta + ng, 0, ng * sizeof(int), ctx->stream));
+  KernelScope ks(ctx, "group", 0.0, (double)Pc * 6.0);
+  k_group_count<<<grid_for(Pc, 256, 4 * 152), 256, 0, ctx->stream>>>(Sv, Pc, ng, meta + ng);
+  k_group_scan<<<1, 1, 0, ctx->stream>>>(meta, ng, tp);
+  const unsigned gs = (unsigned)((Pc + 256 * SCATTER_ITEMS - 1) / (256 * SCATTER_ITEMS));
+  k_group_scatter<<<gs, 256, 0, ctx->stream>>>(Sv, Pc, ng, meta + 3 * ng + 1, perm);
+  TNFA_LAUNCH_CHECK();
+  j.perm = perm;
+}
+
+template <class T>
+void vjp_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, const double* X, int64_t P,
+              int ncols, const std::vector<DigitEntry>& prog, int xmem, const double* dout,
+              int dout_mem, T* dT) {
+  const Topo& Tp = net->topo;
+  const int V = Tp.V;
+  EvalPlan plan = make_plan(Tp);
+  const int nroots = (int)plan.roots.size();
+  std::vector<int> root_index(V, -1);
+  for (int r = 0; r < nroots; ++r) root_index[plan.roots[r]] = r;
+  size_t per_point = V + 4 + (xmem == TNFA_MEM_HOST ? ncols * 8 : 0) +
+                     (dout_mem == TNFA_MEM_HOST ? 8 : 0) + nroots * (sizeof(T) + 4);
+  for (int v = 0; v < V; ++v) per_point += 2 * ((size_t)Tp.link[v] * sizeof(T) + 4);
+  int64_t Pc_max = (int64_t)(ctx->eval_budget / per_point);
+  Pc_max = std::max<int64_t>(256, std::min<int64_t>(Pc_max, int64_t(1) << 30));
+  const int Pcap = (int)std::max<int64_t>(std::min<int64_t>(P, (Pc_max / 256) * 256), 1);
+  int maxsd = 1;
+  for (int v = 0; v < V; ++v) maxsd = std::max(maxsd, Tp.site_dim[v]);
+  DBuf dprog(ctx, prog.size() * sizeof(DigitEntry));
+  if (!prog.empty())
+    TNFA_CUDA(cudaMemcpyAsync(dprog.p, prog.data(), prog.size() * sizeof(DigitEntry),
+                              cudaMemcpyHostToDevice, ctx->stream));
+  DBuf dS(ctx, (size_t)V * Pcap), dperm(ctx, (size_t)Pcap * 4);
+  DBuf dmeta(ctx, group_meta_ints(maxsd) * 4), derr(ctx, 4);
+  TNFA_CUDA(cudaMemsetAsync(derr.p, 0, 4, ctx->stream));
+  std::vector<DBuf> in(V), ine(V), E(V), Ee(V);
+  for (int v = 0; v < V; ++v) {
+    if (!plan.fused_leaf[v]) {
+      in[v] = DBuf(ctx, (size_t)Pcap * Tp.link[v] * sizeof(T));
+      ine[v] = DBuf(ctx, (size_t)Pcap * 4);
+    }
+    E[v] = DBuf(ctx, (size_t)Pcap * Tp.link[v] * sizeof(T));
+    Ee[v] = DBuf(ctx, (size_t)Pcap * 4);
+  }
+  DBuf droot(ctx, (size_t)nroots * Pcap * sizeof(T)), droote(ctx, (size_t)nroots * Pcap * 4);
+  DBuf dX(ctx, xmem == TNFA_MEM_HOST ? (size_t)Pcap * ncols * 8 : 0);
+  DBuf ddout(ctx, dout_mem == TNFA_MEM_HOST ? (size_t)Pcap * 8 : 0);
+  int* meta = dmeta.as<int>();
+  auto inside_src = [&](int c) {
+    ChildSrc<T> s{};
+    s.dim = Tp.link[c];
+    if (plan.fused_leaf[c]) {
+      s.ptr = tensors + Tp.off[c];
+      s.exps = nullptr;
+      s.S = dS.as<uint8_t>() + (int64_t)c * Pcap;
+    } else {
+      s.ptr = in[c].as<T>();
+      s.exps = ine[c].as<int>();
+      s.S = nullptr;
+    }
+    return s;
+  };
+  for (int64_t p0 = 0; p0 < P; p0 += Pcap) {
+    const int Pc = (int)std::min<int64_t>(Pcap, P - p0);
+    const double* Xc = X + p0 * ncols;
+    if (xmem == TNFA_MEM_HOST) {
+      TNFA_CUDA(cudaMemcpyAsync(dX.p, Xc, (size_t)Pc * ncols * 8, cudaMemcpyHostToDevice, ctx->stream));
+      Xc = dX.as<double>();
+    }
+    const double* dc = dout + p0;
+    if (dout_mem == TNFA_MEM_HOST) {
+      TNFA_CUDA(cudaMemcpyAsync(ddout.p, dc, (size_t)Pc * 8, cudaMemcpyHostToDevice, ctx->stream));
+      dc = ddout.as<double>();
+    }
+    TNFA_CUDA(cudaMemsetAsync(dS.p, 0, (size_t)V * Pcap, ctx->stream));
+    if (!prog.empty()) {
+      KernelScope ks(ctx, "digitize", 0.0, (double)Pc * (ncols * 8.0 + V));
+      k_digitize<<<grid_for(Pc, 256, 8 * 152 * 8), 256, 0, ctx->stream>>>(
+          Xc, ncols, Pc, dprog.as<DigitEntry>(), (int)prog.size(), dS.as<uint8_t>(), (int64_t)Pcap,
+          derr.as<int>());
+      TNFA_LAUNCH_CHECK();
+    }
+    // forward: inside messages of every non-leaf vertex
+    for (int v : plan.order) {
+      VertexJob<T> j{};
+      j.nchild = (int)Tp.children[v].size();
+      TNFA_CHECK(j.nchild <= EVAL_MAXC, TNFA_ERR_UNSUPPORTED, "vertex degree too high");
+      int64_t K = 1;
+      int sumdim = 0;
+      for (int i = 0; i < j.nchild; ++i) {
+        j.ch[i] = inside_src(Tp.children[v][i]);
+        K *= j.ch[i].dim;
+        sumdim += j.ch[i].dim;
+      }
+      j.K = (int)K;
+      j.chi_a = Tp.link[v];
+      j.site_dim = Tp.site_dim[v];
+      j.B = tensors + Tp.off[v];
+      j.Pc = Pc;
+      if (Tp.parent[v] < 0) {
+        j.out = (T*)droot.p + (size_t)root_index[v] * Pcap;
+        j.out_exp = droote.as<int>() + (size_t)root_index[v] * Pcap;
+      } else {
+        j.out = in[v].as<T>();
+        j.out_exp = ine[v].as<int>();
+      }
+      group_by_site(ctx, j, dS.as<uint8_t>() + (int64_t)v * Pcap, Pc, j.site_dim,
+                    contract_tile_rows(j.chi_a, sumdim, sizeof(T)), meta, dperm.as<int>());
+      launch_contract<T>(ctx, j, Pc);
+    }
+    // seeds: E of a root = dout times the other roots' values
+    for (int r = 0; r < nroots; ++r)
+      k_vjp_seed<T><<<grid_for(Pc, 256, 4096), 256, 0, ctx->stream>>>(
+          dc, (const T*)droot.p, droote.as<int>(), nroots, r, Pcap, E[plan.roots[r]].as<T>(),
+          Ee[plan.roots[r]].as<int>());
+    TNFA_LAUNCH_CHECK();
+    // top-down: outside messages of every child
+    for (int v = 0; v < V; ++v) {
+      const auto& kids = Tp.children[v];
+      std::vector<int> shp{Tp.site_dim[v], Tp.link[v]};
+      for (int c : kids) shp.push_back(Tp.link[c]);
+      for (size_t jx = 0; jx < kids.size(); ++jx) {
+        const int c = kids[jx];
+        // T_v with child c's axis moved to position 1: [s][c][parent][others]
+        DBuf perm_t(ctx, (size_t)Tp.size(v) * sizeof(T));
+        la::PermJob pj{};
+        pj.src = tensors + Tp.off[v];
+        pj.dst = perm_t.p;
+        pj.nd = (int)shp.size();
+        TNFA_CHECK(pj.nd <= la::MAXD, TNFA_ERR_UNSUPPORTED, "vertex degree too high");
+        std::vector<int> order;
+        order.push_back(0);
+        order.push_back(2 + (int)jx);
+        for (int a = 1; a < pj.nd; ++a)
+          if (a != 2 + (int)jx) order.push_back(a);
+        pj.n = Tp.size(v);
+        for (int a = 0; a < pj.nd; ++a) {
+          pj.shape[a] = shp[a];
+          pj.perm[a] = order[a];
+        }
+        la::permute<T>(ctx, {pj});
+        VertexJob<T> j{};
+        j.nchild = 0;
+        ChildSrc<T> e{};
+        e.ptr = E[v].as<T>();
+        e.exps = Ee[v].as<int>();
+        e.S = nullptr;
+        e.dim = Tp.link[v];
+        j.ch[j.nchild++] = e;
+        int64_t K = e.dim;
+        int sumdim = e.dim;
+        for (size_t q = 0; q < kids.size(); ++q) {
+          if (q == jx) continue;
+          TNFA_CHECK(j.nchild < EVAL_MAXC, TNFA_ERR_UNSUPPORTED, "vertex degree too high");
+          j.ch[j.nchild++] = inside_src(kids[q]);
+          K *= Tp.link[kids[q]];
+          sumdim += Tp.link[kids[q]];
+        }
+        j.K = (int)K;
+        j.chi_a = Tp.link[c];
+        j.site_dim = Tp.site_dim[v];
+        j.B = perm_t.as<T>();
+        j.Pc = Pc;
+        j.out = E[c].as<T>();
+        j.out_exp = Ee[c].as<int>();
+        group_by_site(ctx, j, dS.as<uint8_t>() + (int64_t)v * Pcap, Pc, j.site_dim,
+                      contract_tile_rows(j.chi_a, sumdim, sizeof(T)), meta, dperm.as<int>());
+        launch_contract<T>(ctx, j, Pc);
+      }
+    }
+    // accumulation: dT_v[s][(a, c...)] += sum_p E_v[p][a] prod m_c[p][c]
+    for (int v = 0; v < V; ++v) {
+      VertexJob<T> j{};
+      ChildSrc<T> e{};
+      e.ptr = E[v].as<T>();
+      e.exps = Ee[v].as<int>();
+      e.S = nullptr;
+      e.dim = Tp.link[v];
+      j.ch[j.nchild++] = e;
+      int64_t K = e.dim;
+      int sumdim = e.dim;
+      for (int c : Tp.children[v]) {
+        TNFA_CHECK(j.nchild < EVAL_MAXC, TNFA_ERR_UNSUPPORTED, "vertex degree too high");
+        j.ch[j.nchild++] = inside_src(c);
+        K *= Tp.link[c];
+        sumdim += Tp.link[c];
+      }
+      TNFA_CHECK(K < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "gradient block too large");
+      j.K = (int)K;
+      j.chi_a = 1;
+      j.site_dim = Tp.site_dim[v];
+      j.Pc = Pc;
+      constexpr int TP = 64;
+      group_by_site(ctx, j, dS.as<uint8_t>() + (int64_t)v * Pcap, Pc, j.site_dim, TP, meta,
+                    dperm.as<int>());
+      const size_t sm = (size_t)sumdim * TP * sizeof(T) + TP * sizeof(T) + 2 * TP * sizeof(int);
+      TNFA_CHECK(sm <= 200 * 1024, TNFA_ERR_UNSUPPORTED, "bonds too large for the gradient kernel");
+      if (sm > 48 * 1024)
+        TNFA_CUDA(cudaFuncSetAttribute(k_grad_acc<T, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sm));
+      dim3 grid((unsigned)((Pc + TP - 1) / TP + j.ngroups), (unsigned)((K + 255) / 256));
+      KernelScope ks(ctx, "grad_acc", 2.0 * Pc * (double)K, 0.0);
+      k_grad_acc<T, TP><<<grid, 256, sm, ctx->stream>>>(j, dT + Tp.off[v]);
+      TNFA_LAUNCH_CHECK();
+    }
+  }
+  int herr = 0;
+  TNFA_CUDA(cudaMemcpyAsync(&herr, derr.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  TNFA_CHECK(herr == 0, TNFA_ERR_DOMAIN,
+             "a coordinate is negative or not finite (the digit map needs x >= 0)");
+}
+
+}  // namespace
+}  // namespace tnfa
+
+extern "C" int tnfa_evaluate_vjp(tnfa_ctx* ctx, const tnfa_net* net, const double* X,
+                                 int64_t n_points, int32_t n_dims, const int32_t* dims,
+                                 int x_memory, const double* dout, int dout_memory, void* dtensors,
+                                 int dtensors_memory) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(net, "evaluate_vjp");
+  TNFA_CHECK(n_points >= 0, TNFA_ERR_INVALID_ARGUMENT, "n_points < 0");
+  if (n_points == 0) return TNFA_OK;
+  TNFA_CHECK(X && dout && dtensors && (n_dims == 0 || dims), TNFA_ERR_INVALID_ARGUMENT,
+             "null X, dout, dtensors or dims");
+  for (int m : {x_memory, dout_memory, dtensors_memory})
+    TNFA_CHECK(m == TNFA_MEM_HOST || m == TNFA_MEM_DEVICE, TNFA_ERR_INVALID_ARGUMENT, "bad memory kind");
+  for (int v = 0; v < net->topo.V; ++v)
+    TNFA_CHECK(net->topo.site_dim[v] <= 256, TNFA_ERR_UNSUPPORTED, "site dimension above 256");
+  int ncols = 0;
+  std::vector<DigitEntry> prog = make_digit_program(net->topo, n_dims, dims, &ncols);
+  const size_t es = dtype_size(net->dtype);
+  const size_t bytes = (size_t)net->topo.n_elem * es;
+  DBuf acc;
+  void* dT = dtensors;
+  if (dtensors_memory == TNFA_MEM_HOST) {
+    acc = DBuf(ctx, bytes);
+    TNFA_CUDA(cudaMemcpyAsync(acc.p, dtensors, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    dT = acc.p;
+  }
+  if (net->dtype == TNFA_F64)
+    vjp_impl<double>(ctx, net, (const double*)net->d, X, n_points, ncols, prog, x_memory, dout,
+                     dout_memory, (double*)dT);
+  else if (net->dtype == TNFA_F32)
+    vjp_impl<float>(ctx, net, (const float*)net->d, X, n_points, ncols, prog, x_memory, dout,
+                    dout_memory, (float*)dT);
+  else
+    vjp_impl<cplx>(ctx, net, (const cplx*)net->d, X, n_points, ncols, prog, x_memory, dout,
+                   dout_memory, (cplx*)dT);
+  if (dtensors_memory == TNFA_MEM_HOST) {
+    TNFA_CUDA(cudaMemcpyAsync(dtensors, acc.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  TNFA_API_END
+}

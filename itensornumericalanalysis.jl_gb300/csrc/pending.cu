@@ -20,9 +20,5 @@ int tnfa_linsolve(tnfa_ctx* ctx, const tnfa_net*, const tnfa_net*, const tnfa_ne
                   const tnfa_linsolve_params*, tnfa_net**, double*) {
   TNFA_PENDING("tnfa_linsolve")
 }
-int tnfa_evaluate_vjp(tnfa_ctx* ctx, const tnfa_net*, const double*, int64_t, int32_t,
-                      const int32_t*, int, const double*, int, void*, int) {
-  TNFA_PENDING("tnfa_evaluate_vjp")
-}
 
 }  // extern "C"

@@ -67,6 +67,7 @@ from .indexmap import (
     real_continuous_siteinds,
     reduced_indsnetworkmap,
 )
+from .grad import TTNEvaluate, evaluate_vjp
 from .integration import integrate, partial_integrate
 from .network import ITensorNetworkFunction, calculate_fx, evaluate, inner
 from .operate import operate

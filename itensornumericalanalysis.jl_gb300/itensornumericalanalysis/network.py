@@ -76,6 +76,21 @@ class ITensorNetworkFunction:
                  _lib.MEM_HOST, C.byref(h))
         return cls(s, h, ctx, legs)
 
+    def with_tensors_device(self, flat) -> "ITensorNetworkFunction":
+        """A network with this one's shape and tensors from a flat device
+        buffer (anything with data_ptr(), e.g. a CUDA torch tensor) in
+        canonical layout; FP64 or FP32 from the buffer's element size."""
+        _, _, ne, link = self.info()
+        es = flat.element_size()
+        dtype = {8: _lib.F64, 4: _lib.F32}[es]
+        if flat.numel() != ne:
+            raise ValueError(f"flat buffer has {flat.numel()} elements, network needs {ne}")
+        topo, keep = topology_struct(self.s, link, self._legs)
+        h = C.c_void_p()
+        self._ctx.call("tnfa_net_create", C.byref(topo), dtype, C.c_void_p(flat.data_ptr()),
+                       _lib.MEM_DEVICE, C.byref(h))
+        return self._wrap(h)
+
     def _wrap(self, handle: C.c_void_p, s: IndsNetworkMap | None = None, legs="same"):
         return type(self)(s or self.s, handle, self._ctx, self._legs if legs == "same" else legs)
 

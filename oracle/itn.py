@@ -21,7 +21,7 @@ __all__ = [
     "delta_p", "random_net", "net_add", "net_multiply", "net_scale",
     "evaluate", "integrate", "dense", "dense_grid_1d",
     "forward_shift_terms", "backward_shift_terms", "stencil_terms", "apply_terms_dense",
-    "bond_spectrum",
+    "bond_spectrum", "gradient",
 ]
 
 _next_id = itertools.count()
@@ -642,3 +642,26 @@ def bond_spectrum(F: np.ndarray, left_axes) -> np.ndarray:
     rest = [a for a in range(F.ndim) if a not in left]
     M = np.transpose(F, left + rest).reshape(int(np.prod([F.shape[a] for a in left])), -1)
     return np.linalg.svd(M, compute_uv=False)
+
+
+def gradient(f: Net, X, dims, dout) -> dict:
+    """sum_p dout_p d f(x_p) / d T_v for every vertex: f is linear in each
+    T_v, so the derivative at a point is the environment of v (every other
+    tensor sliced at the point's digits and contracted), placed at the slice
+    of v's own site value.  Arrays use the order site inds + links of f.T[v]."""
+    out = {v: np.zeros(f.T[v].arr.shape, dtype=np.result_type(f.T[v].arr, float)) for v in f.s.verts}
+    for x, w in zip(X, dout):
+        iv = calculate_ind_values(f.s, list(x), dims)
+        sliced = {}
+        for v in f.s.verts:
+            t = f.T[v]
+            for i in f.s.site[v]:
+                t = t * onehot(i, iv[i])
+            sliced[v] = t
+        for v in f.s.verts:
+            env = contract([sliced[u] for u in f.s.verts if u != v])
+            links = [i for i in f.T[v].inds if i not in f.s.site[v]]
+            env = env.permute(links) if links else env
+            idx = tuple(iv[i] for i in f.s.site[v])
+            out[v][idx] += w * env.arr
+    return out

@@ -29,12 +29,18 @@ def test_config1_fixture(ina):
     s = ina.continuous_siteinds(ina.named_grid((12, 1)))
     f = ina.exp_itn(s, k=-1.0) + ina.sin_itn(s, k=2 * np.pi)
     assert np.max(np.abs(f.evaluate_batch(d["X"]) - d["f"])) < 1e-12
-    g = ina.operate(ina.second_derivative_operator(s), f, cutoff=1e-15)
+    op = ina.second_derivative_operator(s)
     scale = np.max(np.abs(d["d2f_grid"]))
-    assert np.max(np.abs(g.evaluate_batch(d["X"]) - d["d2f"])) / scale < 1e-10
     xs = np.arange(2**12) / 2**12
+    # cutoff 0: the exact product, up to rounding
+    g = ina.operate(op, f, cutoff=0.0)
+    assert np.max(np.abs(g.evaluate_batch(d["X"]) - d["d2f"])) / scale < 1e-10
     assert np.max(np.abs(g.evaluate_batch(xs) - d["d2f_grid"])) / scale < 1e-10
     assert abs(ina.integrate(g) - d["integral_d2f"]) / scale < 1e-10
+    # cutoff 1e-15: each bond may drop sqrt(1e-15) of the 2-norm
+    gt = ina.operate(op, f, cutoff=1e-15)
+    err = np.linalg.norm(gt.evaluate_batch(xs) - d["d2f_grid"])
+    assert err <= 11 * np.sqrt(1e-15) * np.linalg.norm(d["d2f_grid"])
 
 
 @pytest.mark.parametrize("boundary", ["Dirichlet", "Periodic", "Neumann"])

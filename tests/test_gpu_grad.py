@@ -1,0 +1,108 @@
+"""Gradient (VJP) of batched evaluation on the GPU: against the oracle's
+environment gradient, central finite differences, FP32 vs FP64, and a short
+fit through the autograd wrapper (the config-4 workflow at reduced size)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from _helpers import oracle_to_tensors, upload_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _grad_to_layout(net, grads, s_prod):
+    tmp = O.Net(net.s, {v: O.Tensor(grads[v], net.T[v].inds) for v in net.s.verts}, net.link)
+    return oracle_to_tensors(tmp, s_prod)
+
+
+@pytest.mark.parametrize("gname", ["binary7", "comb3x3"])
+def test_vjp_matches_oracle_gradient(ina, gname):
+    graph = {"binary7": O.binary_tree_graph(7), "comb3x3": O.comb_tree_graph((3, 3))}[gname]
+    rng = np.random.default_rng(50)
+    s_or = O.siteinds(graph, map_dimension=2)
+    net = O.random_net(s_or, 3, rng)
+    f, s = upload_oracle(ina, graph, net)
+    X = rng.random((40, 2))
+    dout = rng.standard_normal(40)
+    got = ina.evaluate_vjp(f, X, dout, [1, 2])
+    ref = _grad_to_layout(net, O.gradient(net, X, [1, 2], dout), s)
+    scale = max(np.max(np.abs(r)) for r in ref.values())
+    for v in s.layout.order:
+        assert np.max(np.abs(got[v] - ref[v])) <= 1e-11 * scale, v
+
+
+def test_vjp_central_differences(ina):
+    """f is linear in every tensor entry, so central differences are exact up
+    to rounding: h = 1e-3 as in the config-4 description."""
+    graph = O.path_graph(8)
+    rng = np.random.default_rng(51)
+    s_or = O.siteinds(graph, map_dimension=2)
+    net = O.random_net(s_or, 4, rng)
+    f, s = upload_oracle(ina, graph, net)
+    X = rng.random((64, 2))
+    dout = rng.standard_normal(64)
+    g = ina.evaluate_vjp(f, X, dout, [1, 2])
+    ts = f.tensors()
+    h = 1e-3
+    for _ in range(12):
+        v = s.layout.order[rng.integers(len(s.layout.order))]
+        idx = tuple(rng.integers(d) for d in ts[v].shape)
+        tp = {k: a.copy() for k, a in ts.items()}
+        tm = {k: a.copy() for k, a in ts.items()}
+        tp[v][idx] += h
+        tm[v][idx] -= h
+        fp = ina.ITensorNetworkFunction.from_tensors(s, tp).evaluate_batch(X, [1, 2])
+        fm = ina.ITensorNetworkFunction.from_tensors(s, tm).evaluate_batch(X, [1, 2])
+        fd = np.dot(dout, fp - fm) / (2 * h)
+        assert abs(fd - g[v][idx]) <= 1e-9 * max(1.0, abs(fd)), (v, idx, fd, g[v][idx])
+
+
+def test_vjp_fp32_vs_fp64_config4_shape(ina):
+    """Comb 2 x 12 (a 24-site path), chi 8, N(0, 0.1^2) tensors: FP32 gradient
+    agrees with FP64."""
+    L = 12
+    g = ina.named_comb_tree((2, L))
+    s = ina.continuous_siteinds(g, [[(1, j) for j in range(L, 0, -1)], [(2, j) for j in range(1, L + 1)]])
+    f64 = ina.rand_itn(s, link_space=8, rng=52)
+    ts = {v: 0.1 * a for v, a in f64.tensors().items()}
+    f64 = ina.ITensorNetworkFunction.from_tensors(s, ts)
+    f32 = ina.ITensorNetworkFunction.from_tensors(s, ts, dtype=ina._lib.F32)
+    rng = np.random.default_rng(53)
+    X = rng.random((4096, 2))
+    dout = rng.standard_normal(4096)
+    a = ina.evaluate_vjp(f64, X, dout, [1, 2])
+    b = ina.evaluate_vjp(f32, X, dout, [1, 2])
+    num = np.sqrt(sum(np.sum((a[v] - b[v].astype(np.float64)) ** 2) for v in a))
+    den = np.sqrt(sum(np.sum(a[v] ** 2) for v in a))
+    assert num / den < 1e-4
+
+
+def test_fit_decreases_loss(ina):
+    """Gradient descent on sin(3x) cos(5y) exp(-(x^2 + y^2)) through the
+    autograd wrapper (config 4 at reduced size)."""
+    torch = pytest.importorskip("torch")
+    L = 8
+    g = ina.named_comb_tree((2, L))
+    s = ina.continuous_siteinds(g, [[(1, j) for j in range(L, 0, -1)], [(2, j) for j in range(1, L + 1)]])
+    chi = 4
+    f = ina.rand_itn(s, link_space=chi, rng=54)
+    # variance-preserving start (std 1/sqrt(2 chi)): outputs O(1), gradients alive
+    ts = {v: a / np.sqrt(2 * chi) for v, a in f.tensors().items()}
+    flat = np.concatenate([ts[v].ravel() for v in s.layout.order])
+    template = ina.ITensorNetworkFunction.from_tensors(s, ts)
+    params = torch.tensor(flat, dtype=torch.float64, device="cuda", requires_grad=True)
+    rng = np.random.default_rng(55)
+    Xh = rng.random((1 << 12, 2))
+    x, y = Xh[:, 0], Xh[:, 1]
+    target = torch.tensor(np.sin(3 * x) * np.cos(5 * y) * np.exp(-(x**2 + y**2)), device="cuda")
+    X = torch.tensor(Xh, device="cuda")
+    opt = torch.optim.Adam([params], lr=0.02)
+    losses = []
+    for _ in range(40):
+        opt.zero_grad()
+        pred = ina.TTNEvaluate.apply(params, X, template, [1, 2])
+        loss = torch.mean((pred - target) ** 2)
+        loss.backward()
+        opt.step()
+        losses.append(float(loss))
+    assert losses[-1] < 0.5 * losses[0], losses[::8]
