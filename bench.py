@@ -232,6 +232,95 @@ def run_reference(args, ws, rank):
     }), flush=True)
 
 
+def _timed(fn, reps=1):
+    import torch
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = fn()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / reps, out
+
+
+def secondary_measurements(ctx, ws, rank, args) -> dict:
+    """The other configurations of the metric, one timed repetition each after
+    a warm-up: batched MPO apply + truncate (512 uneven MPS, first derivative,
+    cutoff 1e-10, FP64), the reference's CPU case end to end (L = 20), and the
+    gradient of batched evaluation (comb 2 x 12, chi 32, FP32, 2^20 points)."""
+    import itensornumericalanalysis as ina
+    from itensornumericalanalysis.workloads import uneven_mps_batch, upload_batch
+
+    out = {}
+    # --- config 5: MPO apply + truncate of an uneven batch -------------------
+    batch = uneven_mps_batch(n=args.mps, seed=3)
+    fs = upload_batch(batch, ctx=ctx)
+    ops = {}
+    for s, _ in batch:
+        if s.nv() not in ops:
+            ops[s.nv()] = ina.first_derivative_operator(s)
+    oplist = [ops[s.nv()] for s, _ in batch]
+    ina.operate_batched(oplist[:8], fs[:8], cutoff=1e-10)  # warm-up (allocator, kernels)
+    ctx.kernel_stats(reset=True)
+    ctx.set_timing(True)
+    t, res = _timed(lambda: ina.operate_batched(oplist, fs, cutoff=1e-10))
+    ctx.set_timing(False)
+    st = ctx.kernel_stats(reset=True)
+    t = max_over_ranks(t, ws)
+    fl = {k: v["flops"] for k, v in st.items()}
+    out["mpo_apply_truncate"] = {
+        "value": ws * len(fs) / t, "unit": "MPS/s", "batch": len(fs), "s_per_batch": t,
+        "precision": "f64 (plain; the mixed apply path is not built)",
+        "max_bond_after": max(r.maxlinkdim() for r in res),
+        "kernel_ms": {k: round(v["ms"], 2) for k, v in sorted(st.items(), key=lambda kv: -kv[1]["ms"])[:6]},
+        "fp64_tflops": sum(v["flops"] for k, v in st.items() if k in ("qr_f64", "svd_f64", "gemm_f64"))
+        / t / 1e12,
+    }
+    del res, fs
+    # --- config 1: the reference's CPU case on the GPU ---------------------------
+    L = 20
+    s = ina.continuous_siteinds(ina.named_grid((L, 1)))
+    X = np.random.default_rng(0).random((4096, 1))
+
+    def cfg1():
+        f = ina.exp_itn(s, k=-1.0) + ina.sin_itn(s, k=2 * np.pi)
+        g = ina.operate(ina.second_derivative_operator(s), f, cutoff=1e-12, maxdim=32)
+        return g.evaluate_batch(X), g.integrate()
+
+    cfg1()
+    t1, _ = _timed(cfg1)
+    out["config1_latency"] = {"value": t1, "unit": "s",
+                              "what": "build f, build d2/dx2, apply+truncate (1e-12, 32), 4096 evals, integrate"}
+    # --- config 4: gradient of batched evaluation --------------------------------
+    import torch
+
+    L4 = 12
+    s4 = ina.continuous_siteinds(ina.named_comb_tree((2, L4)),
+                                 [[(1, j) for j in range(1, L4 + 1)], [(2, j) for j in range(1, L4 + 1)]])
+    rng = np.random.default_rng(2)
+    lay = s4.layout
+    ts = {}
+    for i, v in enumerate(lay.order):
+        shape = (2, 32 if lay.parent[i] >= 0 else 1) + (32,) * len(lay.children[i])
+        ts[v] = 0.1 * rng.standard_normal(shape)
+    f4 = ina.ITensorNetworkFunction.from_tensors(s4, ts, ctx=ctx, dtype=2 - 1)  # FP32
+    P4 = 1 << 20
+    X4 = torch.tensor(rng.random((P4, 2)), device="cuda")
+    dout = torch.tensor(rng.standard_normal(P4), device="cuda")
+    g4 = torch.zeros(f4.info()[2], dtype=torch.float32, device="cuda")
+    dims = (ctypes.c_int32 * 2)(1, 2)
+
+    def grad():
+        ctx.call("tnfa_evaluate_vjp", f4.handle, X4.data_ptr(), P4, 2, dims, 1, dout.data_ptr(), 1,
+                 g4.data_ptr(), 1)
+
+    grad()
+    t4, _ = _timed(grad, 3)
+    out["gradient"] = {"value": P4 / t4, "unit": "points/s", "points": P4,
+                       "what": "tnfa_evaluate_vjp, comb 2x12 chi 32 FP32 (forward + outside messages + accumulation)"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -243,6 +332,8 @@ def main():
     ap.add_argument("--cpu-points", type=int, default=96)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--mps", type=int, default=512, help="config-5 batch size")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_init()
@@ -369,6 +460,8 @@ def main():
         "kernels": {k: {"launches_per_step": v["launches"] // args.steps,
                         "ms_per_step": v["ms"] / args.steps} for k, v in stats.items()},
     }
+    if not args.no_secondary:
+        result["secondary"] = secondary_measurements(ctx, ws, rank, args)
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         rate, wall, pts, vals = cpu_baseline(args.cpu_points, cores)

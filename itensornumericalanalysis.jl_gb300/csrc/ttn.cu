@@ -632,6 +632,312 @@ tnfa_net* reduce_out_legs(tnfa_ctx* ctx, const tnfa_net* op, int take_sum) {
   return out;
 }
 
+// --------------------------------------------- batched paths (MPS) ----
+// Many independent path networks (vertex i's only child is i + 1) truncated
+// step by step together: step t handles one vertex of every network that has
+// it, so each primitive (permute, QR, SVD, GEMM) runs once per step for the
+// whole batch with per-problem shapes.
+
+bool is_rooted_path(const Topo& T) {
+  if (T.V < 1 || T.parent[0] != -1) return false;
+  for (int v = 1; v < T.V; ++v)
+    if (T.parent[v] != v - 1) return false;
+  return true;
+}
+
+struct MoveJob {
+  const void* src;
+  void* dst;
+  std::vector<int> shp;
+  int ax, to;
+};
+
+template <class T>
+void move_axes(tnfa_ctx* ctx, const std::vector<MoveJob>& mv) {
+  std::vector<la::PermJob> jobs;
+  for (const auto& m : mv) {
+    la::PermJob j{};
+    j.src = m.src;
+    j.dst = m.dst;
+    j.nd = (int)m.shp.size();
+    TNFA_CHECK(j.nd <= la::MAXD, TNFA_ERR_UNSUPPORTED, "tensor order above 10");
+    std::vector<int> order(j.nd);
+    std::iota(order.begin(), order.end(), 0);
+    order.erase(order.begin() + m.ax);
+    order.insert(order.begin() + m.to, m.ax);
+    j.n = 1;
+    for (int a = 0; a < j.nd; ++a) {
+      j.shape[a] = m.shp[a];
+      j.perm[a] = order[a];
+      j.n *= m.shp[a];
+    }
+    jobs.push_back(j);
+  }
+  for (size_t i = 0; i < jobs.size(); i += 60000)
+    la::permute<T>(ctx, std::vector<la::PermJob>(jobs.begin() + i,
+                                                 jobs.begin() + std::min(jobs.size(), i + 60000)));
+}
+
+struct BSlot {
+  int net, v;
+};
+
+// QR of the listed vertices with their parent axis (1) as columns; each keeps
+// Q and returns R (k x old) in Rs[i]; ks[i] = k.
+template <class T>
+void qr_parent_axis_batched(std::vector<Work<T>>& W, const std::vector<BSlot>& sl,
+                            std::vector<DBuf>& Rs, std::vector<int>& ks) {
+  if (sl.empty()) return;
+  tnfa_ctx* ctx = W[sl[0].net].ctx;
+  const size_t n = sl.size();
+  std::vector<DBuf> M(n), Q(n), tau(n), back(n);
+  Rs.clear();
+  Rs.resize(n);
+  ks.assign(n, 0);
+  std::vector<MoveJob> mv;
+  std::vector<la::QrJob> qj;
+  std::vector<std::vector<int>> shp(n);
+  for (size_t i = 0; i < n; ++i) {
+    Work<T>& w = W[sl[i].net];
+    const int v = sl[i].v;
+    shp[i] = w.shape(v);
+    const int cols = shp[i][1];
+    const int64_t rows = w.size(v) / cols;
+    TNFA_CHECK(rows < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "matrix too large");
+    ks[i] = (int)std::min<int64_t>(rows, cols);
+    M[i] = DBuf(ctx, (size_t)w.size(v) * sizeof(T));
+    Q[i] = DBuf(ctx, (size_t)rows * ks[i] * sizeof(T));
+    Rs[i] = DBuf(ctx, (size_t)ks[i] * cols * sizeof(T));
+    tau[i] = DBuf(ctx, (size_t)ks[i] * sizeof(T));
+    mv.push_back({w.t[v].p, M[i].p, shp[i], 1, (int)shp[i].size() - 1});
+    qj.push_back({M[i].p, Q[i].p, Rs[i].p, tau[i].p, (int)rows, cols});
+  }
+  move_axes<T>(ctx, mv);
+  la::qr<T>(ctx, qj);
+  mv.clear();
+  for (size_t i = 0; i < n; ++i) {
+    std::vector<int> qshp = shp[i];
+    qshp.erase(qshp.begin() + 1);
+    qshp.push_back(ks[i]);
+    const int64_t rows = W[sl[i].net].size(sl[i].v) / shp[i][1];
+    back[i] = DBuf(ctx, (size_t)rows * ks[i] * sizeof(T));
+    mv.push_back({Q[i].p, back[i].p, qshp, (int)qshp.size() - 1, 1});
+  }
+  move_axes<T>(ctx, mv);
+  for (size_t i = 0; i < n; ++i) W[sl[i].net].t[sl[i].v] = std::move(back[i]);
+}
+
+// T_v <- M x_ax T_v for every listed vertex (M newdims[i] x old).
+template <class T>
+void absorb_batched(std::vector<Work<T>>& W, const std::vector<BSlot>& sl, const std::vector<int>& ax,
+                    const std::vector<const void*>& Ms, const std::vector<int>& newd) {
+  if (sl.empty()) return;
+  tnfa_ctx* ctx = W[sl[0].net].ctx;
+  const size_t n = sl.size();
+  std::vector<DBuf> a(n), b(n), c(n);
+  std::vector<MoveJob> mv;
+  std::vector<la::GemmJob> gj;
+  std::vector<std::vector<int>> shp(n);
+  for (size_t i = 0; i < n; ++i) {
+    Work<T>& w = W[sl[i].net];
+    const int v = sl[i].v;
+    shp[i] = w.shape(v);
+    const int old = shp[i][ax[i]];
+    const int64_t rest = w.size(v) / old;
+    a[i] = DBuf(ctx, (size_t)w.size(v) * sizeof(T));
+    b[i] = DBuf(ctx, (size_t)newd[i] * rest * sizeof(T));
+    mv.push_back({w.t[v].p, a[i].p, shp[i], ax[i], 0});
+    gj.push_back({Ms[i], a[i].p, b[i].p, newd[i], (int)rest, old, old, (int)rest, (int)rest, 0, 0,
+                  1.0, 0.0});
+  }
+  move_axes<T>(ctx, mv);
+  for (size_t i = 0; i < gj.size(); i += 60000)
+    la::gemm<T>(ctx, std::vector<la::GemmJob>(gj.begin() + i, gj.begin() + std::min(gj.size(), i + 60000)));
+  mv.clear();
+  for (size_t i = 0; i < n; ++i) {
+    std::vector<int> nshp = shp[i];
+    const int64_t rest = W[sl[i].net].size(sl[i].v) / nshp[ax[i]];
+    nshp.erase(nshp.begin() + ax[i]);
+    nshp.insert(nshp.begin(), newd[i]);
+    c[i] = DBuf(ctx, (size_t)newd[i] * rest * sizeof(T));
+    mv.push_back({b[i].p, c[i].p, nshp, 0, ax[i]});
+  }
+  move_axes<T>(ctx, mv);
+  for (size_t i = 0; i < n; ++i) W[sl[i].net].t[sl[i].v] = std::move(c[i]);
+}
+
+template <class T>
+void truncate_paths_batched(std::vector<Work<T>>& W, const tnfa_trunc_params& prm) {
+  if (W.empty()) return;
+  tnfa_ctx* ctx = W[0].ctx;
+  int maxV = 0;
+  for (auto& w : W) maxV = std::max(maxV, w.topo.V);
+  // (1) orthogonalise toward vertex 0, from the far end of every path
+  for (int t = 0; t + 1 < maxV; ++t) {
+    std::vector<BSlot> sl;
+    for (int i = 0; i < (int)W.size(); ++i) {
+      const int v = W[i].topo.V - 1 - t;
+      if (v >= 1) sl.push_back({i, v});
+    }
+    std::vector<DBuf> Rs;
+    std::vector<int> ks;
+    qr_parent_axis_batched(W, sl, Rs, ks);
+    std::vector<BSlot> ps;
+    std::vector<int> ax;
+    std::vector<const void*> Ms;
+    for (size_t q = 0; q < sl.size(); ++q) {
+      ps.push_back({sl[q].net, sl[q].v - 1});
+      ax.push_back(2);
+      Ms.push_back(Rs[q].p);
+    }
+    absorb_batched(W, ps, ax, Ms, ks);
+    for (size_t q = 0; q < sl.size(); ++q) W[sl[q].net].topo.link[sl[q].v] = ks[q];
+  }
+  // (2) SVD sweep from vertex 0: bond (t, t + 1) of every path at step t
+  for (int t = 0; t + 1 < maxV; ++t) {
+    std::vector<BSlot> sl;
+    for (int i = 0; i < (int)W.size(); ++i)
+      if (t + 1 < W[i].topo.V) sl.push_back({i, t});
+    const size_t n = sl.size();
+    std::vector<DBuf> M(n), Qb(n), Rb(n), taub(n), Ub(n), Sb(n), Vb(n), left(n), MT(n), sw(n);
+    std::vector<int> rows(n), cols(n), nsv(n);
+    std::vector<char> tall(n);
+    std::vector<std::vector<int>> shp(n);
+    std::vector<MoveJob> mv;
+    for (size_t q = 0; q < n; ++q) {
+      Work<T>& w = W[sl[q].net];
+      const int v = sl[q].v;
+      shp[q] = w.shape(v);
+      cols[q] = shp[q][2];
+      const int64_t r64 = w.size(v) / cols[q];
+      TNFA_CHECK(r64 < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "matrix too large");
+      rows[q] = (int)r64;
+      tall[q] = rows[q] >= cols[q];
+      nsv[q] = tall[q] ? cols[q] : rows[q];
+      M[q] = DBuf(ctx, (size_t)w.size(v) * sizeof(T));
+      mv.push_back({w.t[v].p, M[q].p, shp[q], 2, (int)shp[q].size() - 1});
+      Sb[q] = DBuf(ctx, (size_t)nsv[q] * sizeof(double));
+      sw[q] = DBuf(ctx, sizeof(int));
+    }
+    move_axes<T>(ctx, mv);
+    std::vector<la::QrJob> qj;
+    std::vector<MoveJob> tj;
+    for (size_t q = 0; q < n; ++q) {
+      if (tall[q]) {
+        Qb[q] = DBuf(ctx, (size_t)rows[q] * cols[q] * sizeof(T));
+        Rb[q] = DBuf(ctx, (size_t)cols[q] * cols[q] * sizeof(T));
+        taub[q] = DBuf(ctx, (size_t)cols[q] * sizeof(T));
+        qj.push_back({M[q].p, Qb[q].p, Rb[q].p, taub[q].p, rows[q], cols[q]});
+      } else {
+        MT[q] = DBuf(ctx, (size_t)rows[q] * cols[q] * sizeof(T));
+        tj.push_back({M[q].p, MT[q].p, {rows[q], cols[q]}, 1, 0});
+      }
+    }
+    la::qr<T>(ctx, qj);
+    move_axes<T>(ctx, tj);
+    std::vector<la::SvdJob> sj;
+    for (size_t q = 0; q < n; ++q) {
+      const int k = nsv[q];
+      Vb[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
+      if (tall[q]) {
+        Ub[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
+        sj.push_back({Rb[q].p, Ub[q].p, Sb[q].as<double>(), Vb[q].p, k, k, sw[q].as<int>()});
+      } else {
+        Ub[q] = DBuf(ctx, (size_t)cols[q] * k * sizeof(T));
+        sj.push_back({MT[q].p, Ub[q].p, Sb[q].as<double>(), Vb[q].p, cols[q], k, sw[q].as<int>()});
+      }
+    }
+    la::svd<T>(ctx, sj);
+    std::vector<la::GemmJob> gl;
+    for (size_t q = 0; q < n; ++q)
+      if (tall[q]) {
+        left[q] = DBuf(ctx, (size_t)rows[q] * nsv[q] * sizeof(T));
+        gl.push_back({Qb[q].p, Ub[q].p, left[q].p, rows[q], nsv[q], nsv[q], nsv[q], nsv[q], nsv[q],
+                      0, 0, 1.0, 0.0});
+      }
+    la::gemm<T>(ctx, gl);
+    // singular values of the whole step to the host
+    std::vector<std::vector<double>> sv(n);
+    std::vector<int> sweeps(n);
+    for (size_t q = 0; q < n; ++q) {
+      sv[q].resize(nsv[q]);
+      TNFA_CUDA(cudaMemcpyAsync(sv[q].data(), Sb[q].p, nsv[q] * sizeof(double),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+      TNFA_CUDA(cudaMemcpyAsync(&sweeps[q], sw[q].p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<int> r(n);
+    std::vector<DBuf> sd(n), X(n), newv(n), back(n);
+    std::vector<la::GemmJob> gx;
+    for (size_t q = 0; q < n; ++q) {
+      TNFA_CHECK(sweeps[q] >= 0, TNFA_ERR_NOT_CONVERGED, "Jacobi SVD hit its sweep cap");
+      r[q] = la::truncation_rank(sv[q].data(), nsv[q], prm.cutoff, prm.maxdim, prm.mindim);
+      std::vector<T> diag((size_t)r[q] * r[q], hreal<T>(0.0));
+      for (int i = 0; i < r[q]; ++i) diag[(size_t)i * r[q] + i] = hreal<T>(sv[q][i]);
+      sd[q] = DBuf(ctx, diag.size() * sizeof(T));
+      TNFA_CUDA(cudaMemcpyAsync(sd[q].p, diag.data(), diag.size() * sizeof(T), cudaMemcpyHostToDevice,
+                                ctx->stream));
+      X[q] = DBuf(ctx, (size_t)r[q] * cols[q] * sizeof(T));
+      newv[q] = DBuf(ctx, (size_t)rows[q] * r[q] * sizeof(T));
+      if (tall[q]) {
+        copy2d<T>(ctx, newv[q].p, r[q], left[q].p, nsv[q], rows[q], r[q], false);
+        gx.push_back({sd[q].p, Vb[q].p, X[q].p, r[q], cols[q], r[q], r[q], nsv[q], cols[q], 0, 2,
+                      1.0, 0.0});
+      } else {
+        copy2d<T>(ctx, newv[q].p, r[q], Vb[q].p, nsv[q], rows[q], r[q], true);
+        gx.push_back({sd[q].p, Ub[q].p, X[q].p, r[q], cols[q], r[q], r[q], nsv[q], cols[q], 0, 1,
+                      1.0, 0.0});
+      }
+    }
+    // the host staging vectors of diag() must outlive the async copies
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+    la::gemm<T>(ctx, gx);
+    mv.clear();
+    for (size_t q = 0; q < n; ++q) {
+      std::vector<int> nshp = shp[q];
+      nshp.erase(nshp.begin() + 2);
+      nshp.push_back(r[q]);
+      back[q] = DBuf(ctx, (size_t)rows[q] * r[q] * sizeof(T));
+      mv.push_back({newv[q].p, back[q].p, nshp, (int)nshp.size() - 1, 2});
+    }
+    move_axes<T>(ctx, mv);
+    std::vector<BSlot> cs;
+    std::vector<int> ax;
+    std::vector<const void*> Ms;
+    for (size_t q = 0; q < n; ++q) {
+      W[sl[q].net].t[sl[q].v] = std::move(back[q]);
+      cs.push_back({sl[q].net, sl[q].v + 1});
+      ax.push_back(1);
+      Ms.push_back(X[q].p);
+    }
+    absorb_batched(W, cs, ax, Ms, r);
+    for (size_t q = 0; q < n; ++q) W[sl[q].net].topo.link[sl[q].v + 1] = r[q];
+  }
+  if (prm.normalize) {
+    // the centre ends at the last vertex of every path
+    for (auto& w : W) {
+      const int c = w.topo.V - 1;
+      const double nrm = host_norm<T>(ctx, w.t[c], w.size(c));
+      if (nrm > 0) {
+        k_scale_by<T><<<grid_for(w.size(c), 256, 1024), 256, 0, ctx->stream>>>(
+            w.t[c].template as<T>(), w.size(c), 1.0 / nrm);
+        TNFA_LAUNCH_CHECK();
+      }
+    }
+  }
+}
+
+template <class T>
+void batch_apply_truncate(tnfa_ctx* ctx, int n, const tnfa_net* const* ops, const tnfa_net* const* fs,
+                          const tnfa_trunc_params& prm, int dtype, tnfa_net** outs) {
+  std::vector<Work<T>> W;
+  W.reserve(n);
+  for (int i = 0; i < n; ++i)
+    W.push_back(ops ? apply_exact<T>(ctx, ops[i], fs[i]) : load_work<T>(ctx, fs[i]));
+  truncate_paths_batched(W, prm);
+  for (int i = 0; i < n; ++i) outs[i] = store_work(W[i], dtype);
+}
+
 }  // namespace
 
 tnfa_net* apply_truncate(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f,
@@ -694,11 +1000,19 @@ int tnfa_apply_batched(tnfa_ctx* ctx, int32_t n, const tnfa_net* const* ops,
   TNFA_CHECK(n >= 0 && (n == 0 || (ops && fs && outs)), TNFA_ERR_INVALID_ARGUMENT, "null arrays");
   for (int i = 0; i < n; ++i) outs[i] = nullptr;
   try {
+    bool paths = n > 0;
     for (int i = 0; i < n; ++i) {
       require_net(ops[i], "apply_batched operator");
       require_net(fs[i], "apply_batched function");
-      outs[i] = apply_truncate(ctx, ops[i], fs[i], *params);
+      paths = paths && is_rooted_path(fs[i]->topo) && fs[i]->dtype == fs[0]->dtype &&
+              ops[i]->dtype == fs[i]->dtype;
     }
+    if (paths && fs[0]->dtype == TNFA_F64)
+      batch_apply_truncate<double>(ctx, n, ops, fs, *params, TNFA_F64, outs);
+    else if (paths && fs[0]->dtype == TNFA_C128)
+      batch_apply_truncate<cplx>(ctx, n, ops, fs, *params, TNFA_C128, outs);
+    else
+      for (int i = 0; i < n; ++i) outs[i] = apply_truncate(ctx, ops[i], fs[i], *params);
   } catch (...) {
     for (int i = 0; i < n; ++i)
       if (outs[i]) {
@@ -729,10 +1043,17 @@ int tnfa_truncate_batched(tnfa_ctx* ctx, int32_t n, const tnfa_net* const* fs,
   TNFA_CHECK(n >= 0 && (n == 0 || (fs && outs)), TNFA_ERR_INVALID_ARGUMENT, "null arrays");
   for (int i = 0; i < n; ++i) outs[i] = nullptr;
   try {
+    bool paths = n > 0;
     for (int i = 0; i < n; ++i) {
       require_net(fs[i], "truncate_batched");
-      outs[i] = truncate_net(ctx, fs[i], *params);
+      paths = paths && is_rooted_path(fs[i]->topo) && fs[i]->dtype == fs[0]->dtype;
     }
+    if (paths && fs[0]->dtype == TNFA_F64)
+      batch_apply_truncate<double>(ctx, n, nullptr, fs, *params, TNFA_F64, outs);
+    else if (paths && fs[0]->dtype == TNFA_C128)
+      batch_apply_truncate<cplx>(ctx, n, nullptr, fs, *params, TNFA_C128, outs);
+    else
+      for (int i = 0; i < n; ++i) outs[i] = truncate_net(ctx, fs[i], *params);
   } catch (...) {
     for (int i = 0; i < n; ++i)
       if (outs[i]) {

@@ -70,7 +70,7 @@ from .indexmap import (
 from .grad import TTNEvaluate, evaluate_vjp
 from .integration import integrate, partial_integrate
 from .network import ITensorNetworkFunction, calculate_fx, evaluate, inner
-from .operate import operate
-from .truncation import truncate
+from .operate import operate, operate_batched
+from .truncation import truncate, truncate_batched
 
 __version__ = "0.1.0"

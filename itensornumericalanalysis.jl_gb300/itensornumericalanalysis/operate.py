@@ -18,3 +18,20 @@ def operate(op, f, cutoff=1e-15, maxdim=None, normalize=False, precision="f64", 
     h = C.c_void_p()
     f.ctx.call("tnfa_apply", op.handle, f.handle, C.byref(p), C.byref(h))
     return type(f)(f.s, h, f.ctx)
+
+
+def operate_batched(ops, fs, cutoff=1e-15, maxdim=None, normalize=False, precision="f64"):
+    """[O_i f_i] for many independent (operator, function) pairs in one
+    scheduled pass (paths of uneven length and bond dimension are processed
+    step by step together)."""
+    n = len(fs)
+    if len(ops) != n:
+        raise ValueError("ops and fs differ in length")
+    p = trunc_params(cutoff, maxdim, 1, normalize, precision)
+    oh = (C.c_void_p * max(n, 1))(*[o.handle.value for o in ops])
+    fh = (C.c_void_p * max(n, 1))(*[f.handle.value for f in fs])
+    out = (C.c_void_p * max(n, 1))()
+    if n == 0:
+        return []
+    fs[0].ctx.call("tnfa_apply_batched", n, oh, fh, C.byref(p), out)
+    return [type(f)(f.s, C.c_void_p(out[i]), f.ctx) for i, f in enumerate(fs)]

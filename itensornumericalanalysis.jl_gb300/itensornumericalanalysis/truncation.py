@@ -20,3 +20,15 @@ def truncate(f, cutoff=1e-15, maxdim=None, mindim=1, normalize=False, precision=
     h = C.c_void_p()
     f.ctx.call("tnfa_truncate", f.handle, C.byref(p), C.byref(h))
     return f._wrap(h)
+
+
+def truncate_batched(fs, cutoff=1e-15, maxdim=None, mindim=1, normalize=False, precision="f64"):
+    """truncate() of many networks in one scheduled pass."""
+    n = len(fs)
+    if n == 0:
+        return []
+    p = trunc_params(cutoff, maxdim, mindim, normalize, precision)
+    fh = (C.c_void_p * n)(*[f.handle.value for f in fs])
+    out = (C.c_void_p * n)()
+    fs[0].ctx.call("tnfa_truncate_batched", n, fh, C.byref(p), out)
+    return [f._wrap(C.c_void_p(out[i])) for i, f in enumerate(fs)]

@@ -258,3 +258,31 @@ def test_config1_apply_truncate_evaluate_integrate(ina):
     assert np.max(np.abs(got - ref)) / scale < 1e-8
     assert abs(g.integrate() - np.mean(G)) / scale < 1e-8
     assert g.maxlinkdim() <= 32
+
+
+def test_batched_apply_matches_single(ina):
+    """Config-5 shapes at reduced size: paths of uneven length and bond
+    dimension applied and truncated in one batched pass equal the per-network
+    results (function values)."""
+    from itensornumericalanalysis.workloads import uneven_mps_batch, upload_batch
+
+    batch = uneven_mps_batch(n=12, seed=3, lmin=6, lmax=14, chimin=2, chimax=24)
+    fs = upload_batch(batch)
+    ops = {}
+    for s, _ in batch:
+        L = s.nv()
+        if L not in ops:
+            ops[L] = ina.first_derivative_operator(s)
+    oplist = [ops[s.nv()] for s, _ in batch]
+    outs = ina.operate_batched(oplist, fs, cutoff=1e-10)
+    rng = np.random.default_rng(60)
+    X = rng.random((200, 1))
+    for o, f, g in zip(oplist, fs, outs):
+        single = ina.operate(o, f, cutoff=1e-10)
+        a, b = g.evaluate_batch(X), single.evaluate_batch(X)
+        assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(b))
+        assert g.linkdims() == single.linkdims()
+    tr = ina.truncate_batched(outs, cutoff=1e-6)
+    for g, t in zip(outs, tr):
+        a, b = t.evaluate_batch(X), g.evaluate_batch(X)
+        assert np.linalg.norm(a - b) <= 1e-2 * np.linalg.norm(b)
