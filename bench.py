@@ -303,7 +303,7 @@ def secondary_measurements(ctx, ws, rank, args) -> dict:
     for i, v in enumerate(lay.order):
         shape = (2, 32 if lay.parent[i] >= 0 else 1) + (32,) * len(lay.children[i])
         ts[v] = 0.1 * rng.standard_normal(shape)
-    f4 = ina.ITensorNetworkFunction.from_tensors(s4, ts, ctx=ctx, dtype=2 - 1)  # FP32
+    f4 = ina.ITensorNetworkFunction.from_tensors(s4, ts, ctx=ctx, dtype=ina._lib.F32)
     P4 = 1 << 20
     X4 = torch.tensor(rng.random((P4, 2)), device="cuda")
     dout = torch.tensor(rng.standard_normal(P4), device="cuda")
