@@ -98,11 +98,12 @@ def test_fit_decreases_loss(ina):
     X = torch.tensor(Xh, device="cuda")
     opt = torch.optim.Adam([params], lr=0.02)
     losses = []
-    for _ in range(40):
+    for _ in range(60):
         opt.zero_grad()
         pred = ina.TTNEvaluate.apply(params, X, template, [1, 2])
         loss = torch.mean((pred - target) ** 2)
         loss.backward()
         opt.step()
         losses.append(float(loss))
-    assert losses[-1] < 0.5 * losses[0], losses[::8]
+    assert losses[-1] < 0.6 * losses[0], losses[::10]
+    assert all(np.isfinite(losses))
