@@ -481,6 +481,153 @@ void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
   }
 }
 
+// ------------------------------------------------------------------ lu --
+constexpr int LU_NB = 32;
+
+// Factor columns k..k+kb-1 (rows k..n-1); row swaps inside the panel only.
+__global__ void __launch_bounds__(512) k_lu_panel(double* A, int n, int k, int kb, int* piv,
+                                                  int* singular) {
+  __shared__ double vmax[32];
+  __shared__ int imax[32];
+  __shared__ int p_sh;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = k; j < k + kb; ++j) {
+    double best = -1.0;
+    int bi = j;
+    for (int r = j + threadIdx.x; r < n; r += blockDim.x) {
+      const double a = fabs(A[(int64_t)r * n + j]);
+      if (a > best) {
+        best = a;
+        bi = r;
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      vmax[warp] = best;
+      imax[warp] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = -1.0;
+      int i = j;
+      for (int w = 0; w < nw; ++w)
+        if (vmax[w] > b || (vmax[w] == b && imax[w] < i)) {
+          b = vmax[w];
+          i = imax[w];
+        }
+      p_sh = i;
+      piv[j] = i;
+      if (!(b > 0.0)) *singular = 1;
+    }
+    __syncthreads();
+    const int p = p_sh;
+    if (p != j)
+      for (int c = k + threadIdx.x; c < k + kb; c += blockDim.x) {
+        const double t = A[(int64_t)j * n + c];
+        A[(int64_t)j * n + c] = A[(int64_t)p * n + c];
+        A[(int64_t)p * n + c] = t;
+      }
+    __syncthreads();
+    const double d = A[(int64_t)j * n + j];
+    if (d != 0.0) {
+      for (int r = j + 1 + threadIdx.x; r < n; r += blockDim.x) {
+        double* row = A + (int64_t)r * n;
+        const double l = row[j] / d;
+        row[j] = l;
+        for (int c = j + 1; c < k + kb; ++c) row[c] -= l * A[(int64_t)j * n + c];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Apply the panel's row swaps to the columns outside it.
+__global__ void k_lu_swap(double* A, int n, int k, int kb, const int* piv) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    if (c >= k && c < k + kb) continue;
+    for (int j = k; j < k + kb; ++j) {
+      const int p = piv[j];
+      if (p != j) {
+        const double t = A[(int64_t)j * n + c];
+        A[(int64_t)j * n + c] = A[(int64_t)p * n + c];
+        A[(int64_t)p * n + c] = t;
+      }
+    }
+  }
+}
+
+// U12 = L11^{-1} A12 (unit lower triangular L11), one column per thread.
+__global__ void k_lu_trsm(double* A, int n, int k, int kb) {
+  for (int c = k + kb + blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+    for (int r = k + 1; r < k + kb; ++r) {
+      double acc = A[(int64_t)r * n + c];
+      for (int t = k; t < r; ++t) acc -= A[(int64_t)r * n + t] * A[(int64_t)t * n + c];
+      A[(int64_t)r * n + c] = acc;
+    }
+}
+
+// Swaps on b, then L y = b (unit diagonal) and U x = y, one CTA.
+__global__ void __launch_bounds__(512) k_lu_subst(const double* A, int n, const int* piv, double* b) {
+  __shared__ double red[32];
+  if (threadIdx.x == 0)
+    for (int j = 0; j < n; ++j) {
+      const int p = piv[j];
+      if (p != j) {
+        const double t = b[j];
+        b[j] = b[p];
+        b[p] = t;
+      }
+    }
+  __syncthreads();
+  for (int r = 1; r < n; ++r) {
+    double part = 0.0;
+    for (int t = threadIdx.x; t < r; t += blockDim.x) part += A[(int64_t)r * n + t] * b[t];
+    const double s = block_sum<double>(part, red);
+    if (threadIdx.x == 0) b[r] -= s;
+    __syncthreads();
+  }
+  for (int r = n - 1; r >= 0; --r) {
+    double part = 0.0;
+    for (int t = r + 1 + threadIdx.x; t < n; t += blockDim.x) part += A[(int64_t)r * n + t] * b[t];
+    const double s = block_sum<double>(part, red);
+    if (threadIdx.x == 0) b[r] = (b[r] - s) / A[(int64_t)r * n + r];
+    __syncthreads();
+  }
+}
+
+bool lu_solve(tnfa_ctx* ctx, double* A, double* b, int n) {
+  if (n <= 0) return true;
+  DBuf piv(ctx, (size_t)n * sizeof(int)), sing(ctx, sizeof(int));
+  TNFA_CUDA(cudaMemsetAsync(sing.p, 0, sizeof(int), ctx->stream));
+  KernelScope ks(ctx, "lu_f64", 2.0 / 3.0 * (double)n * n * n, 0.0);
+  for (int k = 0; k < n; k += LU_NB) {
+    const int kb = std::min(LU_NB, n - k);
+    k_lu_panel<<<1, 512, 0, ctx->stream>>>(A, n, k, kb, piv.as<int>(), sing.as<int>());
+    k_lu_swap<<<grid_for(n, 256, 1024), 256, 0, ctx->stream>>>(A, n, k, kb, piv.as<int>());
+    if (k + kb < n) {
+      k_lu_trsm<<<grid_for(n - k - kb, 128, 1024), 128, 0, ctx->stream>>>(A, n, k, kb);
+      const int m2 = n - k - kb;
+      GemmJob g{A + (int64_t)(k + kb) * n + k, A + (int64_t)k * n + k + kb,
+                A + (int64_t)(k + kb) * n + k + kb, m2, m2, kb, n, n, n, 0, 0, -1.0, 1.0};
+      gemm<double>(ctx, {g});
+    }
+    TNFA_LAUNCH_CHECK();
+  }
+  k_lu_subst<<<1, 512, 0, ctx->stream>>>(A, n, piv.as<int>(), b);
+  TNFA_LAUNCH_CHECK();
+  int hs = 0;
+  TNFA_CUDA(cudaMemcpyAsync(&hs, sing.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  return hs == 0;
+}
+
 int truncation_rank(const double* s, int n, double cutoff, int maxdim, int mindim) {
   if (n <= 0) return 0;
   double total = 0.0;

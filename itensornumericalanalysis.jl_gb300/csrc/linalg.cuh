@@ -61,6 +61,12 @@ struct SvdJob {
 template <class T>
 void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps = 60);
 
+// Solve A x = b for one dense n x n FP64 system (A row-major, destroyed; b
+// overwritten by x): blocked right-looking LU with partial pivoting (panel
+// kernel, row swaps, triangular solve, trailing update by the batched GEMM),
+// then forward / back substitution.  Returns false if a pivot is exactly 0.
+bool lu_solve(tnfa_ctx* ctx, double* A, double* b, int n);
+
 // Rank kept by the reference truncation rule: smallest r >= mindim with
 // sum_{i >= r} s_i^2 <= cutoff * sum s_i^2, capped by maxdim (> 0).
 int truncation_rank(const double* s, int n, double cutoff, int maxdim, int mindim);

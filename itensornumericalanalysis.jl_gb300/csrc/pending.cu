@@ -16,9 +16,5 @@ int tnfa_partial_integrate(tnfa_ctx* ctx, const tnfa_net*, int32_t, const int32_
                            tnfa_net**) {
   TNFA_PENDING("tnfa_partial_integrate")
 }
-int tnfa_linsolve(tnfa_ctx* ctx, const tnfa_net*, const tnfa_net*, const tnfa_net*,
-                  const tnfa_linsolve_params*, tnfa_net**, double*) {
-  TNFA_PENDING("tnfa_linsolve")
-}
 
 }  // extern "C"

@@ -938,6 +938,364 @@ void batch_apply_truncate(tnfa_ctx* ctx, int n, const tnfa_net* const* ops, cons
   for (int i = 0; i < n; ++i) outs[i] = store_work(W[i], dtype);
 }
 
+// ------------------------------------------------------------ linsolve ----
+// Two-site alternating linear solver on a path (the sweep of
+// ITensorNetworks.linsolve / dmrg with nsites = 2): every update solves the
+// system projected onto the current left / right bases exactly,
+//   (a0 I + a1 LA_i A_i A_{i+1} RA_{i+2}) v = Lb_i b_i b_{i+1} Rb_{i+2},
+// splits v by a truncated SVD and moves the orthogonality centre on.  The
+// residual ||(a0 + a1 A) x - b|| / ||b|| is formed exactly as a network and
+// normed through a QR sweep after every half sweep.
+
+tnfa_net* direct_sum_ext(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g);
+
+// Path order of a connected tree with all degrees <= 2, from its
+// lowest-numbered end: ord[k] is the vertex at position k.
+std::vector<int> path_order(const Topo& T) {
+  TNFA_CHECK(T.roots().size() == 1, TNFA_ERR_UNSUPPORTED, "linsolve needs a connected path");
+  std::vector<std::vector<int>> adj(T.V);
+  for (int v = 0; v < T.V; ++v)
+    if (T.parent[v] >= 0) {
+      adj[v].push_back(T.parent[v]);
+      adj[T.parent[v]].push_back(v);
+    }
+  int end = -1;
+  for (int v = 0; v < T.V; ++v) {
+    TNFA_CHECK(adj[v].size() <= 2, TNFA_ERR_UNSUPPORTED,
+               "linsolve needs a path graph (vertex " + std::to_string(v) +
+                   " has more than two neighbours)");
+    if (adj[v].size() <= 1 && end < 0) end = v;
+  }
+  std::vector<int> ord;
+  for (int prev = -1, v = end; v >= 0;) {
+    ord.push_back(v);
+    int nxt = -1;
+    for (int u : adj[v])
+      if (u != prev) nxt = u;
+    prev = v;
+    v = nxt;
+  }
+  return ord;
+}
+
+// T re-rooted at ord[0]: vertex k of the result is T's vertex ord[k], with
+// parent k - 1; bonds and site legs are carried over.
+Topo path_topo(const Topo& T, const std::vector<int>& ord) {
+  Topo P;
+  P.V = T.V;
+  P.parent.resize(T.V);
+  P.link.resize(T.V);
+  P.nlegs.resize(T.V);
+  for (int k = 0; k < T.V; ++k) {
+    const int c = ord[k];
+    P.parent[k] = k - 1;
+    if (k == 0) {
+      P.link[k] = 1;
+    } else {
+      const int cp = ord[k - 1];
+      P.link[k] = T.parent[c] == cp ? T.link[c] : T.link[cp];
+    }
+    P.nlegs[k] = T.nlegs[c];
+    for (int l = T.leg_off[c]; l < T.leg_off[c + 1]; ++l) {
+      P.leg_dim.push_back(T.leg_dim[l]);
+      P.leg_var.push_back(T.leg_var[l]);
+      P.leg_digit.push_back(T.leg_digit[l]);
+      P.leg_kind.push_back(T.leg_kind[l]);
+    }
+  }
+  P.finalize();
+  return P;
+}
+
+// The tensors (cur, data) laid out for tgt, the same tree rooted elsewhere and
+// numbered so that tgt's vertex t is cur's vertex cur_of[t]: every tensor is
+// permuted to [site, parent, children ascending] of tgt.  A dim-1 parent axis
+// appears (new root) or disappears (old root) without moving memory.
+template <class T>
+Work<T> relayout(tnfa_ctx* ctx, const Topo& cur, const void* data, const Topo& tgt,
+                 const std::vector<int>& cur_of) {
+  Work<T> w{ctx, tgt, {}};
+  std::vector<int> tgt_of(cur.V);
+  for (int t = 0; t < tgt.V; ++t) tgt_of[cur_of[t]] = t;
+  std::vector<la::PermJob> jobs;
+  w.t.reserve(tgt.V);
+  for (int t = 0; t < tgt.V; ++t) {
+    const int c = cur_of[t];
+    const bool cur_root = cur.parent[c] < 0;
+    // axes of the current tensor without a root's dim-1 parent axis, each
+    // tagged with the tgt vertex across it (-1: the site axis)
+    std::vector<int> shp{cur.site_dim[c]}, nb{-1};
+    if (!cur_root) {
+      shp.push_back(cur.link[c]);
+      nb.push_back(tgt_of[cur.parent[c]]);
+    }
+    for (int ch : cur.children[c]) {
+      shp.push_back(cur.link[ch]);
+      nb.push_back(tgt_of[ch]);
+    }
+    auto axis_of = [&](int u) { return (int)(std::find(nb.begin(), nb.end(), u) - nb.begin()); };
+    std::vector<int> perm{0};
+    if (tgt.parent[t] >= 0) perm.push_back(axis_of(tgt.parent[t]));
+    for (int ch : tgt.children[t]) perm.push_back(axis_of(ch));
+    TNFA_CHECK(perm.size() == shp.size() && (int)shp.size() <= la::MAXD, TNFA_ERR_UNSUPPORTED,
+               "relayout: trees differ");
+    for (int a : perm) TNFA_CHECK(a < (int)shp.size(), TNFA_ERR_UNSUPPORTED, "relayout: trees differ");
+    const int64_t n = cur.size(c);
+    TNFA_CHECK(n == tgt.size(t), TNFA_ERR_SHAPE, "relayout: sizes differ");
+    w.t.emplace_back(ctx, (size_t)n * sizeof(T));
+    la::PermJob j{};
+    j.src = (const T*)data + cur.off[c];
+    j.dst = w.t.back().p;
+    j.nd = (int)shp.size();
+    j.n = n;
+    for (int a = 0; a < j.nd; ++a) {
+      j.shape[a] = shp[a];
+      j.perm[a] = perm[a];
+    }
+    jobs.push_back(j);
+  }
+  la::permute<T>(ctx, jobs);
+  return w;
+}
+
+// A dense FP64 tensor on the device with its shape.
+struct Dense {
+  DBuf b;
+  std::vector<int> shp;
+  double* p() const { return b.as<double>(); }
+};
+
+Dense permuted(tnfa_ctx* ctx, const double* src, const std::vector<int>& shp,
+               const std::vector<int>& order) {
+  Dense d;
+  d.shp.resize(order.size());
+  int64_t n = 1;
+  for (size_t a = 0; a < order.size(); ++a) {
+    d.shp[a] = shp[order[a]];
+    n *= shp[a];
+  }
+  d.b = DBuf(ctx, (size_t)n * 8);
+  la::PermJob j{};
+  j.src = src;
+  j.dst = d.b.p;
+  j.nd = (int)shp.size();
+  j.n = n;
+  for (int a = 0; a < j.nd; ++a) {
+    j.shape[a] = shp[a];
+    j.perm[a] = order[a];
+  }
+  la::permute<double>(ctx, {j});
+  return d;
+}
+
+// C (m x n) = op(A) op(B), row-major, inner dimension k; C gets shape shp.
+Dense mm(tnfa_ctx* ctx, const double* A, const double* B, int m, int n, int k, int opA, int opB,
+         std::vector<int> shp) {
+  Dense d;
+  d.shp = std::move(shp);
+  d.b = DBuf(ctx, (size_t)m * n * 8);
+  const int lda = opA ? m : k, ldb = opB ? k : n;
+  la::gemm<double>(ctx, {la::GemmJob{A, B, d.b.p, m, n, k, lda, ldb, n, opA, opB, 1.0, 0.0}});
+  return d;
+}
+
+Dense ones(tnfa_ctx* ctx, std::vector<int> shp) {
+  Dense d;
+  d.shp = std::move(shp);
+  d.b = DBuf(ctx, 8);
+  const double one = 1.0;
+  TNFA_CUDA(cudaMemcpyAsync(d.b.p, &one, 8, cudaMemcpyHostToDevice, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  return d;
+}
+
+// Path tensors: x and b are [s][l][r], A is [o][i][wl][wr] (the fused
+// operator leg out * d + in); r = 1 past the last vertex.
+struct LinsolveState {
+  tnfa_ctx* ctx;
+  int L, d;
+  Work<double> x, A, b;
+  // environments at bond k (between vertices k-1 and k; k = 0 and L are the
+  // open ends): LA/RA [bra][operator][ket], Lb/Rb [x bond][b bond]
+  std::vector<Dense> LA, RA, Lb, Rb;
+  int bond(const Work<double>& w, int k) const { return k >= 1 && k < L ? w.topo.link[k] : 1; }
+};
+
+// LA_{i+1} and Lb_{i+1} from LA_i, Lb_i and the left-orthonormal x_i.
+void left_env(LinsolveState& S, int i) {
+  tnfa_ctx* ctx = S.ctx;
+  const int d = S.d;
+  const int l = S.bond(S.x, i), r = S.bond(S.x, i + 1);
+  const int wl = S.bond(S.A, i), wr = S.bond(S.A, i + 1);
+  const int bl = S.bond(S.b, i), br = S.bond(S.b, i + 1);
+  const double* xi = S.x.t[i].as<double>();
+  Dense xp = permuted(ctx, xi, {d, l, r}, {1, 0, 2});                     // [l][s][r]
+  Dense t1 = mm(ctx, S.LA[i].p(), xp.p(), l * wl, d * r, l, 0, 0, {l, wl, d, r});  // [l'][wl][s][r]
+  Dense t1p = permuted(ctx, t1.p(), t1.shp, {0, 3, 1, 2});                // [l'][r][wl][s]
+  Dense Ap = permuted(ctx, S.A.t[i].as<double>(), {d, d, wl, wr}, {2, 1, 0, 3});  // [wl][s][o][wr]
+  Dense t2 = mm(ctx, t1p.p(), Ap.p(), l * r, d * wr, wl * d, 0, 0, {l, r, d, wr});  // [l'][r][o][wr]
+  Dense t2p = permuted(ctx, t2.p(), t2.shp, {2, 0, 3, 1});                // [o][l'][wr][r]
+  S.LA[i + 1] = mm(ctx, xi, t2p.p(), r, wr * r, d * l, 1, 0, {r, wr, r});
+  Dense bp = permuted(ctx, S.b.t[i].as<double>(), {d, bl, br}, {1, 0, 2});  // [bl][s][br]
+  Dense u1 = mm(ctx, S.Lb[i].p(), bp.p(), l, d * br, bl, 0, 0, {l, d, br});   // [l'][s][br]
+  Dense u1p = permuted(ctx, u1.p(), u1.shp, {1, 0, 2});                   // [s][l'][br]
+  S.Lb[i + 1] = mm(ctx, xi, u1p.p(), r, br, d * l, 1, 0, {r, br});
+}
+
+// RA_i and Rb_i from RA_{i+1}, Rb_{i+1} and the right-orthonormal x_i.
+void right_env(LinsolveState& S, int i) {
+  tnfa_ctx* ctx = S.ctx;
+  const int d = S.d;
+  const int l = S.bond(S.x, i), r = S.bond(S.x, i + 1);
+  const int wl = S.bond(S.A, i), wr = S.bond(S.A, i + 1);
+  const int bl = S.bond(S.b, i), br = S.bond(S.b, i + 1);
+  const double* xi = S.x.t[i].as<double>();
+  Dense Rp = permuted(ctx, S.RA[i + 1].p(), S.RA[i + 1].shp, {2, 0, 1});  // [r][r'][wr]
+  Dense t1 = mm(ctx, xi, Rp.p(), d * l, r * wr, r, 0, 0, {d, l, r, wr});  // [s][l][r'][wr]
+  Dense t1p = permuted(ctx, t1.p(), t1.shp, {0, 3, 1, 2});                // [s][wr][l][r']
+  Dense Ap = permuted(ctx, S.A.t[i].as<double>(), {d, d, wl, wr}, {0, 2, 1, 3});  // [o][wl][s][wr]
+  Dense t2 = mm(ctx, Ap.p(), t1p.p(), d * wl, l * r, d * wr, 0, 0, {d, wl, l, r});  // [o][wl][l][r']
+  Dense t2p = permuted(ctx, t2.p(), t2.shp, {0, 3, 1, 2});                // [o][r'][wl][l]
+  Dense xp = permuted(ctx, xi, {d, l, r}, {1, 0, 2});                     // [l'][o][r']
+  S.RA[i] = mm(ctx, xp.p(), t2p.p(), l, wl * l, d * r, 0, 0, {l, wl, l});
+  Dense v1 = mm(ctx, S.b.t[i].as<double>(), S.Rb[i + 1].p(), d * bl, r, br, 0, 1, {d, bl, r});
+  Dense v1p = permuted(ctx, v1.p(), v1.shp, {0, 2, 1});                   // [s][r'][bl]
+  S.Rb[i] = mm(ctx, xp.p(), v1p.p(), l, bl, d * r, 0, 0, {l, bl});
+}
+
+__global__ void k_shift_diag(double* H, int n, double a0, double a1) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn;
+       i += (int64_t)gridDim.x * blockDim.x)
+    H[i] = a1 * H[i] + ((i / n) == (i % n) ? a0 : 0.0);
+}
+
+constexpr int kLocalDenseMax = 8192;  // largest two-site system solved densely
+
+// Solve the projected system at bond (i, i+1); returns v [l][s1][s2][r].
+Dense local_solve(LinsolveState& S, int i, double a0, double a1) {
+  tnfa_ctx* ctx = S.ctx;
+  const int d = S.d;
+  const int l = S.bond(S.x, i), r = S.bond(S.x, i + 2);
+  const int wl = S.bond(S.A, i), wm = S.bond(S.A, i + 1), wr = S.bond(S.A, i + 2);
+  const int64_t n64 = (int64_t)l * d * d * r;
+  TNFA_CHECK(n64 <= kLocalDenseMax, TNFA_ERR_UNSUPPORTED,
+             "linsolve: two-site system of dimension " + std::to_string(n64) +
+                 " above the dense limit " + std::to_string(kLocalDenseMax) + " (lower maxdim)");
+  const int n = (int)n64;
+  // H[l' s1' s2' r'][l s1 s2 r] = LA_i A_i A_{i+1} RA_{i+2}
+  Dense Lp = permuted(ctx, S.LA[i].p(), S.LA[i].shp, {0, 2, 1});                       // [l'][l][wl]
+  Dense A1 = permuted(ctx, S.A.t[i].as<double>(), {d, d, wl, wm}, {2, 0, 1, 3});      // [wl][o][in][wm]
+  Dense P1 = mm(ctx, Lp.p(), A1.p(), l * l, d * d * wm, wl, 0, 0, {l, l, d, d, wm});
+  Dense A2 = permuted(ctx, S.A.t[i + 1].as<double>(), {d, d, wm, wr}, {2, 0, 1, 3});  // [wm][o][in][wr]
+  Dense Rp = permuted(ctx, S.RA[i + 2].p(), S.RA[i + 2].shp, {1, 0, 2});              // [wr][r'][r]
+  Dense P2 = mm(ctx, A2.p(), Rp.p(), wm * d * d, r * r, wr, 0, 0, {wm, d, d, r, r});
+  Dense Hr = mm(ctx, P1.p(), P2.p(), l * l * d * d, d * d * r * r, wm, 0, 0,
+                {l, l, d, d, d, d, r, r});  // [l'][l][s1'][s1][s2'][s2][r'][r]
+  Dense H = permuted(ctx, Hr.p(), Hr.shp, {0, 2, 4, 6, 1, 3, 5, 7});
+  k_shift_diag<<<grid_for(n64 * n64, 256, 8192), 256, 0, ctx->stream>>>(H.p(), n, a0, a1);
+  TNFA_LAUNCH_CHECK();
+  // g[l][s1][s2][r] = Lb_i b_i b_{i+1} Rb_{i+2}
+  const int bl = S.bond(S.b, i), bm = S.bond(S.b, i + 1), br = S.bond(S.b, i + 2);
+  Dense b1 = permuted(ctx, S.b.t[i].as<double>(), {d, bl, bm}, {1, 0, 2});      // [bl][s][bm]
+  Dense G1 = mm(ctx, S.Lb[i].p(), b1.p(), l, d * bm, bl, 0, 0, {l, d, bm});
+  Dense b2 = permuted(ctx, S.b.t[i + 1].as<double>(), {d, bm, br}, {1, 0, 2});  // [bm][s][br]
+  Dense G2 = mm(ctx, G1.p(), b2.p(), l * d, d * br, bm, 0, 0, {l, d, d, br});
+  Dense g = mm(ctx, G2.p(), S.Rb[i + 2].p(), l * d * d, r, br, 0, 1, {l, d, d, r});
+  TNFA_CHECK(la::lu_solve(ctx, H.p(), g.p(), n), TNFA_ERR_NOT_CONVERGED,
+             "linsolve: singular two-site system at bond " + std::to_string(i + 1));
+  return g;
+}
+
+// Write v [l][s1][s2][r] back as x_i x_{i+1} through a truncated SVD; the
+// centre ends in x_{i+1} (toward_right) or in x_i.
+void store_two_site(LinsolveState& S, int i, const Dense& v, const tnfa_trunc_params& tp,
+                    TruncStats& st, bool toward_right) {
+  tnfa_ctx* ctx = S.ctx;
+  const int d = S.d;
+  const int l = S.bond(S.x, i), r = S.bond(S.x, i + 2);
+  // a two-vertex work: vertex 0 = v as [(l s1)][1][(s2 r)], vertex 1 = the
+  // identity on (s2 r); split_bond leaves U in vertex 0 and S V^T in vertex 1
+  Work<double> two{ctx, Topo{}, {}};
+  two.topo.V = 2;
+  two.topo.parent = {-1, 0};
+  two.topo.link = {1, d * r};
+  two.topo.nlegs = {0, 0};
+  two.topo.finalize();
+  two.topo.site_dim = {l * d, d * r};
+  const int64_t nv = (int64_t)l * d * d * r;
+  two.t.emplace_back(ctx, (size_t)nv * 8);
+  TNFA_CUDA(cudaMemcpyAsync(two.t[0].p, v.p(), (size_t)nv * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  {
+    const int q = d * r;
+    std::vector<double> eye((size_t)q * q, 0.0);
+    for (int k = 0; k < q; ++k) eye[(size_t)k * q + k] = 1.0;
+    two.t.emplace_back(ctx, eye.size() * 8);
+    TNFA_CUDA(cudaMemcpyAsync(two.t[1].p, eye.data(), eye.size() * 8, cudaMemcpyHostToDevice,
+                              ctx->stream));
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  split_bond(two, 0, 1, tp, st);
+  const int k = two.topo.link[1];
+  Dense x0 = permuted(ctx, two.t[0].as<double>(), {l, d, k}, {1, 0, 2});  // [s1][l][k]
+  Dense x1 = permuted(ctx, two.t[1].as<double>(), {d, r, k}, {0, 2, 1});  // [s2][k][r]
+  S.x.t[i] = std::move(x0.b);
+  S.x.t[i + 1] = std::move(x1.b);
+  S.x.topo.link[i + 1] = k;
+  if (!toward_right) {
+    // x_{i+1} = Q R with Q right-orthonormal; R moves into x_i
+    DBuf R;
+    const int kq = qr_axis(S.x, i + 1, 1, R);
+    absorb(S.x, i, 2, R.p, kq);
+    S.x.topo.link[i + 1] = kq;
+  }
+  S.x.topo.finalize();
+}
+
+// ||net|| through a QR sweep toward the root (backward stable).
+double qr_norm(tnfa_ctx* ctx, const tnfa_net* net) {
+  Work<double> w = load_work<double>(ctx, net);
+  orthogonalize_to_roots(w);
+  double s2 = 0;
+  for (int r : w.topo.roots()) {
+    const double x = host_norm<double>(ctx, w.t[r], w.size(r));
+    s2 += x * x;
+  }
+  return std::sqrt(s2);
+}
+
+struct NetHold {
+  tnfa_net* p = nullptr;
+  NetHold() = default;
+  explicit NetHold(tnfa_net* q) : p(q) {}
+  NetHold(const NetHold&) = delete;
+  NetHold& operator=(const NetHold&) = delete;
+  ~NetHold() {
+    if (p) tnfa_net_destroy(p);
+  }
+};
+
+void abi(tnfa_ctx* ctx, int status) {
+  if (status != TNFA_OK) fail(status, ctx->last_error);
+}
+
+// ||(a0 + a1 A) x - b|| / ||b||, every network in the path layout.
+double residual(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, Work<double>& x, double a0,
+                double a1, double bnorm) {
+  NetHold xr(store_work(x, TNFA_F64));
+  Work<double> ax = apply_exact<double>(ctx, A, xr.p);
+  NetHold y(store_work(ax, TNFA_F64));
+  abi(ctx, tnfa_net_scale(ctx, y.p, 0, a1, 0.0));
+  NetHold bneg;
+  abi(ctx, tnfa_net_copy(ctx, b, &bneg.p));
+  abi(ctx, tnfa_net_scale(ctx, bneg.p, 0, -1.0, 0.0));
+  NetHold r1(direct_sum_ext(ctx, y.p, bneg.p));
+  if (a0 == 0.0) return qr_norm(ctx, r1.p) / bnorm;
+  abi(ctx, tnfa_net_scale(ctx, xr.p, 0, a0, 0.0));
+  NetHold r2(direct_sum_ext(ctx, r1.p, xr.p));
+  return qr_norm(ctx, r2.p) / bnorm;
+}
+
 }  // namespace
 
 tnfa_net* apply_truncate(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f,
@@ -964,6 +1322,82 @@ tnfa_net* truncate_net(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_trunc_params
     return truncate_work(w, TNFA_C128, prm);
   }
   fail(TNFA_ERR_DTYPE, "truncate: FP64 or complex128 networks");
+}
+
+tnfa_net* direct_sum(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g);  // algebra.cu
+
+namespace {
+tnfa_net* direct_sum_ext(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g) {
+  return direct_sum(ctx, f, g);
+}
+}  // namespace
+
+tnfa_net* linsolve_path(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnfa_net* x0,
+                        const tnfa_linsolve_params& prm, double* rel_res) {
+  TNFA_CHECK(A->dtype == TNFA_F64 && b->dtype == TNFA_F64 && x0->dtype == TNFA_F64, TNFA_ERR_DTYPE,
+             "linsolve works on FP64 networks");
+  check_same_tree(A->topo, b->topo, "linsolve (A, b)");
+  check_same_tree(x0->topo, b->topo, "linsolve (x0, b)");
+  TNFA_CHECK(b->topo.V >= 2, TNFA_ERR_UNSUPPORTED, "linsolve needs at least two vertices");
+  for (int v = 0; v < b->topo.V; ++v)
+    TNFA_CHECK(b->topo.nlegs[v] == 1, TNFA_ERR_UNSUPPORTED, "linsolve needs one site leg per vertex");
+  for (int l = 0; l < b->topo.leg_off[b->topo.V]; ++l) {
+    TNFA_CHECK(A->topo.leg_kind[l] == TNFA_LEG_OPERATOR && b->topo.leg_kind[l] != TNFA_LEG_OPERATOR &&
+                   x0->topo.leg_kind[l] != TNFA_LEG_OPERATOR,
+               TNFA_ERR_INVALID_ARGUMENT, "linsolve(A, b, x0): A an operator, b and x0 functions");
+    TNFA_CHECK(b->topo.leg_dim[l] == b->topo.leg_dim[0] && x0->topo.leg_dim[l] == b->topo.leg_dim[l] &&
+                   A->topo.leg_dim[l] == b->topo.leg_dim[l] * b->topo.leg_dim[l],
+               TNFA_ERR_SHAPE, "linsolve: site dimensions of A, b, x0 disagree");
+  }
+  const std::vector<int> ord = path_order(b->topo);
+  const int L = b->topo.V;
+  LinsolveState S{ctx, L, b->topo.leg_dim[0],
+                  relayout<double>(ctx, x0->topo, x0->d, path_topo(x0->topo, ord), ord),
+                  relayout<double>(ctx, A->topo, A->d, path_topo(A->topo, ord), ord),
+                  relayout<double>(ctx, b->topo, b->d, path_topo(b->topo, ord), ord),
+                  {}, {}, {}, {}};
+  NetHold An(store_work(S.A, TNFA_F64)), bn(store_work(S.b, TNFA_F64));
+  const double bnorm = qr_norm(ctx, bn.p);
+  TNFA_CHECK(bnorm > 0, TNFA_ERR_INVALID_ARGUMENT, "linsolve: b is zero");
+  orthogonalize_to_roots(S.x);  // right-orthonormal, centre at vertex 0
+  S.x.topo.finalize();
+  S.LA.resize(L + 1);
+  S.RA.resize(L + 1);
+  S.Lb.resize(L + 1);
+  S.Rb.resize(L + 1);
+  S.LA[0] = ones(ctx, {1, 1, 1});
+  S.RA[L] = ones(ctx, {1, 1, 1});
+  S.Lb[0] = ones(ctx, {1, 1});
+  S.Rb[L] = ones(ctx, {1, 1});
+  for (int i = L - 1; i >= 2; --i) right_env(S, i);
+  const tnfa_trunc_params tp{prm.cutoff, prm.maxdim, 1, 0, TNFA_PREC_F64};
+  TruncStats st;
+  double res = residual(ctx, An.p, bn.p, S.x, prm.a0, prm.a1, bnorm);
+  for (int sweep = 0; sweep < prm.nsweeps && res > prm.tol; ++sweep) {
+    for (int dir = 0; dir < 2 && res > prm.tol; ++dir) {
+      for (int step = 0; step + 1 < L; ++step) {
+        const int i = dir == 0 ? step : L - 2 - step;
+        Dense v = local_solve(S, i, prm.a0, prm.a1);
+        store_two_site(S, i, v, tp, st, dir == 0);
+        if (dir == 0) left_env(S, i);
+        else right_env(S, i + 1);
+      }
+      res = residual(ctx, An.p, bn.p, S.x, prm.a0, prm.a1, bnorm);
+    }
+  }
+  if (rel_res) *rel_res = res;
+  // back to the caller's numbering and rooting
+  NetHold xp(store_work(S.x, TNFA_F64));
+  Topo back = x0->topo;
+  for (int k = 1; k < L; ++k) {
+    const int c = ord[k], cp = ord[k - 1];
+    (back.parent[c] == cp ? back.link[c] : back.link[cp]) = S.x.topo.link[k];
+  }
+  back.finalize();
+  std::vector<int> pos(L);
+  for (int k = 0; k < L; ++k) pos[ord[k]] = k;
+  Work<double> wb = relayout<double>(ctx, xp.p->topo, xp.p->d, back, pos);
+  return store_work(wb, TNFA_F64);
 }
 
 void inner_product(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, bool conjF, double* out) {
@@ -1072,6 +1506,22 @@ int tnfa_inner(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, double* out)
   require_net(g, "inner g");
   TNFA_CHECK(out, TNFA_ERR_INVALID_ARGUMENT, "null out");
   inner_product(ctx, f, g, true, out);
+  TNFA_API_END
+}
+
+int tnfa_linsolve(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnfa_net* x0,
+                  const tnfa_linsolve_params* params, tnfa_net** x, double* rel_residual) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(A, "linsolve A");
+  require_net(b, "linsolve b");
+  require_net(x0, "linsolve x0");
+  TNFA_CHECK(params && x, TNFA_ERR_INVALID_ARGUMENT, "null params or out");
+  TNFA_CHECK(params->maxdim >= 0 && params->cutoff >= 0 && params->tol >= 0, TNFA_ERR_INVALID_ARGUMENT,
+             "negative linsolve parameter");
+  double rr = 0;
+  *x = linsolve_path(ctx, A, b, x0, *params, &rr);
+  if (rel_residual) *rel_residual = rr;
   TNFA_API_END
 }
 

@@ -71,6 +71,7 @@ from .grad import TTNEvaluate, evaluate_vjp
 from .integration import integrate, partial_integrate
 from .network import ITensorNetworkFunction, calculate_fx, evaluate, inner
 from .operate import operate, operate_batched
+from .solvers import linsolve
 from .truncation import truncate, truncate_batched
 
 __version__ = "0.1.0"

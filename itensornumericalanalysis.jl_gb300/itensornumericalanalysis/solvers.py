@@ -1,0 +1,41 @@
+"""Linear solve on tree tensor networks.
+
+The reference hands its solver sweeps to ITensorNetworks (``dmrg`` in
+examples/2d_laplace_solver.jl:33-34, and ``linsolve`` with the signature
+``linsolve(A, b, x0; nsweeps, ...)`` solving ``(a0 + a1 A) x = b``); here the
+sweep runs in libtnfa (tnfa_linsolve).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import _lib
+from .truncation import PRECISIONS
+
+
+def linsolve(A, b, x0=None, a0: float = 0.0, a1: float = 1.0, nsweeps: int = 10,
+             maxdim: int | None = None, cutoff: float = 1e-14, tol: float = 1e-10,
+             krylov_dim: int = 0, precision: str = "f64"):
+    """Solve (a0 + a1 A) x = b for x, A an ITensorNetworkOperator and b an
+    ITensorNetworkFunction on the same path-shaped tree (a comb of two
+    dimensions is a path).
+
+    Two-site alternating sweeps: each update solves the system projected onto
+    the current left and right bases densely on the device (FP64 LU with
+    partial pivoting) and splits the two-site solution by an SVD truncated
+    with ``cutoff`` / ``maxdim``.  Sweeps stop after ``nsweeps`` or as soon as
+    ||(a0 + a1 A) x - b|| / ||b|| <= tol; that residual, evaluated exactly in
+    FP64, is stored on the result as ``x.rel_residual``.  ``x0`` (default b)
+    seeds the sweep.
+    """
+    if x0 is None:
+        x0 = b
+    p = _lib.LinsolveParams(int(nsweeps), int(maxdim or 0), float(cutoff), float(tol),
+                            int(krylov_dim), PRECISIONS[precision], float(a0), float(a1))
+    h = C.c_void_p()
+    res = C.c_double(0.0)
+    b.ctx.call("tnfa_linsolve", A.handle, b.handle, x0.handle, C.byref(p), C.byref(h),
+               C.byref(res))
+    x = b._wrap(h)
+    x.rel_residual = float(res.value)
+    return x

@@ -1,0 +1,115 @@
+"""Linear solve by two-site sweeps on the GPU, against a dense FP64 solve with
+the oracle's operator matrix (the finite-difference stencils of
+src/elementary_operators.jl:122-189 written out as dense digit operators)."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _dense_operator(terms, n_sites, axis_of):
+    """The operator matrix M[i, j] on the 2^n_sites grid (row-major digits)."""
+    N = 2**n_sites
+    eye = np.eye(N).reshape((2,) * n_sites + (N,))
+    return O.apply_terms_dense(terms, eye, axis_of).reshape(N, N)
+
+
+def _grid_1d(L):
+    return np.arange(2**L) / 2.0**L
+
+
+def _grid_2d(L):
+    g = _grid_1d(L)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    return np.stack([X.ravel(), Y.ravel()], axis=1)
+
+
+def _check(M, a0, a1, bv, xv, rel_residual):
+    K = a0 * np.eye(M.shape[0]) + a1 * M
+    ref = np.linalg.solve(K, bv)
+    err = np.linalg.norm(xv - ref) / np.linalg.norm(ref)
+    res = np.linalg.norm(K @ xv - bv) / np.linalg.norm(bv)
+    return err, res
+
+
+def test_second_derivative_path(ina):
+    """d2/dx2 x = b on a 9-bit path with Dirichlet boundaries."""
+    L = 9
+    s = ina.continuous_siteinds(ina.named_path_graph(L))
+    b = ina.rand_itn(s, link_space=2, rng=70)
+    A = ina.second_derivative_operator(s)
+    x = ina.linsolve(A, b, nsweeps=4, cutoff=1e-15, tol=1e-12)
+    M = _dense_operator(O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2), L,
+                        {(1, k): k - 1 for k in range(1, L + 1)})
+    xs = _grid_1d(L)
+    err, res = _check(M, 0.0, 1.0, b.evaluate_batch(xs), x.evaluate_batch(xs), x.rel_residual)
+    assert err < 1e-9, err
+    assert res < 1e-11, res
+    assert x.rel_residual < 1e-11
+    # the reported residual is the dense one up to rounding
+    assert abs(x.rel_residual - res) < 1e-11 + 1e-3 * res
+
+
+@pytest.mark.parametrize("a0,a1", [(0.0, 1.0), (1.0, -1e-3), (2.0, 0.5)])
+def test_laplacian_comb(ina, a0, a1):
+    """(a0 + a1 Laplacian) u = b on a 2 x 5 comb (a 10-site path whose layout
+    root sits mid-path), x0 random."""
+    L = 5
+    g = ina.named_comb_tree((2, L))
+    s = ina.continuous_siteinds(g, [[(1, j) for j in range(L, 0, -1)],
+                                    [(2, j) for j in range(1, L + 1)]])
+    b = ina.rand_itn(s, link_space=3, rng=71)
+    x0 = ina.rand_itn(s, link_space=2, rng=72)
+    A = ina.laplacian_operator(s)
+    x = ina.linsolve(A, b, x0, a0=a0, a1=a1, nsweeps=6, cutoff=1e-15, tol=1e-12)
+    terms = (O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2, dim=1)
+             + O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2, dim=2))
+    axis_of = {(1, k): k - 1 for k in range(1, L + 1)}
+    axis_of.update({(2, k): L + k - 1 for k in range(1, L + 1)})
+    M = _dense_operator(terms, 2 * L, axis_of)
+    X = _grid_2d(L)
+    err, res = _check(M, a0, a1, b.evaluate_batch(X, [1, 2]), x.evaluate_batch(X, [1, 2]),
+                      x.rel_residual)
+    assert err < 1e-8, err
+    assert res < 1e-10, res
+    assert abs(x.rel_residual - res) < 1e-11 + 1e-3 * res
+
+
+def test_poisson_sine_source(ina):
+    """Laplacian u = sin(pi x) sin(pi y) (the Laplace workload's source term)
+    on a 2 x 6 comb: the solution tracks -sin(pi x) sin(pi y) / (2 pi^2) up to
+    the discretisation error, and the bond dimension stays small."""
+    L = 6
+    g = ina.named_comb_tree((2, L))
+    s = ina.continuous_siteinds(g, [[(1, j) for j in range(L, 0, -1)],
+                                    [(2, j) for j in range(1, L + 1)]])
+    b = ina.sin_itn(s, k=np.pi, dim=1) * ina.sin_itn(s, k=np.pi, dim=2)
+    A = ina.laplacian_operator(s)
+    x = ina.linsolve(A, b, nsweeps=6, maxdim=16, cutoff=1e-14, tol=1e-10)
+    assert x.rel_residual < 1e-10
+    X = _grid_2d(L)
+    exact = -np.sin(np.pi * X[:, 0]) * np.sin(np.pi * X[:, 1]) / (2 * np.pi**2)
+    got = x.evaluate_batch(X, [1, 2])
+    # O(h) boundary error (the grid's left Dirichlet node sits at x = -h)
+    assert np.max(np.abs(got - exact)) < 0.05 * np.max(np.abs(exact))
+    assert x.maxlinkdim() <= 16
+
+
+def test_maxdim_caps_solution(ina):
+    L = 8
+    s = ina.continuous_siteinds(ina.named_path_graph(L))
+    b = ina.rand_itn(s, link_space=6, rng=73)
+    A = ina.second_derivative_operator(s)
+    x = ina.linsolve(A, b, nsweeps=2, maxdim=3, cutoff=0.0, tol=0.0)
+    assert x.maxlinkdim() <= 3
+    assert np.isfinite(x.rel_residual) and x.rel_residual > 0
+
+
+def test_non_path_rejected(ina):
+    s = ina.continuous_siteinds(ina.named_binary_tree(7))
+    b = ina.rand_itn(s, link_space=2, rng=74)
+    A = ina.second_derivative_operator(s)
+    with pytest.raises(ina.TnfaError, match="path"):
+        ina.linsolve(A, b)
