@@ -204,13 +204,19 @@ void convert_f64_to_f32(tnfa_ctx* ctx, const double* src, float* dst, int64_t n)
 
 // Launch accounting: construct before a launch, destroy after it.  Counts
 // the launch and its algorithmic work; records CUDA events when timing is on.
+// With the environment variable TNFA_TRACE set (to a file path, or to 1 for
+// stderr) every launch is also timed and written out as one line: family,
+// algorithmic flops, milliseconds and the launcher's note.
 struct KernelScope {
   tnfa_ctx* ctx;
   int fam;
+  double flops;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  std::string note;
   KernelScope(tnfa_ctx* c, const char* family, double flops, double bytes);
   ~KernelScope();
 };
+bool trace_on();
 
 inline unsigned grid_for(int64_t n, int block, int cap = 1 << 20) {
   int64_t g = (n + block - 1) / block;

