@@ -178,6 +178,20 @@ void gemm(tnfa_ctx* ctx, const std::vector<GemmJob>& jobs) {
   TNFA_LAUNCH_CHECK();
 }
 
+template <class Job>
+std::string size_note(const std::vector<Job>& jobs) {
+  int mm = 0, mn = 0;
+  double work = 0;
+  for (const auto& j : jobs) {
+    mm = std::max(mm, j.m);
+    mn = std::max(mn, j.n);
+    work += (double)j.m * j.n * j.n;
+  }
+  char b[160];
+  snprintf(b, sizeof b, "jobs=%zu max_m=%d max_n=%d sum_mn2=%.3g", jobs.size(), mm, mn, work);
+  return b;
+}
+
 // ------------------------------------------------------------------ qr --
 template <class T>
 __device__ inline T block_sum(T v, T* red) {
@@ -307,20 +321,6 @@ void qr(tnfa_ctx* ctx, const std::vector<QrJob>& jobs) {
 }
 
 // ----------------------------------------------------------------- svd --
-template <class Job>
-std::string size_note(const std::vector<Job>& jobs) {
-  int mm = 0, mn = 0;
-  double work = 0;
-  for (const auto& j : jobs) {
-    mm = std::max(mm, j.m);
-    mn = std::max(mn, j.n);
-    work += (double)j.m * j.n * j.n;
-  }
-  char b[160];
-  snprintf(b, sizeof b, "jobs=%zu max_m=%d max_n=%d sum_mn2=%.3g", jobs.size(), mm, mn, work);
-  return b;
-}
-
 void trace_sweeps(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs) {
   int mx = 0, capped = 0, cnt = 0;
   long tot = 0;
