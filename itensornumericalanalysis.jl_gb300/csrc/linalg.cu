@@ -10,7 +10,11 @@
 #include <cmath>
 #include <cstdlib>
 
+#include <cooperative_groups.h>
+
 #include "linalg.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace tnfa {
 namespace la {
@@ -27,6 +31,13 @@ __host__ __device__ inline cplx scal(cplx x, double a) { return {x.re * a, x.im 
 template <class T> __host__ __device__ inline T from_real(double a);
 template <> __host__ __device__ inline double from_real<double>(double a) { return a; }
 template <> __host__ __device__ inline cplx from_real<cplx>(double a) { return {a, 0.0}; }
+__host__ __device__ inline float re(float x) { return x; }
+__host__ __device__ inline float abs2(float x) { return x * x; }
+__host__ __device__ inline float conj(float x) { return x; }
+__host__ __device__ inline float scal(float x, float a) { return x * a; }
+template <> __host__ __device__ inline float from_real<float>(double a) { return (float)a; }
+__device__ inline float shfl_xor(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ inline float phase(float x) { return x < 0 ? -1.0f : 1.0f; }
 __device__ inline double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 __device__ inline cplx shfl_xor(cplx v, int o) {
   return {__shfl_xor_sync(0xffffffffu, v.re, o), __shfl_xor_sync(0xffffffffu, v.im, o)};
@@ -463,28 +474,212 @@ __global__ void __launch_bounds__(512) k_svd(const SvdJob* __restrict__ jobs, T*
   if (threadIdx.x == 0 && jb.sweeps) *jb.sweeps = converged ? sweep : -1;
 }
 
+// The same Jacobi iteration spread over a thread-block cluster: the pairs of a
+// round are shared by the warps of all CTAs of the cluster, the columns live
+// in global memory (L2-resident; loads and stores bypass L1), and a cluster
+// barrier (release / acquire at cluster scope) separates the rounds.  The
+// convergence decision of a sweep is read by every CTA from one global flag
+// after the sweep's last barrier, so all CTAs leave the loop together; flag
+// k % 3 is cleared two sweeps before it is reused, after every CTA has read it.
+template <class T> struct RealOf { using type = double; };
+template <> struct RealOf<float> { using type = float; };
+
+__device__ inline double ldcg(const double* p) { return __ldcg(p); }
+__device__ inline float ldcg(const float* p) { return __ldcg(p); }
+__device__ inline cplx ldcg(const cplx* p) {
+  const double2 v = __ldcg((const double2*)p);
+  return {v.x, v.y};
+}
+__device__ inline void stcg(double* p, double v) { __stcg(p, v); }
+__device__ inline void stcg(float* p, float v) { __stcg(p, v); }
+__device__ inline void stcg(cplx* p, cplx v) { __stcg((double2*)p, make_double2(v.re, v.im)); }
+__device__ inline float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ inline double fmaT(double a, double b, double c) { return fma(a, b, c); }
+__device__ inline cplx fmaT(cplx a, cplx b, cplx c) { return Sc<cplx>::fma(a, b, c); }
+
+template <class T>
+__global__ void __launch_bounds__(512) k_svd_cluster(const SvdJob* __restrict__ jobs, T* __restrict__ work,
+                                                     const int64_t* __restrict__ woff, int* __restrict__ flags,
+                                                     int max_sweeps, int init_v) {
+  using R = typename RealOf<T>::type;
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks(), crank = (int)cl.block_rank();
+  const int ji = blockIdx.x / C;
+  const SvdJob jb = jobs[ji];
+  const int m = jb.m, n = jb.n;
+  T* U = work + woff[ji];
+  T* V = U + (int64_t)m * n;
+  double* sig = (double*)(V + (int64_t)n * n);
+  int* rank = (int*)(sig + n);
+  int* flag = flags + 3 * ji;
+  const T* A = (const T*)jb.A;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int64_t gt = (int64_t)crank * blockDim.x + threadIdx.x, gs = (int64_t)C * blockDim.x;
+  for (int64_t i = gt; i < (int64_t)m * n; i += gs) {
+    const int r = (int)(i / n), c = (int)(i % n);
+    stcg(U + (int64_t)c * m + r, A[i]);
+  }
+  // V starts as the identity, or (init_v) as jb.V given row-major
+  for (int64_t i = gt; i < (int64_t)n * n; i += gs) {
+    const int c = (int)(i / n), r = (int)(i % n);
+    stcg(V + i, init_v ? ((const T*)jb.V)[(int64_t)r * n + c] : from_real<T>(r == c ? 1.0 : 0.0));
+  }
+  __shared__ double red[32];
+  double part = 0.0;
+  for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) part += (double)abs2(A[i]);
+  const double fro2 = block_sum<double>(part, red);
+  const double eps = sizeof(R) == 4 ? 1.1920929e-7 : 2.220446049250313e-16;
+  const double negl = (sizeof(R) == 4 ? 1e-13 : 1e-30) * fro2;
+  const R tol = (R)(8.0 * sqrt((double)m) * eps);
+  const int n2 = (n + 1) & ~1;
+  const int gw = crank * nw + warp, nwc = C * nw;
+  int sweep = 0;
+  bool converged = (n < 2);
+  cl.sync();
+  while (!converged && sweep < max_sweeps) {
+    if (crank == 0 && threadIdx.x == 0) flag[(sweep + 1) % 3] = 0;
+    int rotated_here = 0;
+    for (int r = 0; r < n2 - 1; ++r) {
+      for (int slot = gw; slot < n2 / 2; slot += nwc) {
+        int p, q;
+        rr_pair(n2, r, slot, p, q);
+        if (q >= n) continue;
+        T* up = U + (int64_t)p * m;
+        T* uq = U + (int64_t)q * m;
+        R a = 0, b = 0;
+        T g = from_real<T>(0.0);
+        for (int i = lane; i < m; i += 32) {
+          const T xp = ldcg(up + i), xq = ldcg(uq + i);
+          a += abs2(xp);
+          b += abs2(xq);
+          g = fmaT(conj(xp), xq, g);
+        }
+        a = warp_sum(a);
+        b = warp_sum(b);
+        g = warp_sum(g);
+        const R ag = sqrt(abs2(g));
+        if (ag <= tol * sqrt(a * b) || ag == (R)0 || (double)a < negl || (double)b < negl) continue;
+        const R zeta = (b - a) / ((R)2 * ag);
+        const R big = sizeof(R) == 4 ? (R)1e18 : (R)1e150;
+        const R t = fabs(zeta) > big ? (R)0.5 / zeta
+                                     : (zeta >= 0 ? (R)1 : (R)-1) / (fabs(zeta) + sqrt((R)1 + zeta * zeta));
+        if (t == (R)0) continue;
+        const R c = (R)1 / sqrt((R)1 + t * t), sn = c * t;
+        const T e = phase(g);
+        const T se = scal(e, sn), sec = scal(conj(e), sn);
+        for (int i = lane; i < m; i += 32) {
+          const T xp = ldcg(up + i), xq = ldcg(uq + i);
+          stcg(up + i, scal(xp, c) - sec * xq);
+          stcg(uq + i, se * xp + scal(xq, c));
+        }
+        T* vp = V + (int64_t)p * n;
+        T* vq = V + (int64_t)q * n;
+        for (int i = lane; i < n; i += 32) {
+          const T xp = ldcg(vp + i), xq = ldcg(vq + i);
+          stcg(vp + i, scal(xp, c) - sec * xq);
+          stcg(vq + i, se * xp + scal(xq, c));
+        }
+        rotated_here = 1;
+      }
+      cl.sync();
+    }
+    // (a flag store after the round's barrier would still precede the read
+    // below only through the next barrier, so it is stored before the last one)
+    if (rotated_here && lane == 0) atomicOr(flag + sweep % 3, 1);
+    cl.sync();
+    converged = (__ldcg(flag + sweep % 3) == 0);
+    ++sweep;
+  }
+  for (int c = gw; c < n; c += nwc) {
+    double s2 = 0.0;
+    for (int i = lane; i < m; i += 32) s2 += (double)abs2(ldcg(U + (int64_t)c * m + i));
+    s2 = warp_sum(s2);
+    if (lane == 0) __stcg(sig + c, sqrt(s2));
+  }
+  cl.sync();
+  for (int64_t c = gt; c < n; c += gs) {
+    const double sc = __ldcg(sig + c);
+    int rk = 0;
+    for (int d = 0; d < n; ++d) {
+      const double sd = __ldcg(sig + d);
+      rk += (sd > sc) || (sd == sc && d < c);
+    }
+    __stcg(rank + c, rk);
+    jb.S[rk] = sc;
+  }
+  cl.sync();
+  T* Uo = (T*)jb.U;
+  T* Vo = (T*)jb.V;
+  for (int64_t i = gt; i < (int64_t)m * n; i += gs) {
+    const int c = (int)(i / m), r = (int)(i % m);
+    const double sc = __ldcg(sig + c);
+    Uo[(int64_t)r * n + __ldcg(rank + c)] = sc > 0 ? scal(ldcg(U + i), (R)(1.0 / sc)) : from_real<T>(0.0);
+  }
+  for (int64_t i = gt; i < (int64_t)n * n; i += gs) {
+    const int c = (int)(i / n), r = (int)(i % n);
+    Vo[(int64_t)r * n + __ldcg(rank + c)] = ldcg(V + i);
+  }
+  if (crank == 0 && threadIdx.x == 0 && jb.sweeps) *jb.sweeps = converged ? sweep : -1;
+}
+
+constexpr int SVD_CLUSTER = 8;  // CTAs (SMs) per large matrix
+
+// A job goes to the cluster kernel when its Jacobi work is large enough to
+// pay for a cluster barrier per round.
+inline bool svd_big(const SvdJob& j) { return j.n >= 96 && (double)j.m * j.n * j.n >= 2.0e6; }
+
+template <class T>
+void launch_svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, bool init_v,
+                const char* family) {
+  std::vector<SvdJob> big, small;
+  for (const auto& j : jobs) (svd_big(j) ? big : small).push_back(j);
+  for (int pass = 0; pass < 2; ++pass) {
+    const std::vector<SvdJob>& js = pass == 0 ? big : small;
+    if (js.empty()) continue;
+    std::vector<int64_t> woff(js.size() + 1, 0);
+    double fl = 0;
+    for (size_t i = 0; i < js.size(); ++i) {
+      TNFA_CHECK(js[i].m >= js[i].n, TNFA_ERR_INVALID_ARGUMENT, "svd needs m >= n");
+      const int64_t m = js[i].m, n = js[i].n;
+      // U, V in T; sig (n doubles) and rank (n ints) rounded up to T slots
+      woff[i + 1] = woff[i] + m * n + n * n + (int64_t)((n * 12 + sizeof(T) - 1) / sizeof(T)) + 2;
+      fl += 6.0 * m * n * n * 8;  // ~8 sweeps
+    }
+    DBuf work(ctx, (size_t)woff.back() * sizeof(T));
+    DBuf dw = upload(ctx, woff);
+    DBuf d = upload(ctx, js);
+    KernelScope ks(ctx, family, fl, 0.0);
+    if (trace_on()) ks.note = (pass == 0 ? "cluster " : "single ") + size_note(js);
+    if (pass == 0) {
+      DBuf flags(ctx, js.size() * 3 * sizeof(int));
+      TNFA_CUDA(cudaMemsetAsync(flags.p, 0, js.size() * 3 * sizeof(int), ctx->stream));
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3((unsigned)(js.size() * SVD_CLUSTER));
+      cfg.blockDim = dim3(512);
+      cfg.stream = ctx->stream;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = SVD_CLUSTER;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      TNFA_CUDA(cudaLaunchKernelEx(&cfg, k_svd_cluster<T>, (const SvdJob*)d.as<SvdJob>(), work.as<T>(),
+                                   (const int64_t*)dw.as<int64_t>(), flags.as<int>(), max_sweeps,
+                                   init_v ? 1 : 0));
+    } else {
+      TNFA_CHECK(!init_v, TNFA_ERR_UNSUPPORTED, "svd: initial V needs the cluster kernel");
+      k_svd<T><<<(unsigned)js.size(), 512, 0, ctx->stream>>>(d.as<SvdJob>(), work.as<T>(),
+                                                             dw.as<int64_t>(), max_sweeps);
+    }
+    TNFA_LAUNCH_CHECK();
+  }
+}
+
 template <class T>
 void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
   if (jobs.empty()) return;
-  std::vector<int64_t> woff(jobs.size() + 1, 0);
-  double fl = 0;
-  for (size_t i = 0; i < jobs.size(); ++i) {
-    TNFA_CHECK(jobs[i].m >= jobs[i].n, TNFA_ERR_INVALID_ARGUMENT, "svd needs m >= n");
-    const int64_t m = jobs[i].m, n = jobs[i].n;
-    // U, V in T; sig (n doubles) and rank (n ints) rounded up to T slots
-    woff[i + 1] = woff[i] + m * n + n * n + (int64_t)((n * 12 + sizeof(T) - 1) / sizeof(T)) + 1;
-    fl += 6.0 * m * n * n * 8;  // ~8 sweeps
-  }
-  DBuf work(ctx, (size_t)woff.back() * sizeof(T));
-  DBuf dw = upload(ctx, woff);
-  DBuf d = upload(ctx, jobs);
-  {
-    KernelScope ks(ctx, sizeof(T) == 8 ? "svd_f64" : "svd_c128", fl, 0.0);
-    if (trace_on()) ks.note = size_note(jobs);
-    k_svd<T><<<(unsigned)jobs.size(), 512, 0, ctx->stream>>>(d.as<SvdJob>(), work.as<T>(),
-                                                             dw.as<int64_t>(), max_sweeps);
-    TNFA_LAUNCH_CHECK();
-  }
+  launch_svd<T>(ctx, jobs, max_sweeps, false, sizeof(T) == 8 ? "svd_f64" : "svd_c128");
   if (trace_on()) trace_sweeps(ctx, jobs);
   // Diagnostics: with TNFA_DEBUG_DIR set, the input of every SVD that hit the
   // sweep cap is written there (int32 m, int32 n, element size, then data).

@@ -199,6 +199,23 @@ def test_truncate_recovers_rank(ina):
         assert len(kept) == t.linkdims()[(lay.order[lay.parent[i]], v)]
 
 
+@pytest.mark.parametrize("dtype", [float, complex])
+def test_truncate_large_bonds(ina, dtype):
+    """Bonds of 96 doubled to 192 by f + f (the SVDs of the middle bonds are
+    large enough for the cluster-parallel Jacobi kernel): truncation restores
+    the generic ranks min(96, 2^k, 2^(L-k)) and the values."""
+    L = 16
+    s = ina.continuous_siteinds(ina.named_path_graph(L))
+    f = ina.rand_itn(s, link_space=96, rng=24, dtype=dtype, normalize=True)
+    ff = f + f
+    assert ff.maxlinkdim() == 192
+    t = ina.truncate(ff, cutoff=1e-14)
+    X = np.random.default_rng(25).random(512)
+    assert rel_err(t.evaluate_batch(X), 2 * f.evaluate_batch(X)) < 1e-10
+    expect = sorted(min(96, 2**k, 2 ** (L - k)) for k in range(1, L))
+    assert sorted(t.linkdims().values()) == expect
+
+
 def test_truncate_maxdim_and_normalize(ina):
     graph = O.path_graph(10)
     rng = np.random.default_rng(22)
