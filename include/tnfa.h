@@ -195,12 +195,20 @@ int tnfa_integrate_operator(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* n
                             double* out);
 
 /* Contract the site legs of variables vars[0..n_vars) with the uniform
- * vector (1/base, or 1 when take_sum) and absorb vertices left without legs
- * into a neighbour.  Replaces partial_integrate (src/integration.jl:35-54) with
- * merge_internal_tensors (src/utils.jl:99-113).  The result has fewer
- * vertices; query it with tnfa_net_info / tnfa_net_topology. */
+ * vector (1/base, or 1 when take_sum) and, with merge_vertices, absorb every
+ * vertex left without legs into its first neighbour (a vertex with no
+ * neighbour left multiplies its scalar into the first vertex that still has
+ * legs).  Replaces
+ * partial_integrate (src/integration.jl:35-54) with merge_internal_tensors
+ * (src/utils.jl:99-113).  "First" follows vertex_rank (one int per vertex,
+ * e.g. the position in the caller's vertex order; NULL: the layout order).
+ * The survivors are numbered breadth first, roots and neighbours in rank
+ * order; out_vertex_of (sized n_vertices of net, may be NULL) receives the
+ * input vertex of every output vertex.  Integrating every variable is an
+ * error (use tnfa_integrate).  FP64 and complex128. */
 int tnfa_partial_integrate(tnfa_ctx* ctx, const tnfa_net* net, int32_t n_vars, const int32_t* vars,
-                           int take_sum, tnfa_net** out);
+                           int take_sum, int merge_vertices, const int32_t* vertex_rank,
+                           tnfa_net** out, int32_t* out_vertex_of);
 /* Topology of a network (arrays sized by tnfa_net_info's n_vertices and the
  * leg count returned in *n_legs_total). Any pointer may be NULL. */
 int tnfa_net_topology(const tnfa_net* net, int32_t* parent, int32_t* link_dim, int32_t* n_legs,
@@ -223,6 +231,16 @@ int tnfa_operator_proj(tnfa_ctx* ctx, const tnfa_net* f, tnfa_net** out);
  * functions of disjoint vertex sets).  Replaces the disjoint-vertex branch of
  * multiply (src/elementary_operators.jl:263-270). */
 int tnfa_net_concat(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, tnfa_net** out);
+/* Broadcast gather into another layout: output vertex t (of `target`) takes
+ * its tensor from input vertex src_vertex[t], or is all ones when it is -1;
+ * output axis a of t (its site legs one by one, then the parent bond, then
+ * the child bonds) advances the input index by strides[a] elements (0
+ * broadcasts: a leg or bond the input lacks).  Strides are listed vertex after
+ * vertex.  Lifts a factor onto the union tree for multiply on partially
+ * overlapping vertex sets (the shared-vertex branch of
+ * src/elementary_operators.jl:260-281), and re-roots or renumbers a tree. */
+int tnfa_net_gather(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_topology* target,
+                    const int32_t* src_vertex, const int64_t* strides, tnfa_net** out);
 /* Element-type conversion: F64 <-> F32, F64 -> C128, F32 -> C128. */
 int tnfa_net_convert(tnfa_ctx* ctx, const tnfa_net* f, int dtype, tnfa_net** out);
 

@@ -103,6 +103,37 @@ __global__ void k_convert(const S* __restrict__ s, D* __restrict__ d, int64_t n)
   }
 }
 
+// Strided broadcast gather: dst[i] = src[sum_a x_a(i) * st[a]] over the
+// output axes (x_a the coordinates of i); an output vertex without a source
+// is all ones.
+struct GatherJob {
+  int64_t soff, doff, n;
+  int nd;
+  int has_src;
+  int d[ALG_MAXD];
+  int64_t st[ALG_MAXD];
+};
+
+template <class T>
+__global__ void k_gather(const T* __restrict__ src, T* __restrict__ dst,
+                         const GatherJob* __restrict__ jobs) {
+  const GatherJob& jb = jobs[blockIdx.y];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < jb.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (!jb.has_src) {
+      dst[jb.doff + i] = Sc<T>::one();
+      continue;
+    }
+    int64_t r = i, si = 0;
+    for (int a = jb.nd - 1; a >= 0; --a) {
+      const int64_t x = r % jb.d[a];
+      r /= jb.d[a];
+      si += x * jb.st[a];
+    }
+    dst[jb.doff + i] = src[jb.soff + si];
+  }
+}
+
 // Axis dims of v's tensor: [site, parent, children...].
 static std::vector<int> axes(const Topo& T, int v) {
   std::vector<int> a{T.site_dim[v], T.link[v]};
@@ -314,6 +345,57 @@ tnfa_net* convert(tnfa_ctx* ctx, const tnfa_net* f, int dtype) {
   return out;
 }
 
+Topo topo_from_abi(const tnfa_topology* t);  // core.cu
+
+tnfa_net* gather(tnfa_ctx* ctx, const tnfa_net* f, const Topo& O, const int32_t* src_vertex,
+                 const int64_t* strides) {
+  const Topo& S = f->topo;
+  TNFA_CHECK(src_vertex && strides, TNFA_ERR_INVALID_ARGUMENT, "gather: null arrays");
+  tnfa_net* out = new_net(ctx, O, f->dtype);
+  std::vector<GatherJob> jobs;
+  int64_t nmax = 1, k = 0;
+  try {
+    for (int t = 0; t < O.V; ++t) {
+      GatherJob j{};
+      j.doff = O.off[t];
+      j.n = O.size(t);
+      const int sv = src_vertex[t];
+      TNFA_CHECK(sv >= -1 && sv < S.V, TNFA_ERR_INVALID_ARGUMENT, "gather: source vertex out of range");
+      j.has_src = sv >= 0;
+      j.soff = sv >= 0 ? S.off[sv] : 0;
+      std::vector<int> d;
+      for (int l = O.leg_off[t]; l < O.leg_off[t + 1]; ++l) d.push_back(O.leg_dim[l]);
+      d.push_back(O.link[t]);
+      for (int c : O.children[t]) d.push_back(O.link[c]);
+      TNFA_CHECK((int)d.size() <= ALG_MAXD, TNFA_ERR_UNSUPPORTED, "gather: vertex order above 12");
+      j.nd = (int)d.size();
+      int64_t reach = 0;
+      for (int a = 0; a < j.nd; ++a) {
+        j.d[a] = d[a];
+        j.st[a] = strides[k++];
+        TNFA_CHECK(j.st[a] >= 0, TNFA_ERR_INVALID_ARGUMENT, "gather: negative stride");
+        reach += (int64_t)(d[a] - 1) * j.st[a];
+      }
+      // every read stays inside the source vertex's tensor
+      TNFA_CHECK(sv < 0 || reach < S.size(sv), TNFA_ERR_INVALID_ARGUMENT,
+                 "gather: strides of vertex " + std::to_string(t) + " reach past its source tensor");
+      jobs.push_back(j);
+      nmax = std::max(nmax, j.n);
+    }
+    DBuf dj = upload_jobs(ctx, jobs);
+    dim3 grid(grid_for(nmax, 256, 1024), O.V);
+    TNFA_CHECK(O.V <= 65535, TNFA_ERR_UNSUPPORTED, "more than 65535 vertices");
+    TNFA_DISPATCH(f->dtype, T, {
+      k_gather<T><<<grid, 256, 0, ctx->stream>>>((const T*)f->d, (T*)out->d, dj.as<GatherJob>());
+    });
+    TNFA_LAUNCH_CHECK();
+  } catch (...) {
+    tnfa_net_destroy(out);
+    throw;
+  }
+  return out;
+}
+
 }  // namespace tnfa
 
 using namespace tnfa;
@@ -356,6 +438,17 @@ int tnfa_net_concat(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, tnfa_ne
   require_net(g, "concat g");
   TNFA_CHECK(out, TNFA_ERR_INVALID_ARGUMENT, "null out");
   *out = concat(ctx, f, g);
+  TNFA_API_END
+}
+
+int tnfa_net_gather(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_topology* target,
+                    const int32_t* src_vertex, const int64_t* strides, tnfa_net** out) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(f, "gather");
+  TNFA_CHECK(out, TNFA_ERR_INVALID_ARGUMENT, "null out");
+  Topo O = topo_from_abi(target);
+  *out = gather(ctx, f, O, src_vertex, strides);
   TNFA_API_END
 }
 

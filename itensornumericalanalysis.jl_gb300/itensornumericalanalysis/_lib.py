@@ -122,6 +122,7 @@ SIGNATURES = {
         [_P, _PI32, _PI32, _PI32, _PI32, _PI32, _PI32, _PI32, _PI32],
     ),
     "tnfa_net_concat": (C.c_int, [_P, _P, _P, _PP]),
+    "tnfa_net_gather": (C.c_int, [_P, _P, C.POINTER(Topology), _PI32, C.POINTER(C.c_int64), _PP]),
     "tnfa_net_convert": (C.c_int, [_P, _P, C.c_int, _PP]),
     "tnfa_evaluate": (
         C.c_int,
@@ -133,7 +134,7 @@ SIGNATURES = {
     ),
     "tnfa_integrate": (C.c_int, [_P, _P, C.c_int, _PD]),
     "tnfa_integrate_operator": (C.c_int, [_P, _P, _P, C.c_int, _PD]),
-    "tnfa_partial_integrate": (C.c_int, [_P, _P, _I32, _PI32, C.c_int, _PP]),
+    "tnfa_partial_integrate": (C.c_int, [_P, _P, _I32, _PI32, C.c_int, C.c_int, _PI32, _PP, _PI32]),
     "tnfa_add": (C.c_int, [_P, _P, _P, _PP]),
     "tnfa_multiply": (C.c_int, [_P, _P, _P, _PP]),
     "tnfa_operator_proj": (C.c_int, [_P, _P, _PP]),

@@ -258,7 +258,9 @@ def operator_proj(f: ITensorNetworkFunction) -> ITensorNetworkOperator:
 
 def multiply(g: ITensorNetworkFunction, f: ITensorNetworkFunction, *more) -> ITensorNetworkFunction:
     """Pointwise product (src/elementary_operators.jl:260-292): bond dims
-    multiply on shared vertices; functions on disjoint vertex sets form a forest."""
+    multiply on shared vertices; functions on disjoint vertex sets form a
+    forest; on partially shared vertex sets the product lives on the union
+    tree (legs and edges of both)."""
     if more:
         return multiply(multiply(g, f), *more)
     if g.s.same_structure(f.s):
@@ -271,7 +273,16 @@ def multiply(g: ITensorNetworkFunction, f: ITensorNetworkFunction, *more) -> ITe
         h = C.c_void_p()
         g.ctx.call("tnfa_net_concat", a.handle, b.handle, C.byref(h))
         return type(g)(g.s.union(f.s), h, g.ctx)
-    raise NotImplementedError("multiply of functions on partially overlapping vertex sets")
+    # shared vertices: the union tree, each factor lifted onto it (constant
+    # along what it lacks), then the product on one structure
+    u = g.s.union(f.s)
+    if not u.graph.is_forest():
+        raise ValueError("multiply: the union of the two trees has a cycle")
+    a, b = g._promote(f)
+    la, lb = a.lift(u), b.lift(u)
+    h = C.c_void_p()
+    g.ctx.call("tnfa_multiply", la.handle, lb.handle, C.byref(h))
+    return type(g)(u, h, g.ctx)
 
 
 def point_to_opsum(s, x, dim: int) -> OpSum:

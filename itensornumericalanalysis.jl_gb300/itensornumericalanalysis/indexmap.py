@@ -233,10 +233,11 @@ class IndsNetworkMap:
             g.add_vertex(v)
         for u, w in other.graph.edges():
             g.add_edge(u, w)
-        legs = dict(self.legs)
+        legs = {v: list(ls) for v, ls in self.legs.items()}
         for v in other.vertices():
-            if v not in legs:
-                legs[v] = other.legs[v]
+            mine = legs.setdefault(v, [])
+            have = {(l.dim, l.digit, l.kind) for l in mine}
+            mine.extend(l for l in other.legs[v] if (l.dim, l.digit, l.kind) not in have)
         return IndsNetworkMap(g, legs, self.is_complex or other.is_complex)
 
     def same_structure(self, other: "IndsNetworkMap") -> bool:

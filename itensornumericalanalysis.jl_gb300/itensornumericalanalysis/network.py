@@ -135,6 +135,54 @@ class ITensorNetworkFunction:
         return {(lay.order[lay.parent[i]], lay.order[i]): link[i]
                 for i in range(lay.n) if lay.parent[i] >= 0}
 
+    def lift(self, u: IndsNetworkMap) -> "ITensorNetworkFunction":
+        """This function as a network on the tree of `u` (a map containing this
+        one's vertices, edges and legs): constant along the legs and vertices
+        it lacks, bond 1 on the edges it lacks (tnfa_net_gather)."""
+        fl, ul = self.s.layout, u.layout
+        link = self.info()[3]
+        bond = {}
+        for i in range(fl.n):
+            if fl.parent[i] >= 0:
+                bond[frozenset((fl.order[i], fl.order[fl.parent[i]]))] = link[i]
+        link_u = [1] * ul.n
+        for t, v in enumerate(ul.order):
+            if ul.parent[t] >= 0:
+                link_u[t] = bond.get(frozenset((v, ul.order[ul.parent[t]])), 1)
+        nlegs_f, ldim_f = self._leg_shape()
+        src, strides = [], []
+        for t, v in enumerate(ul.order):
+            nbs = ([ul.order[ul.parent[t]]] if ul.parent[t] >= 0 else [None]) + [
+                ul.order[c] for c in ul.children[t]]
+            if v not in fl.pos:
+                src.append(-1)
+                strides += [0] * (len(u.legs[v]) + len(nbs))
+                continue
+            i = fl.pos[v]
+            src.append(i)
+            dims = list(ldim_f[i]) + [link[i]] + [link[c] for c in fl.children[i]]
+            st = [1] * len(dims)
+            for a in range(len(dims) - 2, -1, -1):
+                st[a] = st[a + 1] * dims[a + 1]
+            key = {(l.dim, l.digit, l.kind): k for k, l in enumerate(self.s.legs[v])}
+            for l in u.legs[v]:
+                k = key.get((l.dim, l.digit, l.kind))
+                strides.append(st[k] if k is not None else 0)
+            nl = nlegs_f[i]
+            axis = {}
+            if fl.parent[i] >= 0:
+                axis[fl.order[fl.parent[i]]] = nl
+            for k, c in enumerate(fl.children[i]):
+                axis[fl.order[c]] = nl + 1 + k
+            for w in nbs:
+                strides.append(st[axis[w]] if w in axis else 0)
+        topo, keep = topology_struct(u, link_u)
+        srcv = (C.c_int32 * ul.n)(*src)
+        stv = (C.c_int64 * max(1, len(strides)))(*strides)
+        h = C.c_void_p()
+        self._ctx.call("tnfa_net_gather", self._h, C.byref(topo), srcv, stv, C.byref(h))
+        return type(self)(u, h, self._ctx)
+
     def maxlinkdim(self) -> int:
         d = self.linkdims()
         return max(d.values()) if d else 1
