@@ -104,6 +104,6 @@ def test_fit_decreases_loss(ina):
         loss = torch.mean((pred - target) ** 2)
         loss.backward()
         opt.step()
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
     assert losses[-1] < 0.6 * losses[0], losses[::10]
     assert all(np.isfinite(losses))
