@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <type_traits>
 
 #include <cooperative_groups.h>
 
@@ -363,124 +364,25 @@ __device__ inline void rr_pair(int n2, int r, int i, int& p, int& q) {
   }
 }
 
-template <class T>
-__global__ void __launch_bounds__(512) k_svd(const SvdJob* __restrict__ jobs, T* __restrict__ work,
-                                             const int64_t* __restrict__ woff, int max_sweeps) {
-  const SvdJob jb = jobs[blockIdx.x];
-  const int m = jb.m, n = jb.n;
-  T* U = work + woff[blockIdx.x];     // column-major m x n (columns contiguous)
-  T* V = U + (int64_t)m * n;          // column-major n x n
-  double* sig = (double*)(V + (int64_t)n * n);
-  int* rank = (int*)(sig + n);
-  const T* A = (const T*)jb.A;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __shared__ int rotated;
-  for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) {
-    const int r = (int)(i / n), c = (int)(i % n);
-    U[(int64_t)c * m + r] = A[i];
-  }
-  for (int64_t i = threadIdx.x; i < (int64_t)n * n; i += blockDim.x)
-    V[i] = from_real<T>((i / n) == (i % n) ? 1.0 : 0.0);
-  __shared__ double red[32];
-  double part = 0.0;
-  for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) part += abs2(A[i]);
-  const double fro2 = block_sum<double>(part, red);
-  // columns below this are rounding noise of the whole matrix
-  const double negl = 1e-30 * fro2;
-  const int n2 = (n + 1) & ~1;
-  int sweep = 0;
-  bool converged = (n < 2);
-  // pairs count as orthogonal once |g| <= tol sqrt(a b); the rounding floor of
-  // a length-m dot product is ~sqrt(m) eps
-  const double tol = 8.0 * sqrt((double)m) * 2.220446049250313e-16;
-  while (!converged && sweep < max_sweeps) {
-    if (threadIdx.x == 0) rotated = 0;
-    __syncthreads();
-    for (int r = 0; r < n2 - 1; ++r) {
-      for (int slot = warp; slot < n2 / 2; slot += nw) {
-        int p, q;
-        rr_pair(n2, r, slot, p, q);
-        if (q >= n) continue;
-        T* up = U + (int64_t)p * m;
-        T* uq = U + (int64_t)q * m;
-        double a = 0.0, b = 0.0;
-        T g = from_real<T>(0.0);
-        for (int i = lane; i < m; i += 32) {
-          a += abs2(up[i]);
-          b += abs2(uq[i]);
-          g = Sc<T>::fma(conj(up[i]), uq[i], g);
-        }
-        a = warp_sum(a);
-        b = warp_sum(b);
-        g = warp_sum(g);
-        const double ag = sqrt(abs2(g));
-        // a negligible column carries no singular value worth orthogonalising
-        // against; skipping it also avoids zeta^2 overflow on extreme ratios
-        if (ag <= tol * sqrt(a * b) || ag == 0.0 || a < negl || b < negl) continue;
-        const double zeta = (b - a) / (2.0 * ag);
-        const double t = fabs(zeta) > 1e150
-                             ? 0.5 / zeta
-                             : (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        if (t == 0.0) continue;
-        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
-        const T e = phase(g);  // g / |g|
-        const T se = scal(e, s), sec = scal(conj(e), s);
-        for (int i = lane; i < m; i += 32) {
-          const T xp = up[i], xq = uq[i];
-          up[i] = scal(xp, c) - sec * xq;
-          uq[i] = se * xp + scal(xq, c);
-        }
-        T* vp = V + (int64_t)p * n;
-        T* vq = V + (int64_t)q * n;
-        for (int i = lane; i < n; i += 32) {
-          const T xp = vp[i], xq = vq[i];
-          vp[i] = scal(xp, c) - sec * xq;
-          vq[i] = se * xp + scal(xq, c);
-        }
-        if (lane == 0) rotated = 1;
-      }
-      __syncthreads();
-    }
-    ++sweep;
-    converged = (rotated == 0);
-    __syncthreads();
-  }
-  // singular values, ranks (descending, stable), normalised outputs
-  for (int c = warp; c < n; c += nw) {
-    double s2 = 0.0;
-    for (int i = lane; i < m; i += 32) s2 += abs2(U[(int64_t)c * m + i]);
-    s2 = warp_sum(s2);
-    if (lane == 0) sig[c] = sqrt(s2);
-  }
-  __syncthreads();
-  for (int c = threadIdx.x; c < n; c += blockDim.x) {
-    int rk = 0;
-    for (int d = 0; d < n; ++d) rk += (sig[d] > sig[c]) || (sig[d] == sig[c] && d < c);
-    rank[c] = rk;
-    jb.S[rk] = sig[c];
-  }
-  __syncthreads();
-  T* Uo = (T*)jb.U;
-  T* Vo = (T*)jb.V;
-  for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) {
-    const int c = (int)(i / m), r = (int)(i % m);
-    const double s = sig[c];
-    Uo[(int64_t)r * n + rank[c]] = s > 0 ? scal(U[i], 1.0 / s) : from_real<T>(0.0);
-  }
-  for (int64_t i = threadIdx.x; i < (int64_t)n * n; i += blockDim.x) {
-    const int c = (int)(i / n), r = (int)(i % n);
-    Vo[(int64_t)r * n + rank[c]] = V[i];
-  }
-  if (threadIdx.x == 0 && jb.sweeps) *jb.sweeps = converged ? sweep : -1;
-}
-
-// The same Jacobi iteration spread over a thread-block cluster: the pairs of a
-// round are shared by the warps of all CTAs of the cluster, the columns live
-// in global memory (L2-resident; loads and stores bypass L1), and a cluster
-// barrier (release / acquire at cluster scope) separates the rounds.  The
-// convergence decision of a sweep is read by every CTA from one global flag
-// after the sweep's last barrier, so all CTAs leave the loop together; flag
-// k % 3 is cleared two sweeps before it is reused, after every CTA has read it.
+// One-sided (Hestenes) Jacobi: rotate column pairs (p, q) of U until every
+// pair is orthogonal to tol = 8 sqrt(m) eps relative to |u_p| |u_q|; the
+// singular values are the final column norms.  Round-robin pairing: the n/2
+// pairs of a round are disjoint, so the warps of a round run them in
+// parallel.  The columns live in global memory (L2-resident; loads and
+// stores bypass L1); with MAXR > 0 each lane keeps its MAXR elements of the
+// two columns in registers between the dot products and the rotation.
+//
+// CL: the job is spread over a thread-block cluster -- the warps of all its
+// CTAs share the pairs of a round and a cluster barrier (release / acquire at
+// cluster scope) separates the rounds.  The stop decision of a sweep is read
+// by every CTA from one global flag after the sweep's last barrier, so all
+// CTAs leave the loop together; flag k % 3 is cleared two sweeps before it is
+// reused, after every CTA has read it.
+//
+// A sweep ends the iteration when no pair had |g| > stop sqrt(a b) with
+// stop = max(tol, stop_rel): Jacobi converges quadratically near the end, so
+// after a sweep whose rotations were all below ~1e-10 the next one would
+// change nothing above rounding.
 template <class T> struct RealOf { using type = double; };
 template <> struct RealOf<float> { using type = float; };
 
@@ -497,19 +399,31 @@ __device__ inline float fmaT(float a, float b, float c) { return fmaf(a, b, c); 
 __device__ inline double fmaT(double a, double b, double c) { return fma(a, b, c); }
 __device__ inline cplx fmaT(cplx a, cplx b, cplx c) { return Sc<cplx>::fma(a, b, c); }
 
-template <class T>
-__global__ void __launch_bounds__(512) k_svd_cluster(const SvdJob* __restrict__ jobs, T* __restrict__ work,
-                                                     const int64_t* __restrict__ woff, int* __restrict__ flags,
-                                                     int max_sweeps, int init_v) {
+template <bool CL>
+__device__ inline void jsync() {
+  if constexpr (CL)
+    cg::this_cluster().sync();
+  else
+    __syncthreads();
+}
+
+template <class T, bool CL, int MAXR>
+__global__ void __launch_bounds__(512) k_jacobi(const SvdJob* __restrict__ jobs, T* __restrict__ work,
+                                                const int64_t* __restrict__ woff, int* __restrict__ flags,
+                                                int max_sweeps, double stop_rel) {
   using R = typename RealOf<T>::type;
-  cg::cluster_group cl = cg::this_cluster();
-  const int C = (int)cl.num_blocks(), crank = (int)cl.block_rank();
+  int C = 1, crank = 0;
+  if constexpr (CL) {
+    C = (int)cg::this_cluster().num_blocks();
+    crank = (int)cg::this_cluster().block_rank();
+  }
   const int ji = blockIdx.x / C;
   const SvdJob jb = jobs[ji];
   const int m = jb.m, n = jb.n;
-  T* U = work + woff[ji];
-  T* V = U + (int64_t)m * n;
-  double* sig = (double*)(V + (int64_t)n * n);
+  const bool want_v = jb.V != nullptr;
+  T* U = work + woff[ji];  // column-major m x n
+  T* V = U + (int64_t)m * n;  // column-major n x n (when wanted)
+  double* sig = (double*)(V + (want_v ? (int64_t)n * n : 0));
   int* rank = (int*)(sig + n);
   int* flag = flags + 3 * ji;
   const T* A = (const T*)jb.A;
@@ -519,26 +433,26 @@ __global__ void __launch_bounds__(512) k_svd_cluster(const SvdJob* __restrict__ 
     const int r = (int)(i / n), c = (int)(i % n);
     stcg(U + (int64_t)c * m + r, A[i]);
   }
-  // V starts as the identity, or (init_v) as jb.V given row-major
-  for (int64_t i = gt; i < (int64_t)n * n; i += gs) {
-    const int c = (int)(i / n), r = (int)(i % n);
-    stcg(V + i, init_v ? ((const T*)jb.V)[(int64_t)r * n + c] : from_real<T>(r == c ? 1.0 : 0.0));
-  }
+  if (want_v)
+    for (int64_t i = gt; i < (int64_t)n * n; i += gs)
+      stcg(V + i, from_real<T>((i / n) == (i % n) ? 1.0 : 0.0));
   __shared__ double red[32];
   double part = 0.0;
   for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) part += (double)abs2(A[i]);
   const double fro2 = block_sum<double>(part, red);
   const double eps = sizeof(R) == 4 ? 1.1920929e-7 : 2.220446049250313e-16;
+  // columns below this are rounding noise of the whole matrix
   const double negl = (sizeof(R) == 4 ? 1e-13 : 1e-30) * fro2;
   const R tol = (R)(8.0 * sqrt((double)m) * eps);
+  const R stop = (R)fmax((double)tol, stop_rel);
   const int n2 = (n + 1) & ~1;
   const int gw = crank * nw + warp, nwc = C * nw;
   int sweep = 0;
   bool converged = (n < 2);
-  cl.sync();
+  jsync<CL>();
   while (!converged && sweep < max_sweeps) {
     if (crank == 0 && threadIdx.x == 0) flag[(sweep + 1) % 3] = 0;
-    int rotated_here = 0;
+    int busy = 0;
     for (int r = 0; r < n2 - 1; ++r) {
       for (int slot = gw; slot < n2 / 2; slot += nwc) {
         int p, q;
@@ -548,55 +462,84 @@ __global__ void __launch_bounds__(512) k_svd_cluster(const SvdJob* __restrict__ 
         T* uq = U + (int64_t)q * m;
         R a = 0, b = 0;
         T g = from_real<T>(0.0);
-        for (int i = lane; i < m; i += 32) {
-          const T xp = ldcg(up + i), xq = ldcg(uq + i);
-          a += abs2(xp);
-          b += abs2(xq);
-          g = fmaT(conj(xp), xq, g);
+        T xp[MAXR > 0 ? MAXR : 1], xq[MAXR > 0 ? MAXR : 1];
+        if constexpr (MAXR > 0) {
+#pragma unroll
+          for (int k = 0; k < MAXR; ++k) {
+            const int i = lane + 32 * k;
+            xp[k] = i < m ? ldcg(up + i) : from_real<T>(0.0);
+            xq[k] = i < m ? ldcg(uq + i) : from_real<T>(0.0);
+            a += abs2(xp[k]);
+            b += abs2(xq[k]);
+            g = fmaT(conj(xp[k]), xq[k], g);
+          }
+        } else {
+          for (int i = lane; i < m; i += 32) {
+            const T x = ldcg(up + i), y = ldcg(uq + i);
+            a += abs2(x);
+            b += abs2(y);
+            g = fmaT(conj(x), y, g);
+          }
         }
         a = warp_sum(a);
         b = warp_sum(b);
         g = warp_sum(g);
         const R ag = sqrt(abs2(g));
-        if (ag <= tol * sqrt(a * b) || ag == (R)0 || (double)a < negl || (double)b < negl) continue;
+        // a negligible column carries no singular value worth orthogonalising
+        // against; skipping it also avoids zeta^2 overflow on extreme ratios
+        if ((double)a < negl || (double)b < negl) continue;
+        const R nab = sqrt(a) * sqrt(b);
+        if (ag > stop * nab) busy = 1;
+        if (ag <= tol * nab || ag == (R)0) continue;
         const R zeta = (b - a) / ((R)2 * ag);
         const R big = sizeof(R) == 4 ? (R)1e18 : (R)1e150;
         const R t = fabs(zeta) > big ? (R)0.5 / zeta
                                      : (zeta >= 0 ? (R)1 : (R)-1) / (fabs(zeta) + sqrt((R)1 + zeta * zeta));
         if (t == (R)0) continue;
         const R c = (R)1 / sqrt((R)1 + t * t), sn = c * t;
-        const T e = phase(g);
+        const T e = phase(g);  // g / |g|
         const T se = scal(e, sn), sec = scal(conj(e), sn);
-        for (int i = lane; i < m; i += 32) {
-          const T xp = ldcg(up + i), xq = ldcg(uq + i);
-          stcg(up + i, scal(xp, c) - sec * xq);
-          stcg(uq + i, se * xp + scal(xq, c));
+        if constexpr (MAXR > 0) {
+#pragma unroll
+          for (int k = 0; k < MAXR; ++k) {
+            const int i = lane + 32 * k;
+            if (i < m) {
+              stcg(up + i, scal(xp[k], c) - sec * xq[k]);
+              stcg(uq + i, se * xp[k] + scal(xq[k], c));
+            }
+          }
+        } else {
+          for (int i = lane; i < m; i += 32) {
+            const T x = ldcg(up + i), y = ldcg(uq + i);
+            stcg(up + i, scal(x, c) - sec * y);
+            stcg(uq + i, se * x + scal(y, c));
+          }
         }
-        T* vp = V + (int64_t)p * n;
-        T* vq = V + (int64_t)q * n;
-        for (int i = lane; i < n; i += 32) {
-          const T xp = ldcg(vp + i), xq = ldcg(vq + i);
-          stcg(vp + i, scal(xp, c) - sec * xq);
-          stcg(vq + i, se * xp + scal(xq, c));
+        if (want_v) {
+          T* vp = V + (int64_t)p * n;
+          T* vq = V + (int64_t)q * n;
+          for (int i = lane; i < n; i += 32) {
+            const T x = ldcg(vp + i), y = ldcg(vq + i);
+            stcg(vp + i, scal(x, c) - sec * y);
+            stcg(vq + i, se * x + scal(y, c));
+          }
         }
-        rotated_here = 1;
       }
-      cl.sync();
+      jsync<CL>();
     }
-    // (a flag store after the round's barrier would still precede the read
-    // below only through the next barrier, so it is stored before the last one)
-    if (rotated_here && lane == 0) atomicOr(flag + sweep % 3, 1);
-    cl.sync();
+    if (busy && lane == 0) atomicOr(flag + sweep % 3, 1);
+    jsync<CL>();
     converged = (__ldcg(flag + sweep % 3) == 0);
     ++sweep;
   }
+  // singular values, ranks (descending, stable), normalised outputs
   for (int c = gw; c < n; c += nwc) {
     double s2 = 0.0;
     for (int i = lane; i < m; i += 32) s2 += (double)abs2(ldcg(U + (int64_t)c * m + i));
     s2 = warp_sum(s2);
     if (lane == 0) __stcg(sig + c, sqrt(s2));
   }
-  cl.sync();
+  jsync<CL>();
   for (int64_t c = gt; c < n; c += gs) {
     const double sc = __ldcg(sig + c);
     int rk = 0;
@@ -607,17 +550,19 @@ __global__ void __launch_bounds__(512) k_svd_cluster(const SvdJob* __restrict__ 
     __stcg(rank + c, rk);
     jb.S[rk] = sc;
   }
-  cl.sync();
+  jsync<CL>();
   T* Uo = (T*)jb.U;
-  T* Vo = (T*)jb.V;
   for (int64_t i = gt; i < (int64_t)m * n; i += gs) {
     const int c = (int)(i / m), r = (int)(i % m);
     const double sc = __ldcg(sig + c);
     Uo[(int64_t)r * n + __ldcg(rank + c)] = sc > 0 ? scal(ldcg(U + i), (R)(1.0 / sc)) : from_real<T>(0.0);
   }
-  for (int64_t i = gt; i < (int64_t)n * n; i += gs) {
-    const int c = (int)(i / n), r = (int)(i % n);
-    Vo[(int64_t)r * n + __ldcg(rank + c)] = ldcg(V + i);
+  if (want_v) {
+    T* Vo = (T*)jb.V;
+    for (int64_t i = gt; i < (int64_t)n * n; i += gs) {
+      const int c = (int)(i / n), r = (int)(i % n);
+      Vo[(int64_t)r * n + __ldcg(rank + c)] = ldcg(V + i);
+    }
   }
   if (crank == 0 && threadIdx.x == 0 && jb.sweeps) *jb.sweeps = converged ? sweep : -1;
 }
@@ -628,9 +573,35 @@ constexpr int SVD_CLUSTER = 8;  // CTAs (SMs) per large matrix
 // pay for a cluster barrier per round.
 inline bool svd_big(const SvdJob& j) { return j.n >= 96 && (double)j.m * j.n * j.n >= 2.0e6; }
 
+template <class T, bool CL, int MAXR>
+void launch_jacobi(tnfa_ctx* ctx, const SvdJob* d, T* work, const int64_t* woff, int* flags, int njobs,
+                   int max_sweeps, double stop_rel) {
+  if constexpr (CL) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(njobs * SVD_CLUSTER));
+    cfg.blockDim = dim3(512);
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = SVD_CLUSTER;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    TNFA_CUDA(cudaLaunchKernelEx(&cfg, k_jacobi<T, true, MAXR>, d, work, woff, flags, max_sweeps, stop_rel));
+  } else {
+    k_jacobi<T, false, MAXR><<<(unsigned)njobs, 512, 0, ctx->stream>>>(d, work, woff, flags, max_sweeps,
+                                                                       stop_rel);
+  }
+  TNFA_LAUNCH_CHECK();
+}
+
+// Registers per lane and column kept by the Jacobi kernels (0: reload).
+template <class T> constexpr int jacobi_maxr() { return sizeof(T) == 16 ? 8 : 16; }
+
 template <class T>
-void launch_svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, bool init_v,
-                const char* family) {
+void jacobi(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, double stop_rel,
+            const char* family) {
   std::vector<SvdJob> big, small;
   for (const auto& j : jobs) (svd_big(j) ? big : small).push_back(j);
   for (int pass = 0; pass < 2; ++pass) {
@@ -638,49 +609,53 @@ void launch_svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, 
     if (js.empty()) continue;
     std::vector<int64_t> woff(js.size() + 1, 0);
     double fl = 0;
+    int maxm = 0;
     for (size_t i = 0; i < js.size(); ++i) {
       TNFA_CHECK(js[i].m >= js[i].n, TNFA_ERR_INVALID_ARGUMENT, "svd needs m >= n");
       const int64_t m = js[i].m, n = js[i].n;
-      // U, V in T; sig (n doubles) and rank (n ints) rounded up to T slots
-      woff[i + 1] = woff[i] + m * n + n * n + (int64_t)((n * 12 + sizeof(T) - 1) / sizeof(T)) + 2;
-      fl += 6.0 * m * n * n * 8;  // ~8 sweeps
+      maxm = std::max(maxm, js[i].m);
+      // U (and V) in T; sig (n doubles) and rank (n ints) rounded up to T slots
+      woff[i + 1] = woff[i] + m * n + (js[i].V ? n * n : 0) +
+                    (int64_t)((n * 12 + sizeof(T) - 1) / sizeof(T)) + 2;
+      fl += 5.0 * m * n * n * 8;  // ~8 sweeps of 3 dots + 2 rotations per pair
     }
     DBuf work(ctx, (size_t)woff.back() * sizeof(T));
     DBuf dw = upload(ctx, woff);
     DBuf d = upload(ctx, js);
+    DBuf flags(ctx, js.size() * 3 * sizeof(int));
+    TNFA_CUDA(cudaMemsetAsync(flags.p, 0, js.size() * 3 * sizeof(int), ctx->stream));
     KernelScope ks(ctx, family, fl, 0.0);
     if (trace_on()) ks.note = (pass == 0 ? "cluster " : "single ") + size_note(js);
+    const int need = (maxm + 31) / 32;  // column elements per lane
+    const SvdJob* dj = d.as<SvdJob>();
+    const int nj = (int)js.size();
+    T* w = work.as<T>();
+    const int64_t* wo = dw.as<int64_t>();
+    int* fl_ = flags.as<int>();
     if (pass == 0) {
-      DBuf flags(ctx, js.size() * 3 * sizeof(int));
-      TNFA_CUDA(cudaMemsetAsync(flags.p, 0, js.size() * 3 * sizeof(int), ctx->stream));
-      cudaLaunchConfig_t cfg{};
-      cfg.gridDim = dim3((unsigned)(js.size() * SVD_CLUSTER));
-      cfg.blockDim = dim3(512);
-      cfg.stream = ctx->stream;
-      cudaLaunchAttribute at[1];
-      at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = SVD_CLUSTER;
-      at[0].val.clusterDim.y = 1;
-      at[0].val.clusterDim.z = 1;
-      cfg.attrs = at;
-      cfg.numAttrs = 1;
-      TNFA_CUDA(cudaLaunchKernelEx(&cfg, k_svd_cluster<T>, (const SvdJob*)d.as<SvdJob>(), work.as<T>(),
-                                   (const int64_t*)dw.as<int64_t>(), flags.as<int>(), max_sweeps,
-                                   init_v ? 1 : 0));
+      if (need <= 4)
+        launch_jacobi<T, true, 4>(ctx, dj, w, wo, fl_, nj, max_sweeps, stop_rel);
+      else if (need <= jacobi_maxr<T>())
+        launch_jacobi<T, true, jacobi_maxr<T>()>(ctx, dj, w, wo, fl_, nj, max_sweeps, stop_rel);
+      else
+        launch_jacobi<T, true, 0>(ctx, dj, w, wo, fl_, nj, max_sweeps, stop_rel);
     } else {
-      TNFA_CHECK(!init_v, TNFA_ERR_UNSUPPORTED, "svd: initial V needs the cluster kernel");
-      k_svd<T><<<(unsigned)js.size(), 512, 0, ctx->stream>>>(d.as<SvdJob>(), work.as<T>(),
-                                                             dw.as<int64_t>(), max_sweeps);
+      if (need <= 4)
+        launch_jacobi<T, false, 4>(ctx, dj, w, wo, fl_, nj, max_sweeps, stop_rel);
+      else if (need <= jacobi_maxr<T>())
+        launch_jacobi<T, false, jacobi_maxr<T>()>(ctx, dj, w, wo, fl_, nj, max_sweeps, stop_rel);
+      else
+        launch_jacobi<T, false, 0>(ctx, dj, w, wo, fl_, nj, max_sweeps, stop_rel);
     }
-    TNFA_LAUNCH_CHECK();
   }
+  if (trace_on()) trace_sweeps(ctx, jobs);
 }
 
 template <class T>
 void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
   if (jobs.empty()) return;
-  launch_svd<T>(ctx, jobs, max_sweeps, false, sizeof(T) == 8 ? "svd_f64" : "svd_c128");
-  if (trace_on()) trace_sweeps(ctx, jobs);
+  jacobi<T>(ctx, jobs, max_sweeps, 1e-10,
+            sizeof(T) == 8 ? "svd_f64" : (sizeof(T) == 4 ? "svd_f32" : "svd_c128"));
   // Diagnostics: with TNFA_DEBUG_DIR set, the input of every SVD that hit the
   // sweep cap is written there (int32 m, int32 n, element size, then data).
   static const char* dbg = getenv("TNFA_DEBUG_DIR");
@@ -855,6 +830,186 @@ bool lu_solve(tnfa_ctx* ctx, double* A, double* b, int n) {
   return hs == 0;
 }
 
+// --------------------------------------------------------- factorise --
+// Batched block copy with element conversion: dst[(r, c) or (c, r)] =
+// conv(src[r * lds + c]), conjugated on request.
+struct CopyJob {
+  const void* src;
+  void* dst;
+  int rows, cols, lds, ldd;
+  int trans, conj;
+};
+
+__device__ inline double cvt(double x, double*) { return x; }
+__device__ inline float cvt(double x, float*) { return (float)x; }
+__device__ inline double cvt(float x, double*) { return (double)x; }
+__device__ inline cplx cvt(cplx x, cplx*) { return x; }
+
+template <class S, class D>
+__global__ void k_copy_block(const CopyJob* __restrict__ jobs) {
+  const CopyJob jb = jobs[blockIdx.y];
+  const S* src = (const S*)jb.src;
+  D* dst = (D*)jb.dst;
+  const int64_t n = (int64_t)jb.rows * jb.cols;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / jb.cols), c = (int)(i % jb.cols);
+    S v = src[(int64_t)r * jb.lds + c];
+    if (jb.conj) v = conj(v);
+    const int64_t o = jb.trans ? (int64_t)c * jb.ldd + r : (int64_t)r * jb.ldd + c;
+    dst[o] = cvt(v, (D*)nullptr);
+  }
+}
+
+template <class S, class D>
+void copy_blocks(tnfa_ctx* ctx, const std::vector<CopyJob>& jobs) {
+  if (jobs.empty()) return;
+  int64_t nmax = 1;
+  for (const auto& j : jobs) nmax = std::max<int64_t>(nmax, (int64_t)j.rows * j.cols);
+  TNFA_CHECK(jobs.size() <= 65535, TNFA_ERR_UNSUPPORTED, "more than 65535 copies in one batch");
+  DBuf d = upload(ctx, jobs);
+  k_copy_block<S, D><<<dim3(grid_for(nmax, 256, 1024), (unsigned)jobs.size()), 256, 0, ctx->stream>>>(
+      d.as<CopyJob>());
+  TNFA_LAUNCH_CHECK();
+}
+
+template <class T>
+void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cutoff, int maxdim,
+                  int mindim, int precision, std::vector<FactorResult>& out) {
+  const size_t nj = jobs.size();
+  out.clear();
+  out.resize(nj);
+  if (!nj) return;
+  constexpr bool real64 = std::is_same<T, double>::value;
+  const bool mixed = real64 && (precision == TNFA_PREC_MIXED || precision == TNFA_PREC_F32);
+  std::vector<char> tall(nj);
+  std::vector<int> n(nj);
+  std::vector<DBuf> Q(nj), R(nj), tau(nj), Mt(nj), J(nj), U(nj), S(nj), sw(nj);
+  // (1) the square core J
+  std::vector<CopyJob> adj;
+  std::vector<QrJob> qj;
+  for (size_t q = 0; q < nj; ++q) {
+    const FactorJob& f = jobs[q];
+    tall[q] = f.rows >= f.cols;
+    n[q] = std::min(f.rows, f.cols);
+    const int k = n[q];
+    R[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
+    tau[q] = DBuf(ctx, (size_t)k * sizeof(T));
+    if (tall[q]) {
+      Q[q] = DBuf(ctx, (size_t)f.rows * k * sizeof(T));
+      qj.push_back({f.M, Q[q].p, R[q].p, tau[q].p, f.rows, f.cols});
+    } else {
+      Mt[q] = DBuf(ctx, (size_t)f.rows * f.cols * sizeof(T));
+      adj.push_back({f.M, Mt[q].p, f.rows, f.cols, f.cols, f.rows, 1, 1});
+      Q[q] = DBuf(ctx, (size_t)f.cols * k * sizeof(T));
+      qj.push_back({Mt[q].p, Q[q].p, R[q].p, tau[q].p, f.cols, f.rows});
+    }
+  }
+  copy_blocks<T, T>(ctx, adj);
+  qr<T>(ctx, qj);
+  adj.clear();
+  for (size_t q = 0; q < nj; ++q) {
+    const int k = n[q];
+    if (!tall[q]) {
+      J[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
+      adj.push_back({R[q].p, J[q].p, k, k, k, k, 1, 1});
+    }
+    U[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
+    S[q] = DBuf(ctx, (size_t)k * sizeof(double));
+    sw[q] = DBuf(ctx, sizeof(int));
+  }
+  copy_blocks<T, T>(ctx, adj);
+  auto core = [&](size_t q) { return tall[q] ? R[q].p : J[q].p; };
+  // (2) Jacobi on the core
+  std::vector<SvdJob> sj;
+  if (!mixed) {
+    for (size_t q = 0; q < nj; ++q)
+      sj.push_back({core(q), U[q].p, S[q].as<double>(), nullptr, n[q], n[q], sw[q].as<int>()});
+    jacobi<T>(ctx, sj, 60, 1e-10, real64 ? "svd_f64" : "svd_c128");
+  } else {
+    std::vector<DBuf> J32(nj), U32(nj), V32(nj), S32(nj), sw32(nj), V(nj), G(nj), Y(nj), W(nj);
+    std::vector<CopyJob> down, up;
+    std::vector<SvdJob> s32;
+    for (size_t q = 0; q < nj; ++q) {
+      const int k = n[q];
+      J32[q] = DBuf(ctx, (size_t)k * k * sizeof(float));
+      U32[q] = DBuf(ctx, (size_t)k * k * sizeof(float));
+      V32[q] = DBuf(ctx, (size_t)k * k * sizeof(float));
+      S32[q] = DBuf(ctx, (size_t)k * sizeof(double));
+      sw32[q] = DBuf(ctx, sizeof(int));
+      down.push_back({core(q), J32[q].p, k, k, k, k, 0, 0});
+      s32.push_back({J32[q].p, U32[q].p, S32[q].as<double>(), V32[q].p, k, k, sw32[q].as<int>()});
+      V[q] = DBuf(ctx, (size_t)k * k * sizeof(double));
+      up.push_back({V32[q].p, V[q].p, k, k, k, k, 0, 0});
+    }
+    copy_blocks<double, float>(ctx, down);
+    jacobi<float>(ctx, s32, 60, 0.0, "svd_f32");
+    copy_blocks<float, double>(ctx, up);
+    // V <- V (3 I - V^T V) / 2, twice: orthonormal to rounding
+    for (int it = 0; it < 2; ++it) {
+      std::vector<GemmJob> g1, g2;
+      std::vector<CopyJob> cp;
+      for (size_t q = 0; q < nj; ++q) {
+        const int k = n[q];
+        G[q] = DBuf(ctx, (size_t)k * k * sizeof(double));
+        Y[q] = DBuf(ctx, (size_t)k * k * sizeof(double));
+        g1.push_back({V[q].p, V[q].p, G[q].p, k, k, k, k, k, k, 1, 0, 1.0, 0.0});
+        cp.push_back({V[q].p, Y[q].p, k, k, k, k, 0, 0});
+        g2.push_back({V[q].p, G[q].p, Y[q].p, k, k, k, k, k, k, 0, 0, -0.5, 1.5});
+      }
+      gemm<double>(ctx, g1);
+      copy_blocks<double, double>(ctx, cp);
+      gemm<double>(ctx, g2);
+      for (size_t q = 0; q < nj; ++q) std::swap(V[q], Y[q]);
+    }
+    std::vector<GemmJob> gw;
+    for (size_t q = 0; q < nj; ++q) {
+      const int k = n[q];
+      W[q] = DBuf(ctx, (size_t)k * k * sizeof(double));
+      gw.push_back({core(q), V[q].p, W[q].p, k, k, k, k, k, k, 0, 0, 1.0, 0.0});
+    }
+    gemm<double>(ctx, gw);
+    for (size_t q = 0; q < nj; ++q)
+      sj.push_back({W[q].p, U[q].p, S[q].as<double>(), nullptr, n[q], n[q], sw[q].as<int>()});
+    jacobi<T>(ctx, sj, 60, 1e-10, "svd_polish_f64");
+  }
+  // (3) ranks on the host
+  for (size_t q = 0; q < nj; ++q) {
+    out[q].s.resize(n[q]);
+    TNFA_CUDA(cudaMemcpyAsync(out[q].s.data(), S[q].p, n[q] * sizeof(double), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    TNFA_CUDA(cudaMemcpyAsync(&out[q].sweeps, sw[q].p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<GemmJob> gl, gx;
+  std::vector<CopyJob> cl;
+  for (size_t q = 0; q < nj; ++q) {
+    FactorResult& o = out[q];
+    const FactorJob& f = jobs[q];
+    const int k = n[q];
+    const int r = truncation_rank(o.s.data(), k, cutoff, maxdim, mindim);
+    o.r = r;
+    double tot = 0, drop = 0;
+    for (int i = 0; i < k; ++i) {
+      tot += o.s[i] * o.s[i];
+      if (i >= r) drop += o.s[i] * o.s[i];
+    }
+    o.discarded = tot > 0 ? drop / tot : 0.0;
+    o.L = DBuf(ctx, (size_t)f.rows * r * sizeof(T));
+    o.X = DBuf(ctx, (size_t)r * f.cols * sizeof(T));
+    if (tall[q]) {
+      gl.push_back({Q[q].p, U[q].p, o.L.p, f.rows, r, k, k, k, r, 0, 0, 1.0, 0.0});
+      gx.push_back({U[q].p, R[q].p, o.X.p, r, f.cols, k, k, f.cols, f.cols, 2, 0, 1.0, 0.0});
+    } else {
+      cl.push_back({U[q].p, o.L.p, k, r, k, r, 0, 0});
+      gx.push_back({U[q].p, f.M, o.X.p, r, f.cols, k, k, f.cols, f.cols, 2, 0, 1.0, 0.0});
+    }
+  }
+  gemm<T>(ctx, gl);
+  copy_blocks<T, T>(ctx, cl);
+  gemm<T>(ctx, gx);
+}
+
 int truncation_rank(const double* s, int n, double cutoff, int maxdim, int mindim) {
   if (n <= 0) return 0;
   double total = 0.0;
@@ -881,6 +1036,11 @@ template void qr<double>(tnfa_ctx*, const std::vector<QrJob>&);
 template void qr<cplx>(tnfa_ctx*, const std::vector<QrJob>&);
 template void svd<double>(tnfa_ctx*, const std::vector<SvdJob>&, int);
 template void svd<cplx>(tnfa_ctx*, const std::vector<SvdJob>&, int);
+template void svd<float>(tnfa_ctx*, const std::vector<SvdJob>&, int);
+template void trunc_factor<double>(tnfa_ctx*, const std::vector<FactorJob>&, double, int, int, int,
+                                   std::vector<FactorResult>&);
+template void trunc_factor<cplx>(tnfa_ctx*, const std::vector<FactorJob>&, double, int, int, int,
+                                 std::vector<FactorResult>&);
 
 }  // namespace la
 }  // namespace tnfa

@@ -67,6 +67,30 @@ void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps = 60);
 // then forward / back substitution.  Returns false if a pivot is exactly 0.
 bool lu_solve(tnfa_ctx* ctx, double* A, double* b, int n);
 
+// Truncated factorisation of bond matrices, the SVD step of truncation:
+// M (rows x cols, row-major; overwritten) ~= L X with L (rows x r) having
+// orthonormal columns and X (r x cols), r = truncation_rank of M's singular
+// values.  The square core J (R of M = QR when rows >= cols, else R^H of
+// M^H = QR) is diagonalised by one-sided Jacobi without accumulating V:
+// L = Q U_r (or U_r) and X = U_r^H R (or U_r^H M).  precision MIXED / F32
+// (real FP64 only): Jacobi first runs in FP32 with V accumulated, V is
+// re-orthonormalised in FP64 (two Newton-Schulz steps), and FP64 Jacobi on
+// J V polishes U and the singular values to FP64 accuracy in a few sweeps.
+struct FactorJob {
+  void* M;
+  int rows, cols;
+};
+struct FactorResult {
+  DBuf L, X;
+  int r = 0;
+  double discarded = 0.0;  // relative discarded weight
+  int sweeps = 0;          // FP64 Jacobi sweeps; -1: the sweep cap was hit
+  std::vector<double> s;   // singular values, descending
+};
+template <class T>
+void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cutoff, int maxdim,
+                  int mindim, int precision, std::vector<FactorResult>& out);
+
 // Rank kept by the reference truncation rule: smallest r >= mindim with
 // sum_{i >= r} s_i^2 <= cutoff * sum s_i^2, capped by maxdim (> 0).
 int truncation_rank(const double* s, int n, double cutoff, int maxdim, int mindim);

@@ -32,29 +32,6 @@ inline double habs2(cplx x) { return x.re * x.re + x.im * x.im; }
 template <class T> inline T hreal(double a);
 template <> inline double hreal<double>(double a) { return a; }
 template <> inline cplx hreal<cplx>(double a) { return {a, 0.0}; }
-__device__ inline double dconj(double x) { return x; }
-__device__ inline cplx dconj(cplx x) { return {x.re, -x.im}; }
-
-template <class T>
-__global__ void k_copy2d(T* __restrict__ dst, int ldd, const T* __restrict__ src, int lds,
-                         int rows, int cols, int conjugate) {
-  const int64_t n = (int64_t)rows * cols;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = i / cols, c = i % cols;
-    T v = src[r * lds + c];
-    dst[r * ldd + c] = conjugate ? dconj(v) : v;
-  }
-}
-
-template <class T>
-void copy2d(tnfa_ctx* ctx, void* dst, int ldd, const void* src, int lds, int rows, int cols,
-            bool conjugate) {
-  k_copy2d<T><<<grid_for((int64_t)rows * cols, 256, 4096), 256, 0, ctx->stream>>>(
-      (T*)dst, ldd, (const T*)src, lds, rows, cols, conjugate ? 1 : 0);
-  TNFA_LAUNCH_CHECK();
-}
-
 __device__ inline double dmul(double x, double s) { return x * s; }
 __device__ inline cplx dmul(cplx x, double s) { return {x.re * s, x.im * s}; }
 
@@ -244,69 +221,21 @@ void split_bond(Work<T>& w, int v, int c, const tnfa_trunc_params& prm, TruncSta
   const int rows = (int)rows64;
   DBuf M(ctx, (size_t)w.size(v) * sizeof(T));
   move_axis<T>(ctx, w.t[v].p, M.p, shp, ax, (int)shp.size() - 1);  // [rows][cols]
-  const bool tall = rows >= cols;
-  const int n = tall ? cols : rows;  // number of singular values
-  DBuf S(ctx, (size_t)n * sizeof(double)), sw(ctx, sizeof(int));
-  DBuf U, Vm, left;
-  if (tall) {
-    // M = Q R, R = U S V^H  =>  left = Q U, right = S V^H
-    DBuf Q(ctx, (size_t)rows * cols * sizeof(T)), R(ctx, (size_t)cols * cols * sizeof(T));
-    DBuf tau(ctx, (size_t)cols * sizeof(T));
-    la::qr<T>(ctx, {la::QrJob{M.p, Q.p, R.p, tau.p, rows, cols}});
-    U = DBuf(ctx, (size_t)n * n * sizeof(T));
-    Vm = DBuf(ctx, (size_t)n * n * sizeof(T));
-    la::svd<T>(ctx, {la::SvdJob{R.p, U.p, S.as<double>(), Vm.p, n, n, sw.as<int>()}});
-    left = DBuf(ctx, (size_t)rows * n * sizeof(T));
-    la::gemm<T>(ctx, {la::GemmJob{Q.p, U.p, left.p, rows, n, n, n, n, n, 0, 0, 1.0, 0.0}});
-  } else {
-    // M^T = U S V^H  =>  M = conj(V) S U^T : left = conj(V), right = S U^T
-    DBuf MT(ctx, (size_t)rows * cols * sizeof(T));
-    move_axis<T>(ctx, M.p, MT.p, {rows, cols}, 1, 0);
-    U = DBuf(ctx, (size_t)cols * n * sizeof(T));
-    Vm = DBuf(ctx, (size_t)n * n * sizeof(T));
-    la::svd<T>(ctx, {la::SvdJob{MT.p, U.p, S.as<double>(), Vm.p, cols, n, sw.as<int>()}});
-  }
-  std::vector<double> s(n);
-  int sweeps = 0;
-  TNFA_CUDA(cudaMemcpyAsync(s.data(), S.p, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  TNFA_CUDA(cudaMemcpyAsync(&sweeps, sw.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (sweeps < 0) st.nonconv = true;
-  st.max_sweeps = std::max(st.max_sweeps, sweeps);
-  const int r = la::truncation_rank(s.data(), n, prm.cutoff, prm.maxdim, prm.mindim);
-  double tot = 0, drop = 0;
-  for (int i = 0; i < n; ++i) {
-    tot += s[i] * s[i];
-    if (i >= r) drop += s[i] * s[i];
-  }
-  if (tot > 0) st.max_discarded = std::max(st.max_discarded, drop / tot);
-  // diag(s[:r]) on the device
-  DBuf sd(ctx, (size_t)r * r * sizeof(T));
-  {
-    std::vector<T> diag((size_t)r * r, hreal<T>(0.0));
-    for (int i = 0; i < r; ++i) diag[(size_t)i * r + i] = hreal<T>(s[i]);
-    TNFA_CUDA(cudaMemcpyAsync(sd.p, diag.data(), diag.size() * sizeof(T), cudaMemcpyHostToDevice,
-                              ctx->stream));
-    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
-  }
-  DBuf newv(ctx, (size_t)rows * r * sizeof(T));
-  DBuf X(ctx, (size_t)r * cols * sizeof(T));
-  if (tall) {
-    copy2d<T>(ctx, newv.p, r, left.p, n, rows, r, false);
-    // X[i][j] = s_i conj(V[j][i])
-    la::gemm<T>(ctx, {la::GemmJob{sd.p, Vm.p, X.p, r, cols, r, r, n, cols, 0, 2, 1.0, 0.0}});
-  } else {
-    copy2d<T>(ctx, newv.p, r, Vm.p, n, rows, r, true);
-    // X[i][j] = s_i U[j][i]
-    la::gemm<T>(ctx, {la::GemmJob{sd.p, U.p, X.p, r, cols, r, r, n, cols, 0, 1, 1.0, 0.0}});
-  }
+  std::vector<la::FactorResult> res;
+  la::trunc_factor<T>(ctx, {la::FactorJob{M.p, rows, cols}}, prm.cutoff, prm.maxdim, prm.mindim,
+                      prm.precision, res);
+  la::FactorResult& o = res[0];
+  if (o.sweeps < 0) st.nonconv = true;
+  st.max_sweeps = std::max(st.max_sweeps, o.sweeps);
+  st.max_discarded = std::max(st.max_discarded, o.discarded);
+  const int r = o.r;
   std::vector<int> nshp = shp;
   nshp.erase(nshp.begin() + ax);
   nshp.push_back(r);
   DBuf back(ctx, (size_t)rows * r * sizeof(T));
-  move_axis<T>(ctx, newv.p, back.p, nshp, (int)nshp.size() - 1, ax);
+  move_axis<T>(ctx, o.L.p, back.p, nshp, (int)nshp.size() - 1, ax);
   w.t[v] = std::move(back);
-  absorb(w, c, 1, X.p, r);
+  absorb(w, c, 1, o.X.p, r);
   w.topo.link[c] = r;
 }
 
@@ -799,11 +728,11 @@ void truncate_paths_batched(std::vector<Work<T>>& W, const tnfa_trunc_params& pr
     for (int i = 0; i < (int)W.size(); ++i)
       if (t + 1 < W[i].topo.V) sl.push_back({i, t});
     const size_t n = sl.size();
-    std::vector<DBuf> M(n), Qb(n), Rb(n), taub(n), Ub(n), Sb(n), Vb(n), left(n), MT(n), sw(n);
-    std::vector<int> rows(n), cols(n), nsv(n);
-    std::vector<char> tall(n);
+    std::vector<DBuf> M(n), back(n);
+    std::vector<int> rows(n), cols(n), r(n);
     std::vector<std::vector<int>> shp(n);
     std::vector<MoveJob> mv;
+    std::vector<la::FactorJob> fj;
     for (size_t q = 0; q < n; ++q) {
       Work<T>& w = W[sl[q].net];
       const int v = sl[q].v;
@@ -812,93 +741,22 @@ void truncate_paths_batched(std::vector<Work<T>>& W, const tnfa_trunc_params& pr
       const int64_t r64 = w.size(v) / cols[q];
       TNFA_CHECK(r64 < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "matrix too large");
       rows[q] = (int)r64;
-      tall[q] = rows[q] >= cols[q];
-      nsv[q] = tall[q] ? cols[q] : rows[q];
       M[q] = DBuf(ctx, (size_t)w.size(v) * sizeof(T));
       mv.push_back({w.t[v].p, M[q].p, shp[q], 2, (int)shp[q].size() - 1});
-      Sb[q] = DBuf(ctx, (size_t)nsv[q] * sizeof(double));
-      sw[q] = DBuf(ctx, sizeof(int));
+      fj.push_back({M[q].p, rows[q], cols[q]});
     }
     move_axes<T>(ctx, mv);
-    std::vector<la::QrJob> qj;
-    std::vector<MoveJob> tj;
-    for (size_t q = 0; q < n; ++q) {
-      if (tall[q]) {
-        Qb[q] = DBuf(ctx, (size_t)rows[q] * cols[q] * sizeof(T));
-        Rb[q] = DBuf(ctx, (size_t)cols[q] * cols[q] * sizeof(T));
-        taub[q] = DBuf(ctx, (size_t)cols[q] * sizeof(T));
-        qj.push_back({M[q].p, Qb[q].p, Rb[q].p, taub[q].p, rows[q], cols[q]});
-      } else {
-        MT[q] = DBuf(ctx, (size_t)rows[q] * cols[q] * sizeof(T));
-        tj.push_back({M[q].p, MT[q].p, {rows[q], cols[q]}, 1, 0});
-      }
-    }
-    la::qr<T>(ctx, qj);
-    move_axes<T>(ctx, tj);
-    std::vector<la::SvdJob> sj;
-    for (size_t q = 0; q < n; ++q) {
-      const int k = nsv[q];
-      Vb[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
-      if (tall[q]) {
-        Ub[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
-        sj.push_back({Rb[q].p, Ub[q].p, Sb[q].as<double>(), Vb[q].p, k, k, sw[q].as<int>()});
-      } else {
-        Ub[q] = DBuf(ctx, (size_t)cols[q] * k * sizeof(T));
-        sj.push_back({MT[q].p, Ub[q].p, Sb[q].as<double>(), Vb[q].p, cols[q], k, sw[q].as<int>()});
-      }
-    }
-    la::svd<T>(ctx, sj);
-    std::vector<la::GemmJob> gl;
-    for (size_t q = 0; q < n; ++q)
-      if (tall[q]) {
-        left[q] = DBuf(ctx, (size_t)rows[q] * nsv[q] * sizeof(T));
-        gl.push_back({Qb[q].p, Ub[q].p, left[q].p, rows[q], nsv[q], nsv[q], nsv[q], nsv[q], nsv[q],
-                      0, 0, 1.0, 0.0});
-      }
-    la::gemm<T>(ctx, gl);
-    // singular values of the whole step to the host
-    std::vector<std::vector<double>> sv(n);
-    std::vector<int> sweeps(n);
-    for (size_t q = 0; q < n; ++q) {
-      sv[q].resize(nsv[q]);
-      TNFA_CUDA(cudaMemcpyAsync(sv[q].data(), Sb[q].p, nsv[q] * sizeof(double),
-                                cudaMemcpyDeviceToHost, ctx->stream));
-      TNFA_CUDA(cudaMemcpyAsync(&sweeps[q], sw[q].p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    }
-    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
-    std::vector<int> r(n);
-    std::vector<DBuf> sd(n), X(n), newv(n), back(n);
-    std::vector<la::GemmJob> gx;
-    for (size_t q = 0; q < n; ++q) {
-      TNFA_CHECK(sweeps[q] >= 0, TNFA_ERR_NOT_CONVERGED, "Jacobi SVD hit its sweep cap");
-      r[q] = la::truncation_rank(sv[q].data(), nsv[q], prm.cutoff, prm.maxdim, prm.mindim);
-      std::vector<T> diag((size_t)r[q] * r[q], hreal<T>(0.0));
-      for (int i = 0; i < r[q]; ++i) diag[(size_t)i * r[q] + i] = hreal<T>(sv[q][i]);
-      sd[q] = DBuf(ctx, diag.size() * sizeof(T));
-      TNFA_CUDA(cudaMemcpyAsync(sd[q].p, diag.data(), diag.size() * sizeof(T), cudaMemcpyHostToDevice,
-                                ctx->stream));
-      X[q] = DBuf(ctx, (size_t)r[q] * cols[q] * sizeof(T));
-      newv[q] = DBuf(ctx, (size_t)rows[q] * r[q] * sizeof(T));
-      if (tall[q]) {
-        copy2d<T>(ctx, newv[q].p, r[q], left[q].p, nsv[q], rows[q], r[q], false);
-        gx.push_back({sd[q].p, Vb[q].p, X[q].p, r[q], cols[q], r[q], r[q], nsv[q], cols[q], 0, 2,
-                      1.0, 0.0});
-      } else {
-        copy2d<T>(ctx, newv[q].p, r[q], Vb[q].p, nsv[q], rows[q], r[q], true);
-        gx.push_back({sd[q].p, Ub[q].p, X[q].p, r[q], cols[q], r[q], r[q], nsv[q], cols[q], 0, 1,
-                      1.0, 0.0});
-      }
-    }
-    // the host staging vectors of diag() must outlive the async copies
-    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
-    la::gemm<T>(ctx, gx);
+    std::vector<la::FactorResult> res;
+    la::trunc_factor<T>(ctx, fj, prm.cutoff, prm.maxdim, prm.mindim, prm.precision, res);
     mv.clear();
     for (size_t q = 0; q < n; ++q) {
+      TNFA_CHECK(res[q].sweeps >= 0, TNFA_ERR_NOT_CONVERGED, "Jacobi SVD hit its sweep cap");
+      r[q] = res[q].r;
       std::vector<int> nshp = shp[q];
       nshp.erase(nshp.begin() + 2);
       nshp.push_back(r[q]);
       back[q] = DBuf(ctx, (size_t)rows[q] * r[q] * sizeof(T));
-      mv.push_back({newv[q].p, back[q].p, nshp, (int)nshp.size() - 1, 2});
+      mv.push_back({res[q].L.p, back[q].p, nshp, (int)nshp.size() - 1, 2});
     }
     move_axes<T>(ctx, mv);
     std::vector<BSlot> cs;
@@ -908,7 +766,7 @@ void truncate_paths_batched(std::vector<Work<T>>& W, const tnfa_trunc_params& pr
       W[sl[q].net].t[sl[q].v] = std::move(back[q]);
       cs.push_back({sl[q].net, sl[q].v + 1});
       ax.push_back(1);
-      Ms.push_back(X[q].p);
+      Ms.push_back(res[q].X.p);
     }
     absorb_batched(W, cs, ax, Ms, r);
     for (size_t q = 0; q < n; ++q) W[sl[q].net].topo.link[sl[q].v + 1] = r[q];
