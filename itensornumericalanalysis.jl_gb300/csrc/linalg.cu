@@ -204,6 +204,21 @@ std::string size_note(const std::vector<Job>& jobs) {
   return b;
 }
 
+// Loads and stores that bypass L1 (data shared between the CTAs of a
+// cluster through L2).
+__device__ inline double ldcg(const double* p) { return __ldcg(p); }
+__device__ inline float ldcg(const float* p) { return __ldcg(p); }
+__device__ inline cplx ldcg(const cplx* p) {
+  const double2 v = __ldcg((const double2*)p);
+  return {v.x, v.y};
+}
+__device__ inline void stcg(double* p, double v) { __stcg(p, v); }
+__device__ inline void stcg(float* p, float v) { __stcg(p, v); }
+__device__ inline void stcg(cplx* p, cplx v) { __stcg((double2*)p, make_double2(v.re, v.im)); }
+__device__ inline float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ inline double fmaT(double a, double b, double c) { return fma(a, b, c); }
+__device__ inline cplx fmaT(cplx a, cplx b, cplx c) { return Sc<cplx>::fma(a, b, c); }
+
 // ------------------------------------------------------------------ qr --
 template <class T>
 __device__ inline T block_sum(T v, T* red) {
@@ -225,111 +240,158 @@ __device__ inline T block_sum(T v, T* red) {
 
 // Workspace per job: A copied column-major into W (m*n), Q column-major
 // into Qw (m*kq); reflector j is stored in W column j rows j..m-1.
-template <class T>
+//
+// Columns are dealt round-robin to the CTAs of a cluster (CL; one CTA
+// otherwise): the owner of column j builds reflector j in place, a barrier
+// publishes it, and every CTA applies it to the columns it owns; Q is then
+// formed column by column by the owners without further barriers.
+template <bool CL>
+__device__ inline void qsync() {
+  if constexpr (CL)
+    cg::this_cluster().sync();
+  else
+    __syncthreads();
+}
+
+template <class T, bool CL>
 __global__ void __launch_bounds__(512) k_qr(const QrJob* __restrict__ jobs, T* __restrict__ work,
                                             const int64_t* __restrict__ woff) {
-  const QrJob jb = jobs[blockIdx.x];
+  int C = 1, crank = 0;
+  if constexpr (CL) {
+    C = (int)cg::this_cluster().num_blocks();
+    crank = (int)cg::this_cluster().block_rank();
+  }
+  const int ji = blockIdx.x / C;
+  const QrJob jb = jobs[ji];
   const int m = jb.m, n = jb.n, kq = min(m, n);
-  T* W = work + woff[blockIdx.x];
+  T* W = work + woff[ji];
   T* Qw = W + (int64_t)m * n;
+  T* alpha_g = Qw + (int64_t)m * kq;  // kq diagonal entries of R
   T* tau = (T*)jb.tau;
   const T* A = (const T*)jb.A;
   __shared__ T red[32];
-  __shared__ T alpha_sh;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) {
     const int r = (int)(i / n), c = (int)(i % n);
-    W[(int64_t)c * m + r] = A[i];
+    if (c % C == crank) W[(int64_t)c * m + r] = A[i];
   }
   __syncthreads();
   T* R = (T*)jb.R;
   for (int j = 0; j < kq; ++j) {
     T* x = W + (int64_t)j * m;
-    double part = 0.0;
-    for (int r = j + threadIdx.x; r < m; r += blockDim.x) part += abs2(x[r]);
-    const double nrm2 = re(block_sum<T>(from_real<T>(part), red));
-    if (threadIdx.x == 0) {
-      const T x0 = x[j];
-      const double nrm = sqrt(nrm2);
-      if (!(nrm > 1e-150)) {
-        // an (almost) eliminated column: no reflection.  A residue this small
-        // (rounding left by earlier steps) would make 2 / |v|^2 overflow.
-        tau[j] = from_real<T>(0.0);
-        alpha_sh = x0;
-      } else {
-        const T alpha = scal(phase(x0), -nrm);
-        const T v0 = x0 - alpha;
-        const double vn2 = nrm2 - abs2(x0) + abs2(v0);
-        tau[j] = from_real<T>(vn2 > 0.0 ? 2.0 / vn2 : 0.0);
-        x[j] = v0;
-        alpha_sh = alpha;
+    if (j % C == crank) {
+      double part = 0.0;
+      for (int r = j + threadIdx.x; r < m; r += blockDim.x) part += abs2(x[r]);
+      const double nrm2 = re(block_sum<T>(from_real<T>(part), red));
+      if (threadIdx.x == 0) {
+        const T x0 = x[j];
+        const double nrm = sqrt(nrm2);
+        if (!(nrm > 1e-150)) {
+          // an (almost) eliminated column: no reflection.  A residue this
+          // small (rounding left by earlier steps) would make 2 / |v|^2 overflow.
+          stcg(tau + j, from_real<T>(0.0));
+          stcg(alpha_g + j, x0);
+        } else {
+          const T alpha = scal(phase(x0), -nrm);
+          const T v0 = x0 - alpha;
+          const double vn2 = nrm2 - abs2(x0) + abs2(v0);
+          stcg(tau + j, from_real<T>(vn2 > 0.0 ? 2.0 / vn2 : 0.0));
+          stcg(x + j, v0);
+          stcg(alpha_g + j, alpha);
+        }
       }
     }
-    __syncthreads();
-    const double beta = re(tau[j]);
-    const T alpha = alpha_sh;
+    qsync<CL>();
+    const double beta = re(ldcg(tau + j));
     if (beta != 0.0) {
-      for (int c = j + 1 + warp; c < n; c += nw) {
+      // this CTA's columns c > j: c = crank + C * k
+      const int c0 = j + 1 + ((crank - (j + 1)) % C + C) % C;
+      for (int c = c0 + C * warp; c < n; c += C * nw) {
         T* y = W + (int64_t)c * m;
         T w = from_real<T>(0.0);
-        for (int r = j + lane; r < m; r += 32) w = Sc<T>::fma(conj(x[r]), y[r], w);
+        for (int r = j + lane; r < m; r += 32) w = Sc<T>::fma(conj(ldcg(x + r)), y[r], w);
         w = warp_sum(w);
         const T bw = scal(w, beta);
-        for (int r = j + lane; r < m; r += 32) y[r] = y[r] - x[r] * bw;
+        for (int r = j + lane; r < m; r += 32) y[r] = y[r] - ldcg(x + r) * bw;
       }
     }
     __syncthreads();
-    // R row j: diagonal alpha, then the updated row j of the trailing block
-    for (int c = threadIdx.x; c < n; c += blockDim.x)
-      R[(int64_t)j * n + c] = c < j ? from_real<T>(0.0) : (c == j ? alpha : W[(int64_t)c * m + j]);
-    __syncthreads();
+    // R row j: diagonal alpha, then the updated row j of this CTA's columns
+    for (int c = crank + C * threadIdx.x; c < n; c += C * blockDim.x)
+      R[(int64_t)j * n + c] = c < j ? from_real<T>(0.0) : (c == j ? ldcg(alpha_g + j) : W[(int64_t)c * m + j]);
   }
-  // Q = H_0 ... H_{kq-1} [I; 0]
-  for (int64_t i = threadIdx.x; i < (int64_t)m * kq; i += blockDim.x) {
-    const int c = (int)(i / m), r = (int)(i % m);
-    Qw[i] = from_real<T>(r == c ? 1.0 : 0.0);
+  // Q = H_0 ... H_{kq-1} [I; 0], columns owned as above
+  for (int c = crank + C * warp; c < kq; c += C * nw) {
+    T* y = Qw + (int64_t)c * m;
+    for (int r = lane; r < m; r += 32) y[r] = from_real<T>(r == c ? 1.0 : 0.0);
   }
   __syncthreads();
   for (int j = kq - 1; j >= 0; --j) {
-    const double beta = re(tau[j]);
-    if (beta != 0.0) {
-      const T* x = W + (int64_t)j * m;
-      for (int c = j + warp; c < kq; c += nw) {
-        T* y = Qw + (int64_t)c * m;
-        T w = from_real<T>(0.0);
-        for (int r = j + lane; r < m; r += 32) w = Sc<T>::fma(conj(x[r]), y[r], w);
-        w = warp_sum(w);
-        const T bw = scal(w, beta);
-        for (int r = j + lane; r < m; r += 32) y[r] = y[r] - x[r] * bw;
-      }
+    const double beta = re(ldcg(tau + j));
+    if (beta == 0.0) continue;
+    const T* x = W + (int64_t)j * m;
+    const int c0 = j + ((crank - j) % C + C) % C;
+    for (int c = c0 + C * warp; c < kq; c += C * nw) {
+      T* y = Qw + (int64_t)c * m;
+      T w = from_real<T>(0.0);
+      for (int r = j + lane; r < m; r += 32) w = Sc<T>::fma(conj(ldcg(x + r)), y[r], w);
+      w = warp_sum(w);
+      const T bw = scal(w, beta);
+      for (int r = j + lane; r < m; r += 32) y[r] = y[r] - ldcg(x + r) * bw;
     }
-    __syncthreads();
   }
+  __syncthreads();
   T* Q = (T*)jb.Q;
   for (int64_t i = threadIdx.x; i < (int64_t)m * kq; i += blockDim.x) {
     const int r = (int)(i / kq), c = (int)(i % kq);
-    Q[i] = Qw[(int64_t)c * m + r];
+    if (c % C == crank) Q[i] = Qw[(int64_t)c * m + r];
   }
 }
+
+constexpr int QR_CLUSTER = 8;
 
 template <class T>
 void qr(tnfa_ctx* ctx, const std::vector<QrJob>& jobs) {
   if (jobs.empty()) return;
-  std::vector<int64_t> woff(jobs.size() + 1, 0);
-  double fl = 0;
-  for (size_t i = 0; i < jobs.size(); ++i) {
-    const int64_t m = jobs[i].m, n = jobs[i].n, k = std::min(m, n);
-    woff[i + 1] = woff[i] + m * n + m * k;
-    fl += 4.0 * m * n * k;
+  std::vector<QrJob> big, small;
+  for (const auto& j : jobs)
+    ((double)j.m * j.n * std::min(j.m, j.n) >= 4.0e6 && std::min(j.m, j.n) >= 64 ? big : small).push_back(j);
+  for (int pass = 0; pass < 2; ++pass) {
+    const std::vector<QrJob>& js = pass == 0 ? big : small;
+    if (js.empty()) continue;
+    std::vector<int64_t> woff(js.size() + 1, 0);
+    double fl = 0;
+    for (size_t i = 0; i < js.size(); ++i) {
+      const int64_t m = js[i].m, n = js[i].n, k = std::min(m, n);
+      // W, Qw, the k diagonal entries of R
+      woff[i + 1] = woff[i] + m * n + m * k + k;
+      fl += 4.0 * m * n * k;
+    }
+    DBuf work(ctx, (size_t)woff.back() * sizeof(T));
+    DBuf dw = upload(ctx, woff);
+    DBuf d = upload(ctx, js);
+    KernelScope ks(ctx, sizeof(T) == 8 ? "qr_f64" : "qr_c128", fl, 0.0);
+    if (trace_on()) ks.note = (pass == 0 ? "cluster " : "single ") + size_note(js);
+    if (pass == 0) {
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3((unsigned)(js.size() * QR_CLUSTER));
+      cfg.blockDim = dim3(512);
+      cfg.stream = ctx->stream;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = QR_CLUSTER;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      TNFA_CUDA(cudaLaunchKernelEx(&cfg, k_qr<T, true>, (const QrJob*)d.as<QrJob>(), work.as<T>(),
+                                   (const int64_t*)dw.as<int64_t>()));
+    } else {
+      k_qr<T, false><<<(unsigned)js.size(), 512, 0, ctx->stream>>>(d.as<QrJob>(), work.as<T>(),
+                                                                  dw.as<int64_t>());
+    }
+    TNFA_LAUNCH_CHECK();
   }
-  DBuf work(ctx, (size_t)woff.back() * sizeof(T));
-  DBuf dw = upload(ctx, woff);
-  DBuf d = upload(ctx, jobs);
-  KernelScope ks(ctx, sizeof(T) == 8 ? "qr_f64" : "qr_c128", fl, 0.0);
-  if (trace_on()) ks.note = size_note(jobs);
-  k_qr<T><<<(unsigned)jobs.size(), 512, 0, ctx->stream>>>(d.as<QrJob>(), work.as<T>(),
-                                                          dw.as<int64_t>());
-  TNFA_LAUNCH_CHECK();
 }
 
 // ----------------------------------------------------------------- svd --
@@ -386,18 +448,7 @@ __device__ inline void rr_pair(int n2, int r, int i, int& p, int& q) {
 template <class T> struct RealOf { using type = double; };
 template <> struct RealOf<float> { using type = float; };
 
-__device__ inline double ldcg(const double* p) { return __ldcg(p); }
-__device__ inline float ldcg(const float* p) { return __ldcg(p); }
-__device__ inline cplx ldcg(const cplx* p) {
-  const double2 v = __ldcg((const double2*)p);
-  return {v.x, v.y};
-}
-__device__ inline void stcg(double* p, double v) { __stcg(p, v); }
-__device__ inline void stcg(float* p, float v) { __stcg(p, v); }
-__device__ inline void stcg(cplx* p, cplx v) { __stcg((double2*)p, make_double2(v.re, v.im)); }
-__device__ inline float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
-__device__ inline double fmaT(double a, double b, double c) { return fma(a, b, c); }
-__device__ inline cplx fmaT(cplx a, cplx b, cplx c) { return Sc<cplx>::fma(a, b, c); }
+
 
 template <bool CL>
 __device__ inline void jsync() {
@@ -920,11 +971,16 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
   }
   copy_blocks<T, T>(ctx, adj);
   auto core = [&](size_t q) { return tall[q] ? R[q].p : J[q].p; };
-  // (2) Jacobi on the core
+  // (2) Jacobi on the core: U (n x ku) with ku = n (plain) or the kept
+  // width of the FP32 pass (mixed); extra[q] = weight outside U's span
+  std::vector<int> ku(n);
+  std::vector<double> extra(nj, 0.0);
   std::vector<SvdJob> sj;
   if (!mixed) {
-    for (size_t q = 0; q < nj; ++q)
+    for (size_t q = 0; q < nj; ++q) {
+      ku[q] = n[q];
       sj.push_back({core(q), U[q].p, S[q].as<double>(), nullptr, n[q], n[q], sw[q].as<int>()});
+    }
     jacobi<T>(ctx, sj, 60, 1e-10, real64 ? "svd_f64" : "svd_c128");
   } else {
     std::vector<DBuf> J32(nj), U32(nj), V32(nj), S32(nj), sw32(nj), V(nj), G(nj), Y(nj), W(nj);
@@ -939,23 +995,41 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
       sw32[q] = DBuf(ctx, sizeof(int));
       down.push_back({core(q), J32[q].p, k, k, k, k, 0, 0});
       s32.push_back({J32[q].p, U32[q].p, S32[q].as<double>(), V32[q].p, k, k, sw32[q].as<int>()});
-      V[q] = DBuf(ctx, (size_t)k * k * sizeof(double));
-      up.push_back({V32[q].p, V[q].p, k, k, k, k, 0, 0});
     }
     copy_blocks<double, float>(ctx, down);
     jacobi<float>(ctx, s32, 60, 0.0, "svd_f32");
+    // keep the FP32 directions that a 100x smaller cutoff would keep (all
+    // of them without a cutoff); the rest carries less than 1 % of the
+    // truncation budget and is dropped together
+    std::vector<std::vector<double>> sv32(nj);
+    for (size_t q = 0; q < nj; ++q) {
+      sv32[q].resize(n[q]);
+      TNFA_CUDA(cudaMemcpyAsync(sv32[q].data(), S32[q].p, n[q] * sizeof(double), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+    }
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (size_t q = 0; q < nj; ++q) {
+      const int k = n[q];
+      int keep = cutoff > 0 ? truncation_rank(sv32[q].data(), k, cutoff * 1e-2, 0, 1) : k;
+      if (maxdim > 0) keep = std::min(keep, std::min(k, maxdim + 8));
+      keep = std::max(keep, std::min(k, std::max(mindim, 1)));
+      ku[q] = keep;
+      for (int i = keep; i < k; ++i) extra[q] += sv32[q][i] * sv32[q][i];
+      V[q] = DBuf(ctx, (size_t)k * keep * sizeof(double));
+      up.push_back({V32[q].p, V[q].p, k, keep, k, keep, 0, 0});
+    }
     copy_blocks<float, double>(ctx, up);
-    // V <- V (3 I - V^T V) / 2, twice: orthonormal to rounding
+    // V <- V (3 I - V^T V) / 2, twice: orthonormal columns to rounding
     for (int it = 0; it < 2; ++it) {
       std::vector<GemmJob> g1, g2;
       std::vector<CopyJob> cp;
       for (size_t q = 0; q < nj; ++q) {
-        const int k = n[q];
-        G[q] = DBuf(ctx, (size_t)k * k * sizeof(double));
-        Y[q] = DBuf(ctx, (size_t)k * k * sizeof(double));
-        g1.push_back({V[q].p, V[q].p, G[q].p, k, k, k, k, k, k, 1, 0, 1.0, 0.0});
-        cp.push_back({V[q].p, Y[q].p, k, k, k, k, 0, 0});
-        g2.push_back({V[q].p, G[q].p, Y[q].p, k, k, k, k, k, k, 0, 0, -0.5, 1.5});
+        const int k = n[q], c = ku[q];
+        G[q] = DBuf(ctx, (size_t)c * c * sizeof(double));
+        Y[q] = DBuf(ctx, (size_t)k * c * sizeof(double));
+        g1.push_back({V[q].p, V[q].p, G[q].p, c, c, k, c, c, c, 1, 0, 1.0, 0.0});
+        cp.push_back({V[q].p, Y[q].p, k, c, c, c, 0, 0});
+        g2.push_back({V[q].p, G[q].p, Y[q].p, k, c, c, c, c, c, 0, 0, -0.5, 1.5});
       }
       gemm<double>(ctx, g1);
       copy_blocks<double, double>(ctx, cp);
@@ -964,19 +1038,20 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     }
     std::vector<GemmJob> gw;
     for (size_t q = 0; q < nj; ++q) {
-      const int k = n[q];
-      W[q] = DBuf(ctx, (size_t)k * k * sizeof(double));
-      gw.push_back({core(q), V[q].p, W[q].p, k, k, k, k, k, k, 0, 0, 1.0, 0.0});
+      const int k = n[q], c = ku[q];
+      W[q] = DBuf(ctx, (size_t)k * c * sizeof(double));
+      gw.push_back({core(q), V[q].p, W[q].p, k, c, k, k, c, c, 0, 0, 1.0, 0.0});
+      U[q] = DBuf(ctx, (size_t)k * c * sizeof(T));
     }
     gemm<double>(ctx, gw);
     for (size_t q = 0; q < nj; ++q)
-      sj.push_back({W[q].p, U[q].p, S[q].as<double>(), nullptr, n[q], n[q], sw[q].as<int>()});
+      sj.push_back({W[q].p, U[q].p, S[q].as<double>(), nullptr, n[q], ku[q], sw[q].as<int>()});
     jacobi<T>(ctx, sj, 60, 1e-10, "svd_polish_f64");
   }
   // (3) ranks on the host
   for (size_t q = 0; q < nj; ++q) {
-    out[q].s.resize(n[q]);
-    TNFA_CUDA(cudaMemcpyAsync(out[q].s.data(), S[q].p, n[q] * sizeof(double), cudaMemcpyDeviceToHost,
+    out[q].s.resize(ku[q]);
+    TNFA_CUDA(cudaMemcpyAsync(out[q].s.data(), S[q].p, ku[q] * sizeof(double), cudaMemcpyDeviceToHost,
                               ctx->stream));
     TNFA_CUDA(cudaMemcpyAsync(&out[q].sweeps, sw[q].p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   }
@@ -986,23 +1061,30 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
   for (size_t q = 0; q < nj; ++q) {
     FactorResult& o = out[q];
     const FactorJob& f = jobs[q];
-    const int k = n[q];
-    const int r = truncation_rank(o.s.data(), k, cutoff, maxdim, mindim);
+    const int k = n[q], c = ku[q];
+    double tot = extra[q];
+    for (int i = 0; i < c; ++i) tot += o.s[i] * o.s[i];
+    int r = c;
+    double drop = extra[q];
+    if (tot > 0.0 && cutoff > 0.0)
+      while (r > 1 && drop + o.s[r - 1] * o.s[r - 1] <= cutoff * tot) {
+        --r;
+        drop += o.s[r] * o.s[r];
+      }
+    if (maxdim > 0) r = std::min(r, maxdim);
+    r = std::max(r, std::min(std::max(mindim, 1), c));
+    drop = extra[q];
+    for (int i = r; i < c; ++i) drop += o.s[i] * o.s[i];
     o.r = r;
-    double tot = 0, drop = 0;
-    for (int i = 0; i < k; ++i) {
-      tot += o.s[i] * o.s[i];
-      if (i >= r) drop += o.s[i] * o.s[i];
-    }
     o.discarded = tot > 0 ? drop / tot : 0.0;
     o.L = DBuf(ctx, (size_t)f.rows * r * sizeof(T));
     o.X = DBuf(ctx, (size_t)r * f.cols * sizeof(T));
     if (tall[q]) {
-      gl.push_back({Q[q].p, U[q].p, o.L.p, f.rows, r, k, k, k, r, 0, 0, 1.0, 0.0});
-      gx.push_back({U[q].p, R[q].p, o.X.p, r, f.cols, k, k, f.cols, f.cols, 2, 0, 1.0, 0.0});
+      gl.push_back({Q[q].p, U[q].p, o.L.p, f.rows, r, k, k, c, r, 0, 0, 1.0, 0.0});
+      gx.push_back({U[q].p, R[q].p, o.X.p, r, f.cols, k, c, f.cols, f.cols, 2, 0, 1.0, 0.0});
     } else {
-      cl.push_back({U[q].p, o.L.p, k, r, k, r, 0, 0});
-      gx.push_back({U[q].p, f.M, o.X.p, r, f.cols, k, k, f.cols, f.cols, 2, 0, 1.0, 0.0});
+      cl.push_back({U[q].p, o.L.p, k, r, c, r, 0, 0});
+      gx.push_back({U[q].p, f.M, o.X.p, r, f.cols, k, c, f.cols, f.cols, 2, 0, 1.0, 0.0});
     }
   }
   gemm<T>(ctx, gl);
