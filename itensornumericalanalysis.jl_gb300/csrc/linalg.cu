@@ -330,8 +330,9 @@ __global__ void __launch_bounds__(512) k_qr(const QrJob* __restrict__ jobs, T* _
     const double beta = re(ldcg(tau + j));
     if (beta == 0.0) continue;
     const T* x = W + (int64_t)j * m;
-    const int c0 = j + ((crank - j) % C + C) % C;
-    for (int c = c0 + C * warp; c < kq; c += C * nw) {
+    // a column stays with one warp for all j (no barrier between the j)
+    for (int c = crank + C * warp; c < kq; c += C * nw) {
+      if (c < j) continue;
       T* y = Qw + (int64_t)c * m;
       T w = from_real<T>(0.0);
       for (int r = j + lane; r < m; r += 32) w = Sc<T>::fma(conj(ldcg(x + r)), y[r], w);
