@@ -446,8 +446,20 @@ __device__ inline void rr_pair(int n2, int r, int i, int& p, int& q) {
 // stop = max(tol, stop_rel): Jacobi converges quadratically near the end, so
 // after a sweep whose rotations were all below ~1e-10 the next one would
 // change nothing above rounding.
+//
+// Deflation (small_rel > 0): a pair whose columns both weigh less than
+// small_rel |A|_F^2 / n is skipped.  The columns above that bound end up
+// orthogonal to each other and to the rest, so their norms are singular
+// values and the rest spans the complementary subspace with a known total
+// weight below small_rel |A|_F^2; a truncation whose budget exceeds that
+// drops all of it, and decides exactly like on the full decomposition.
 template <class T> struct RealOf { using type = double; };
 template <> struct RealOf<float> { using type = float; };
+
+struct JacobiOpts {
+  double stop_rel;   // sweep-level stop threshold (relative |g| / sqrt(a b))
+  double small_rel;  // deflation bound (relative to |A|_F^2 / n); 0: none
+};
 
 
 
@@ -462,7 +474,7 @@ __device__ inline void jsync() {
 template <class T, bool CL, int MAXR>
 __global__ void __launch_bounds__(512) k_jacobi(const SvdJob* __restrict__ jobs, T* __restrict__ work,
                                                 const int64_t* __restrict__ woff, int* __restrict__ flags,
-                                                int max_sweeps, double stop_rel) {
+                                                int max_sweeps, JacobiOpts opt) {
   using R = typename RealOf<T>::type;
   int C = 1, crank = 0;
   if constexpr (CL) {
@@ -496,7 +508,9 @@ __global__ void __launch_bounds__(512) k_jacobi(const SvdJob* __restrict__ jobs,
   // columns below this are rounding noise of the whole matrix
   const double negl = (sizeof(R) == 4 ? 1e-13 : 1e-30) * fro2;
   const R tol = (R)(8.0 * sqrt((double)m) * eps);
-  const R stop = (R)fmax((double)tol, stop_rel);
+  const R stop = (R)fmax((double)tol, opt.stop_rel);
+  // pairs of columns both below this are left alone (deflation for truncation)
+  const double small = opt.small_rel * fro2 / n;
   const int n2 = (n + 1) & ~1;
   const int gw = crank * nw + warp, nwc = C * nw;
   int sweep = 0;
@@ -540,6 +554,7 @@ __global__ void __launch_bounds__(512) k_jacobi(const SvdJob* __restrict__ jobs,
         // a negligible column carries no singular value worth orthogonalising
         // against; skipping it also avoids zeta^2 overflow on extreme ratios
         if ((double)a < negl || (double)b < negl) continue;
+        if ((double)a < small && (double)b < small) continue;
         const R nab = sqrt(a) * sqrt(b);
         if (ag > stop * nab) busy = 1;
         if (ag <= tol * nab || ag == (R)0) continue;
@@ -627,7 +642,7 @@ inline bool svd_big(const SvdJob& j) { return j.n >= 96 && (double)j.m * j.n * j
 
 template <class T, bool CL, int MAXR>
 void launch_jacobi(tnfa_ctx* ctx, const SvdJob* d, T* work, const int64_t* woff, int* flags, int njobs,
-                   int max_sweeps, double stop_rel) {
+                   int max_sweeps, JacobiOpts stop_rel) {
   if constexpr (CL) {
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)(njobs * SVD_CLUSTER));
@@ -652,7 +667,7 @@ void launch_jacobi(tnfa_ctx* ctx, const SvdJob* d, T* work, const int64_t* woff,
 template <class T> constexpr int jacobi_maxr() { return sizeof(T) == 16 ? 8 : 16; }
 
 template <class T>
-void jacobi(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, double stop_rel,
+void jacobi(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, JacobiOpts stop_rel,
             const char* family) {
   std::vector<SvdJob> big, small;
   for (const auto& j : jobs) (svd_big(j) ? big : small).push_back(j);
@@ -706,7 +721,7 @@ void jacobi(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, doub
 template <class T>
 void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
   if (jobs.empty()) return;
-  jacobi<T>(ctx, jobs, max_sweeps, 1e-10,
+  jacobi<T>(ctx, jobs, max_sweeps, JacobiOpts{1e-10, 0.0},
             sizeof(T) == 8 ? "svd_f64" : (sizeof(T) == 4 ? "svd_f32" : "svd_c128"));
   // Diagnostics: with TNFA_DEBUG_DIR set, the input of every SVD that hit the
   // sweep cap is written there (int32 m, int32 n, element size, then data).
@@ -934,10 +949,15 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
   if (!nj) return;
   constexpr bool real64 = std::is_same<T, double>::value;
   const bool mixed = real64 && (precision == TNFA_PREC_MIXED || precision == TNFA_PREC_F32);
-  std::vector<char> tall(nj);
-  std::vector<int> n(nj);
+  // Per job the core C (cm x k) that Jacobi diagonalises, and how L and X
+  // follow from its left vectors U_r:
+  //   tall, QR  : M = Q R, C = R (k x k),   L = Q U_r, X = U_r^H R
+  //   tall, none: C = M (rows x k) [mixed], L = U_r,   X = U_r^H M
+  //   wide      : M^H = Q R, C = R^H,       L = U_r,   X = U_r^H M
+  std::vector<int> n(nj), cm(nj), ku(nj);
+  std::vector<char> tall(nj), useq(nj);
   std::vector<DBuf> Q(nj), R(nj), tau(nj), Mt(nj), J(nj), U(nj), S(nj), sw(nj);
-  // (1) the square core J
+  std::vector<const void*> core(nj);
   std::vector<CopyJob> adj;
   std::vector<QrJob> qj;
   for (size_t q = 0; q < nj; ++q) {
@@ -945,60 +965,63 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     tall[q] = f.rows >= f.cols;
     n[q] = std::min(f.rows, f.cols);
     const int k = n[q];
+    useq[q] = tall[q] && !mixed;
+    sw[q] = DBuf(ctx, sizeof(int));
+    if (tall[q] && mixed) {
+      core[q] = f.M;
+      cm[q] = f.rows;
+      continue;
+    }
     R[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
     tau[q] = DBuf(ctx, (size_t)k * sizeof(T));
+    cm[q] = k;
     if (tall[q]) {
       Q[q] = DBuf(ctx, (size_t)f.rows * k * sizeof(T));
       qj.push_back({f.M, Q[q].p, R[q].p, tau[q].p, f.rows, f.cols});
+      core[q] = R[q].p;
     } else {
       Mt[q] = DBuf(ctx, (size_t)f.rows * f.cols * sizeof(T));
       adj.push_back({f.M, Mt[q].p, f.rows, f.cols, f.cols, f.rows, 1, 1});
       Q[q] = DBuf(ctx, (size_t)f.cols * k * sizeof(T));
       qj.push_back({Mt[q].p, Q[q].p, R[q].p, tau[q].p, f.cols, f.rows});
+      J[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
+      core[q] = J[q].p;
     }
   }
   copy_blocks<T, T>(ctx, adj);
   qr<T>(ctx, qj);
   adj.clear();
-  for (size_t q = 0; q < nj; ++q) {
-    const int k = n[q];
-    if (!tall[q]) {
-      J[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
-      adj.push_back({R[q].p, J[q].p, k, k, k, k, 1, 1});
-    }
-    U[q] = DBuf(ctx, (size_t)k * k * sizeof(T));
-    S[q] = DBuf(ctx, (size_t)k * sizeof(double));
-    sw[q] = DBuf(ctx, sizeof(int));
-  }
+  for (size_t q = 0; q < nj; ++q)
+    if (!tall[q]) adj.push_back({R[q].p, J[q].p, n[q], n[q], n[q], n[q], 1, 1});
   copy_blocks<T, T>(ctx, adj);
-  auto core = [&](size_t q) { return tall[q] ? R[q].p : J[q].p; };
-  // (2) Jacobi on the core: U (n x ku) with ku = n (plain) or the kept
-  // width of the FP32 pass (mixed); extra[q] = weight outside U's span
-  std::vector<int> ku(n);
+  const JacobiOpts opts{1e-10, cutoff > 0 ? cutoff * 1e-2 : 0.0};
+  // (2) Jacobi on the core: U (cm x ku); extra[q] = weight outside U's span
   std::vector<double> extra(nj, 0.0);
   std::vector<SvdJob> sj;
   if (!mixed) {
     for (size_t q = 0; q < nj; ++q) {
       ku[q] = n[q];
-      sj.push_back({core(q), U[q].p, S[q].as<double>(), nullptr, n[q], n[q], sw[q].as<int>()});
+      U[q] = DBuf(ctx, (size_t)cm[q] * n[q] * sizeof(T));
+      S[q] = DBuf(ctx, (size_t)n[q] * sizeof(double));
+      sj.push_back({core[q], U[q].p, S[q].as<double>(), nullptr, cm[q], n[q], sw[q].as<int>()});
     }
-    jacobi<T>(ctx, sj, 60, 1e-10, real64 ? "svd_f64" : "svd_c128");
+    jacobi<T>(ctx, sj, 60, opts, real64 ? "svd_f64" : "svd_c128");
   } else {
-    std::vector<DBuf> J32(nj), U32(nj), V32(nj), S32(nj), sw32(nj), V(nj), G(nj), Y(nj), W(nj);
+    std::vector<DBuf> C32(nj), U32(nj), V32(nj), S32(nj), sw32(nj), V(nj), G(nj), Y(nj), W(nj);
     std::vector<CopyJob> down, up;
     std::vector<SvdJob> s32;
     for (size_t q = 0; q < nj; ++q) {
-      const int k = n[q];
-      J32[q] = DBuf(ctx, (size_t)k * k * sizeof(float));
-      U32[q] = DBuf(ctx, (size_t)k * k * sizeof(float));
+      const int k = n[q], m = cm[q];
+      C32[q] = DBuf(ctx, (size_t)m * k * sizeof(float));
+      U32[q] = DBuf(ctx, (size_t)m * k * sizeof(float));
       V32[q] = DBuf(ctx, (size_t)k * k * sizeof(float));
       S32[q] = DBuf(ctx, (size_t)k * sizeof(double));
       sw32[q] = DBuf(ctx, sizeof(int));
-      down.push_back({core(q), J32[q].p, k, k, k, k, 0, 0});
-      s32.push_back({J32[q].p, U32[q].p, S32[q].as<double>(), V32[q].p, k, k, sw32[q].as<int>()});
+      down.push_back({core[q], C32[q].p, m, k, k, k, 0, 0});
+      s32.push_back({C32[q].p, U32[q].p, S32[q].as<double>(), V32[q].p, m, k, sw32[q].as<int>()});
     }
     copy_blocks<double, float>(ctx, down);
-    jacobi<float>(ctx, s32, 60, 0.0, "svd_f32");
+    jacobi<float>(ctx, s32, 60, JacobiOpts{0.0, opts.small_rel}, "svd_f32");
     // keep the FP32 directions that a 100x smaller cutoff would keep (all
     // of them without a cutoff); the rest carries less than 1 % of the
     // truncation budget and is dropped together
@@ -1039,15 +1062,16 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     }
     std::vector<GemmJob> gw;
     for (size_t q = 0; q < nj; ++q) {
-      const int k = n[q], c = ku[q];
-      W[q] = DBuf(ctx, (size_t)k * c * sizeof(double));
-      gw.push_back({core(q), V[q].p, W[q].p, k, c, k, k, c, c, 0, 0, 1.0, 0.0});
-      U[q] = DBuf(ctx, (size_t)k * c * sizeof(T));
+      const int k = n[q], c = ku[q], m = cm[q];
+      W[q] = DBuf(ctx, (size_t)m * c * sizeof(double));
+      gw.push_back({core[q], V[q].p, W[q].p, m, c, k, k, c, c, 0, 0, 1.0, 0.0});
+      U[q] = DBuf(ctx, (size_t)m * c * sizeof(T));
+      S[q] = DBuf(ctx, (size_t)c * sizeof(double));
     }
     gemm<double>(ctx, gw);
     for (size_t q = 0; q < nj; ++q)
-      sj.push_back({W[q].p, U[q].p, S[q].as<double>(), nullptr, n[q], ku[q], sw[q].as<int>()});
-    jacobi<T>(ctx, sj, 60, 1e-10, "svd_polish_f64");
+      sj.push_back({W[q].p, U[q].p, S[q].as<double>(), nullptr, cm[q], ku[q], sw[q].as<int>()});
+    jacobi<T>(ctx, sj, 60, opts, "svd_polish_f64");
   }
   // (3) ranks on the host
   for (size_t q = 0; q < nj; ++q) {
@@ -1062,7 +1086,7 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
   for (size_t q = 0; q < nj; ++q) {
     FactorResult& o = out[q];
     const FactorJob& f = jobs[q];
-    const int k = n[q], c = ku[q];
+    const int k = n[q], c = ku[q], m = cm[q];
     double tot = extra[q];
     for (int i = 0; i < c; ++i) tot += o.s[i] * o.s[i];
     int r = c;
@@ -1080,12 +1104,12 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     o.discarded = tot > 0 ? drop / tot : 0.0;
     o.L = DBuf(ctx, (size_t)f.rows * r * sizeof(T));
     o.X = DBuf(ctx, (size_t)r * f.cols * sizeof(T));
-    if (tall[q]) {
+    if (useq[q]) {
       gl.push_back({Q[q].p, U[q].p, o.L.p, f.rows, r, k, k, c, r, 0, 0, 1.0, 0.0});
       gx.push_back({U[q].p, R[q].p, o.X.p, r, f.cols, k, c, f.cols, f.cols, 2, 0, 1.0, 0.0});
     } else {
-      cl.push_back({U[q].p, o.L.p, k, r, c, r, 0, 0});
-      gx.push_back({U[q].p, f.M, o.X.p, r, f.cols, k, c, f.cols, f.cols, 2, 0, 1.0, 0.0});
+      cl.push_back({U[q].p, o.L.p, m, r, c, r, 0, 0});
+      gx.push_back({U[q].p, f.M, o.X.p, r, f.cols, m, c, f.cols, f.cols, 2, 0, 1.0, 0.0});
     }
   }
   gemm<T>(ctx, gl);

@@ -46,12 +46,12 @@ struct QrJob {
 template <class T>
 void qr(tnfa_ctx* ctx, const std::vector<QrJob>& jobs);
 
-// One-sided Jacobi SVD of A (m x n, m >= n, lda = n, destroyed):
+// One-sided Jacobi SVD of A (m x n, m >= n, lda = n, read only):
 // A = U diag(S) V^H with U (m x n, orthonormal columns where S > 0), S (n,
-// real, descending), V (n x n).  conv receives the sweep count, or -1 when
-// the sweep cap was reached.
+// real, descending), V (n x n; not accumulated when V is null).  sweeps
+// receives the sweep count, or -1 when the sweep cap was reached.
 struct SvdJob {
-  void* A;
+  const void* A;
   void* U;
   double* S;
   void* V;
