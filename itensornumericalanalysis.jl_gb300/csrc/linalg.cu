@@ -39,6 +39,9 @@ __host__ __device__ inline float scal(float x, float a) { return x * a; }
 template <> __host__ __device__ inline float from_real<float>(double a) { return (float)a; }
 __device__ inline float shfl_xor(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 __device__ inline float phase(float x) { return x < 0 ? -1.0f : 1.0f; }
+__device__ inline float absval(float x) { return fabsf(x); }
+__device__ inline double absval(double x) { return fabs(x); }
+__device__ inline double absval(cplx x) { return hypot(x.re, x.im); }
 __device__ inline double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 __device__ inline cplx shfl_xor(cplx v, int o) {
   return {__shfl_xor_sync(0xffffffffu, v.re, o), __shfl_xor_sync(0xffffffffu, v.im, o)};
@@ -51,7 +54,7 @@ __device__ inline T warp_sum(T v) {
 // x / |x| (1 for x = 0)
 __device__ inline double phase(double x) { return x < 0 ? -1.0 : 1.0; }
 __device__ inline cplx phase(cplx x) {
-  double a = sqrt(abs2(x));
+  double a = hypot(x.re, x.im);
   return a > 0 ? cplx{x.re / a, x.im / a} : cplx{1.0, 0.0};
 }
 
@@ -550,7 +553,7 @@ __global__ void __launch_bounds__(512) k_jacobi(const SvdJob* __restrict__ jobs,
         a = warp_sum(a);
         b = warp_sum(b);
         g = warp_sum(g);
-        const R ag = sqrt(abs2(g));
+        const R ag = absval(g);  // |g| without squaring (|g|^2 underflows at small scales)
         // a negligible column carries no singular value worth orthogonalising
         // against; skipping it also avoids zeta^2 overflow on extreme ratios
         if ((double)a < negl || (double)b < negl) continue;
@@ -716,16 +719,11 @@ void jacobi(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, Jaco
     }
   }
   if (trace_on()) trace_sweeps(ctx, jobs);
-}
-
-template <class T>
-void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
-  if (jobs.empty()) return;
-  jacobi<T>(ctx, jobs, max_sweeps, JacobiOpts{1e-10, 0.0},
-            sizeof(T) == 8 ? "svd_f64" : (sizeof(T) == 4 ? "svd_f32" : "svd_c128"));
-  // Diagnostics: with TNFA_DEBUG_DIR set, the input of every SVD that hit the
-  // sweep cap is written there (int32 m, int32 n, element size, then data).
+  // Diagnostics: with TNFA_DEBUG_DIR set, the input of every Jacobi job that
+  // hit the sweep cap (or, with TNFA_DEBUG_SWEEPS=k, took k sweeps or more) is
+  // written there: int32 m, n, element size, sweeps, then the matrix.
   static const char* dbg = getenv("TNFA_DEBUG_DIR");
+  static const int thr = getenv("TNFA_DEBUG_SWEEPS") ? atoi(getenv("TNFA_DEBUG_SWEEPS")) : 0;
   if (dbg && *dbg) {
     static int counter = 0;
     for (const auto& j : jobs) {
@@ -733,21 +731,30 @@ void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
       int sw = 0;
       TNFA_CUDA(cudaMemcpyAsync(&sw, j.sweeps, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
       TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
-      if (sw >= 0) continue;
+      if (sw >= 0 && !(thr > 0 && sw >= thr)) continue;
+      if (counter >= 64) break;
       std::vector<T> h((size_t)j.m * j.n);
       TNFA_CUDA(cudaMemcpyAsync(h.data(), j.A, h.size() * sizeof(T), cudaMemcpyDeviceToHost,
                                 ctx->stream));
       TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
       char path[1024];
-      snprintf(path, sizeof path, "%s/svd_nonconv_%d.bin", dbg, counter++);
+      snprintf(path, sizeof path, "%s/jacobi_%s_%d.bin", dbg, family, counter++);
       if (FILE* fp = fopen(path, "wb")) {
-        int hdr[3] = {j.m, j.n, (int)sizeof(T)};
-        fwrite(hdr, sizeof(int), 3, fp);
+        int hdr[4] = {j.m, j.n, (int)sizeof(T), sw};
+        fwrite(hdr, sizeof(int), 4, fp);
         fwrite(h.data(), sizeof(T), h.size(), fp);
         fclose(fp);
       }
     }
   }
+}
+
+template <class T>
+void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
+  if (jobs.empty()) return;
+  jacobi<T>(ctx, jobs, max_sweeps, JacobiOpts{1e-10, 0.0},
+            sizeof(T) == 8 ? "svd_f64" : (sizeof(T) == 4 ? "svd_f32" : "svd_c128"));
+
 }
 
 // ------------------------------------------------------------------ lu --
@@ -905,7 +912,33 @@ struct CopyJob {
   void* dst;
   int rows, cols, lds, ldd;
   int trans, conj;
+  // when set: multiply by the power of two that brings sqrt(*sumsq) into
+  // [1, 2) (keeps FP32 copies of tiny or huge blocks in range, exactly)
+  const double* sumsq = nullptr;
 };
+
+__device__ inline double pow2_scale(const double* ss) {
+  if (!ss) return 1.0;
+  const double f = sqrt(*ss);
+  return f > 0 && isfinite(f) ? ldexp(1.0, -ilogb(f)) : 1.0;
+}
+
+// Per-job sum of squares of an m x k block (one CTA per job).
+struct SumsqJob {
+  const void* src;
+  int64_t n;
+  double* out;
+};
+
+__global__ void k_sumsq(const SumsqJob* __restrict__ jobs) {
+  const SumsqJob jb = jobs[blockIdx.x];
+  const double* x = (const double*)jb.src;
+  double part = 0.0;
+  for (int64_t i = threadIdx.x; i < jb.n; i += blockDim.x) part += x[i] * x[i];
+  __shared__ double red[32];
+  const double t = block_sum<double>(part, red);
+  if (threadIdx.x == 0) *jb.out = t;
+}
 
 __device__ inline double cvt(double x, double*) { return x; }
 __device__ inline float cvt(double x, float*) { return (float)x; }
@@ -923,6 +956,7 @@ __global__ void k_copy_block(const CopyJob* __restrict__ jobs) {
     const int r = (int)(i / jb.cols), c = (int)(i % jb.cols);
     S v = src[(int64_t)r * jb.lds + c];
     if (jb.conj) v = conj(v);
+    if (jb.sumsq) v = scal(v, (decltype(re(v)))pow2_scale(jb.sumsq));
     const int64_t o = jb.trans ? (int64_t)c * jb.ldd + r : (int64_t)r * jb.ldd + c;
     dst[o] = cvt(v, (D*)nullptr);
   }
@@ -1007,70 +1041,111 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     }
     jacobi<T>(ctx, sj, 60, opts, real64 ? "svd_f64" : "svd_c128");
   } else {
-    std::vector<DBuf> C32(nj), U32(nj), V32(nj), S32(nj), sw32(nj), V(nj), G(nj), Y(nj), W(nj);
-    std::vector<CopyJob> down, up;
-    std::vector<SvdJob> s32;
-    for (size_t q = 0; q < nj; ++q) {
-      const int k = n[q], m = cm[q];
-      C32[q] = DBuf(ctx, (size_t)m * k * sizeof(float));
-      U32[q] = DBuf(ctx, (size_t)m * k * sizeof(float));
-      V32[q] = DBuf(ctx, (size_t)k * k * sizeof(float));
-      S32[q] = DBuf(ctx, (size_t)k * sizeof(double));
-      sw32[q] = DBuf(ctx, sizeof(int));
-      down.push_back({core[q], C32[q].p, m, k, k, k, 0, 0});
-      s32.push_back({C32[q].p, U32[q].p, S32[q].as<double>(), V32[q].p, m, k, sw32[q].as<int>()});
-    }
-    copy_blocks<double, float>(ctx, down);
-    jacobi<float>(ctx, s32, 60, JacobiOpts{0.0, opts.small_rel}, "svd_f32");
-    // keep the FP32 directions that a 100x smaller cutoff would keep (all
-    // of them without a cutoff); the rest carries less than 1 % of the
-    // truncation budget and is dropped together
-    std::vector<std::vector<double>> sv32(nj);
-    for (size_t q = 0; q < nj; ++q) {
-      sv32[q].resize(n[q]);
-      TNFA_CUDA(cudaMemcpyAsync(sv32[q].data(), S32[q].p, n[q] * sizeof(double), cudaMemcpyDeviceToHost,
-                                ctx->stream));
-    }
-    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
-    for (size_t q = 0; q < nj; ++q) {
-      const int k = n[q];
-      int keep = cutoff > 0 ? truncation_rank(sv32[q].data(), k, cutoff * 1e-2, 0, 1) : k;
-      if (maxdim > 0) keep = std::min(keep, std::min(k, maxdim + 8));
-      keep = std::max(keep, std::min(k, std::max(mindim, 1)));
-      ku[q] = keep;
-      for (int i = keep; i < k; ++i) extra[q] += sv32[q][i] * sv32[q][i];
-      V[q] = DBuf(ctx, (size_t)k * keep * sizeof(double));
-      up.push_back({V32[q].p, V[q].p, k, keep, k, keep, 0, 0});
-    }
-    copy_blocks<float, double>(ctx, up);
-    // V <- V (3 I - V^T V) / 2, twice: orthonormal columns to rounding
-    for (int it = 0; it < 2; ++it) {
-      std::vector<GemmJob> g1, g2;
-      std::vector<CopyJob> cp;
-      for (size_t q = 0; q < nj; ++q) {
-        const int k = n[q], c = ku[q];
-        G[q] = DBuf(ctx, (size_t)c * c * sizeof(double));
-        Y[q] = DBuf(ctx, (size_t)k * c * sizeof(double));
-        g1.push_back({V[q].p, V[q].p, G[q].p, c, c, k, c, c, c, 1, 0, 1.0, 0.0});
-        cp.push_back({V[q].p, Y[q].p, k, c, c, c, 0, 0});
-        g2.push_back({V[q].p, G[q].p, Y[q].p, k, c, c, c, c, c, 0, 0, -0.5, 1.5});
+    // Two FP32 passes, each followed by an FP64 change of basis X <- X V.
+    // Pass 1 finds the directions worth keeping; pass 2 runs on X = C V,
+    // whose columns are already scaled by their singular values, so its FP32
+    // rounding is relative to each column and the small directions (which
+    // pass 1 cannot resolve below ~sqrt(eps32) of the largest) come out
+    // right.  FP64 Jacobi then converges in two or three sweeps.
+    std::vector<DBuf> X(nj);
+    std::vector<int> w(nj);
+    std::vector<const void*> xin(core);
+    for (size_t q = 0; q < nj; ++q) w[q] = n[q];
+    for (int pass = 0; pass < 2; ++pass) {
+      std::vector<DBuf> C32(nj), U32(nj), V32(nj), S32(nj), sw32(nj), V(nj), G(nj), Y(nj), Xn(nj);
+      std::vector<CopyJob> down, up;
+      std::vector<SvdJob> s32;
+      // FP32 copies scaled by a power of two to unit size
+      DBuf ss(ctx, nj * sizeof(double));
+      {
+        std::vector<SumsqJob> sq;
+        for (size_t q = 0; q < nj; ++q)
+          sq.push_back({xin[q], (int64_t)cm[q] * w[q], ss.as<double>() + q});
+        DBuf dq = upload(ctx, sq);
+        k_sumsq<<<(unsigned)nj, 256, 0, ctx->stream>>>(dq.as<SumsqJob>());
+        TNFA_LAUNCH_CHECK();
       }
-      gemm<double>(ctx, g1);
-      copy_blocks<double, double>(ctx, cp);
-      gemm<double>(ctx, g2);
-      for (size_t q = 0; q < nj; ++q) std::swap(V[q], Y[q]);
+      for (size_t q = 0; q < nj; ++q) {
+        const int k = w[q], m = cm[q];
+        C32[q] = DBuf(ctx, (size_t)m * k * sizeof(float));
+        U32[q] = DBuf(ctx, (size_t)m * k * sizeof(float));
+        V32[q] = DBuf(ctx, (size_t)k * k * sizeof(float));
+        S32[q] = DBuf(ctx, (size_t)k * sizeof(double));
+        sw32[q] = DBuf(ctx, sizeof(int));
+        down.push_back({xin[q], C32[q].p, m, k, k, k, 0, 0, ss.as<double>() + q});
+        s32.push_back({C32[q].p, U32[q].p, S32[q].as<double>(), V32[q].p, m, k, sw32[q].as<int>()});
+      }
+      copy_blocks<double, float>(ctx, down);
+      jacobi<float>(ctx, s32, 60, JacobiOpts{0.0, opts.small_rel}, "svd_f32");
+      if (pass == 0) {
+        // keep the FP32 directions that half the cutoff would keep (all of
+        // them without a cutoff); the rest carries at most half of the
+        // truncation budget, so the FP64 rule below drops it too (FP32
+        // singular values are accurate to ~1e-7 of the largest)
+        std::vector<std::vector<double>> sv32(nj);
+        std::vector<double> hss(nj);
+        for (size_t q = 0; q < nj; ++q) {
+          sv32[q].resize(n[q]);
+          TNFA_CUDA(cudaMemcpyAsync(sv32[q].data(), S32[q].p, n[q] * sizeof(double),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        TNFA_CUDA(cudaMemcpyAsync(hss.data(), ss.p, nj * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+        TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (size_t q = 0; q < nj; ++q) {
+          const int k = n[q];
+          // undo the power-of-two scaling of the FP32 copy
+          const double f = std::sqrt(hss[q]);
+          const double back = f > 0 && std::isfinite(f) ? std::ldexp(1.0, std::ilogb(f)) : 1.0;
+          for (double& x : sv32[q]) x *= back;
+          int keep = cutoff > 0 ? truncation_rank(sv32[q].data(), k, cutoff * 0.5, 0, 1) : k;
+          if (maxdim > 0) keep = std::min(keep, std::min(k, maxdim + 8));
+          keep = std::max(keep, std::min(k, std::max(mindim, 1)));
+          ku[q] = keep;
+          for (int i = keep; i < k; ++i) extra[q] += sv32[q][i] * sv32[q][i];
+        }
+      }
+      for (size_t q = 0; q < nj; ++q) {
+        const int k = w[q], c = ku[q];
+        V[q] = DBuf(ctx, (size_t)k * c * sizeof(double));
+        up.push_back({V32[q].p, V[q].p, k, c, k, c, 0, 0});
+      }
+      copy_blocks<float, double>(ctx, up);
+      // V <- V (3 I - V^T V) / 2, twice: orthonormal columns to rounding
+      for (int it = 0; it < 2; ++it) {
+        std::vector<GemmJob> g1, g2;
+        std::vector<CopyJob> cp;
+        for (size_t q = 0; q < nj; ++q) {
+          const int k = w[q], c = ku[q];
+          G[q] = DBuf(ctx, (size_t)c * c * sizeof(double));
+          Y[q] = DBuf(ctx, (size_t)k * c * sizeof(double));
+          g1.push_back({V[q].p, V[q].p, G[q].p, c, c, k, c, c, c, 1, 0, 1.0, 0.0});
+          cp.push_back({V[q].p, Y[q].p, k, c, c, c, 0, 0});
+          g2.push_back({V[q].p, G[q].p, Y[q].p, k, c, c, c, c, c, 0, 0, -0.5, 1.5});
+        }
+        gemm<double>(ctx, g1);
+        copy_blocks<double, double>(ctx, cp);
+        gemm<double>(ctx, g2);
+        for (size_t q = 0; q < nj; ++q) std::swap(V[q], Y[q]);
+      }
+      std::vector<GemmJob> gw;
+      for (size_t q = 0; q < nj; ++q) {
+        const int k = w[q], c = ku[q], m = cm[q];
+        Xn[q] = DBuf(ctx, (size_t)m * c * sizeof(double));
+        gw.push_back({xin[q], V[q].p, Xn[q].p, m, c, k, k, c, c, 0, 0, 1.0, 0.0});
+      }
+      gemm<double>(ctx, gw);
+      for (size_t q = 0; q < nj; ++q) {
+        X[q] = std::move(Xn[q]);
+        xin[q] = X[q].p;
+        w[q] = ku[q];
+      }
     }
-    std::vector<GemmJob> gw;
     for (size_t q = 0; q < nj; ++q) {
-      const int k = n[q], c = ku[q], m = cm[q];
-      W[q] = DBuf(ctx, (size_t)m * c * sizeof(double));
-      gw.push_back({core[q], V[q].p, W[q].p, m, c, k, k, c, c, 0, 0, 1.0, 0.0});
-      U[q] = DBuf(ctx, (size_t)m * c * sizeof(T));
-      S[q] = DBuf(ctx, (size_t)c * sizeof(double));
+      U[q] = DBuf(ctx, (size_t)cm[q] * ku[q] * sizeof(T));
+      S[q] = DBuf(ctx, (size_t)ku[q] * sizeof(double));
+      sj.push_back({X[q].p, U[q].p, S[q].as<double>(), nullptr, cm[q], ku[q], sw[q].as<int>()});
     }
-    gemm<double>(ctx, gw);
-    for (size_t q = 0; q < nj; ++q)
-      sj.push_back({W[q].p, U[q].p, S[q].as<double>(), nullptr, cm[q], ku[q], sw[q].as<int>()});
     jacobi<T>(ctx, sj, 60, opts, "svd_polish_f64");
   }
   // (3) ranks on the host
