@@ -490,7 +490,11 @@ __global__ void __launch_bounds__(512) k_jacobi(const SvdJob* __restrict__ jobs,
   const bool want_v = jb.V != nullptr;
   T* U = work + woff[ji];  // column-major m x n
   T* V = U + (int64_t)m * n;  // column-major n x n (when wanted)
-  double* sig = (double*)(V + (want_v ? (int64_t)n * n : 0));
+  // sig (n doubles) starts on an 8-byte boundary (job bases are 16-byte
+  // aligned; for 4-byte T the offset is rounded up to an even count)
+  constexpr int64_t al = sizeof(T) >= 8 ? 1 : 8 / sizeof(T);
+  const int64_t soff = ((int64_t)m * n + (want_v ? (int64_t)n * n : 0) + al - 1) / al * al;
+  double* sig = (double*)(U + soff);
   int* rank = (int*)(sig + n);
   int* flag = flags + 3 * ji;
   const T* A = (const T*)jb.A;
@@ -684,9 +688,11 @@ void jacobi(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, Jaco
       TNFA_CHECK(js[i].m >= js[i].n, TNFA_ERR_INVALID_ARGUMENT, "svd needs m >= n");
       const int64_t m = js[i].m, n = js[i].n;
       maxm = std::max(maxm, js[i].m);
-      // U (and V) in T; sig (n doubles) and rank (n ints) rounded up to T slots
-      woff[i + 1] = woff[i] + m * n + (js[i].V ? n * n : 0) +
-                    (int64_t)((n * 12 + sizeof(T) - 1) / sizeof(T)) + 2;
+      // U (and V) in T; sig (n doubles) and rank (n ints) rounded up to T
+      // slots, with slack for aligning sig; every job base 16-byte aligned
+      const int64_t al = (int64_t)(16 / sizeof(T) > 0 ? 16 / sizeof(T) : 1);
+      const int64_t need = m * n + (js[i].V ? n * n : 0) + (int64_t)((n * 12 + sizeof(T) - 1) / sizeof(T)) + 4;
+      woff[i + 1] = woff[i] + (need + al - 1) / al * al;
       fl += 5.0 * m * n * n * 8;  // ~8 sweeps of 3 dots + 2 rotations per pair
     }
     DBuf work(ctx, (size_t)woff.back() * sizeof(T));
