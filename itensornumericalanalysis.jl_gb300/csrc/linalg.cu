@@ -1056,6 +1056,9 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     std::vector<DBuf> X(nj);
     std::vector<int> w(nj);
     std::vector<const void*> xin(core);
+    // |C|_F^2 and |C V_kept|_F^2 in FP64: their difference is the weight of
+    // the directions dropped after pass 1, exact to FP64 rounding
+    std::vector<double> ss_in(nj), ss_kept(nj);
     for (size_t q = 0; q < nj; ++q) w[q] = n[q];
     for (int pass = 0; pass < 2; ++pass) {
       std::vector<DBuf> C32(nj), U32(nj), V32(nj), S32(nj), sw32(nj), V(nj), G(nj), Y(nj), Xn(nj);
@@ -1070,6 +1073,8 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
         DBuf dq = upload(ctx, sq);
         k_sumsq<<<(unsigned)nj, 256, 0, ctx->stream>>>(dq.as<SumsqJob>());
         TNFA_LAUNCH_CHECK();
+        TNFA_CUDA(cudaMemcpyAsync(pass == 0 ? ss_in.data() : ss_kept.data(), ss.p, nj * sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
       }
       for (size_t q = 0; q < nj; ++q) {
         const int k = w[q], m = cm[q];
@@ -1089,14 +1094,12 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
         // truncation budget, so the FP64 rule below drops it too (FP32
         // singular values are accurate to ~1e-7 of the largest)
         std::vector<std::vector<double>> sv32(nj);
-        std::vector<double> hss(nj);
+        const std::vector<double>& hss = ss_in;
         for (size_t q = 0; q < nj; ++q) {
           sv32[q].resize(n[q]);
           TNFA_CUDA(cudaMemcpyAsync(sv32[q].data(), S32[q].p, n[q] * sizeof(double),
                                     cudaMemcpyDeviceToHost, ctx->stream));
         }
-        TNFA_CUDA(cudaMemcpyAsync(hss.data(), ss.p, nj * sizeof(double), cudaMemcpyDeviceToHost,
-                                  ctx->stream));
         TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
         for (size_t q = 0; q < nj; ++q) {
           const int k = n[q];
@@ -1108,7 +1111,6 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
           if (maxdim > 0) keep = std::min(keep, std::min(k, maxdim + 8));
           keep = std::max(keep, std::min(k, std::max(mindim, 1)));
           ku[q] = keep;
-          for (int i = keep; i < k; ++i) extra[q] += sv32[q][i] * sv32[q][i];
         }
       }
       for (size_t q = 0; q < nj; ++q) {
@@ -1147,6 +1149,8 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
         w[q] = ku[q];
       }
     }
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (size_t q = 0; q < nj; ++q) extra[q] = std::max(0.0, ss_in[q] - ss_kept[q]);
     for (size_t q = 0; q < nj; ++q) {
       U[q] = DBuf(ctx, (size_t)cm[q] * ku[q] * sizeof(T));
       S[q] = DBuf(ctx, (size_t)ku[q] * sizeof(double));
