@@ -629,7 +629,9 @@ __global__ void __launch_bounds__(512) k_jacobi(const SvdJob* __restrict__ jobs,
   for (int64_t i = gt; i < (int64_t)m * n; i += gs) {
     const int c = (int)(i / m), r = (int)(i % m);
     const double sc = __ldcg(sig + c);
-    Uo[(int64_t)r * n + __ldcg(rank + c)] = sc > 0 ? scal(ldcg(U + i), (R)(1.0 / sc)) : from_real<T>(0.0);
+    // a negligible column was never orthogonalised: it leaves U as zeros
+    Uo[(int64_t)r * n + __ldcg(rank + c)] =
+        sc * sc > negl && sc > 0 ? scal(ldcg(U + i), (R)(1.0 / sc)) : from_real<T>(0.0);
   }
   if (want_v) {
     T* Vo = (T*)jb.V;
@@ -1183,6 +1185,11 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
         drop += o.s[r] * o.s[r];
       }
     if (maxdim > 0) r = std::min(r, maxdim);
+    // never keep directions at the rounding floor: Jacobi leaves them
+    // unorthogonalised (zero columns of U)
+    int nz = 0;
+    while (nz < c && o.s[nz] * o.s[nz] > 1e-28 * tot) ++nz;
+    r = std::min(r, std::max(nz, 1));
     r = std::max(r, std::min(std::max(mindim, 1), c));
     drop = extra[q];
     for (int i = r; i < c; ++i) drop += o.s[i] * o.s[i];

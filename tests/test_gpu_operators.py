@@ -235,6 +235,22 @@ def test_mixed_truncation_matches_fp64(ina, L, chi):
         assert rel_err(g.evaluate_batch(X), ref) < 1e-9
 
 
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_apply_without_cutoff_is_exact(ina, precision):
+    """cutoff 0 keeps every direction above the rounding floor: the result is
+    the exact d/dx f on the dense grid (oracle stencil terms), in both the
+    plain and the FP32-preconditioned factorisation."""
+    L = 10
+    s = ina.continuous_siteinds(ina.named_path_graph(L))
+    f = ina.rand_itn(s, link_space=16, rng=28, normalize=True)
+    g = ina.operate(ina.first_derivative_operator(s), f, cutoff=0.0, precision=precision)
+    xs = np.arange(2**L) / 2.0**L
+    F = f.evaluate_batch(xs)
+    G = O.apply_terms_dense(O.stencil_terms(L, [0.0, 0.5, 0.0, -0.5, 0.0], 1), F.reshape((2,) * L),
+                            {(1, k): k - 1 for k in range(1, L + 1)}).reshape(-1)
+    assert rel_err(g.evaluate_batch(xs), G) < 1e-11
+
+
 def test_truncate_maxdim_and_normalize(ina):
     graph = O.path_graph(10)
     rng = np.random.default_rng(22)
