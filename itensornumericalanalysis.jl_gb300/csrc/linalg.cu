@@ -1091,11 +1091,13 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
       copy_blocks<double, float>(ctx, down);
       jacobi<float>(ctx, s32, 60, JacobiOpts{0.0, opts.small_rel}, "svd_f32");
       if (pass == 0) {
-        // keep the FP32 directions that a 100x smaller cutoff would keep
-        // (all of them without a cutoff); the rest carries at most 1 % of the
-        // truncation budget, so the FP64 rule below drops it too (FP32
-        // singular values are accurate to ~1e-7 of the largest), and the
-        // FP64 rule's boundary falls among polished FP64 directions
+        // keep the FP32 directions that a 10^6 times smaller cutoff would
+        // keep (all of them without a cutoff).  What pass 1 drops cannot be
+        // recovered: a kept direction s_k tilts by ~eps32 s_max / s_k into
+        // the dropped span, losing ~eps32 s_drop / s_k of itself, so the
+        // dropped weight must sit far below the truncation budget (here
+        // 1e-6 of it: the FP64 rule below drops it too, and the loss stays
+        // near 1e-10 of the norm).  Exactly-deficient ranks still fall away.
         std::vector<std::vector<double>> sv32(nj);
         const std::vector<double>& hss = ss_in;
         for (size_t q = 0; q < nj; ++q) {
@@ -1110,7 +1112,7 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
           const double f = std::sqrt(hss[q]);
           const double back = f > 0 && std::isfinite(f) ? std::ldexp(1.0, std::ilogb(f)) : 1.0;
           for (double& x : sv32[q]) x *= back;
-          int keep = cutoff > 0 ? truncation_rank(sv32[q].data(), k, cutoff * 1e-2, 0, 1) : k;
+          int keep = cutoff > 0 ? truncation_rank(sv32[q].data(), k, cutoff * 1e-6, 0, 1) : k;
           if (maxdim > 0) keep = std::min(keep, std::min(k, maxdim + 8));
           keep = std::max(keep, std::min(k, std::max(mindim, 1)));
           ku[q] = keep;
