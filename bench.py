@@ -246,8 +246,9 @@ def _timed(fn, reps=1):
 def secondary_measurements(ctx, ws, rank, args) -> dict:
     """The other configurations of the metric, one timed repetition each after
     a warm-up: batched MPO apply + truncate (512 uneven MPS, first derivative,
-    cutoff 1e-10, FP64), the reference's CPU case end to end (L = 20), and the
-    gradient of batched evaluation (comb 2 x 12, chi 32, FP32, 2^20 points)."""
+    cutoff 1e-10; FP64 plain and mixed), the 2-D Laplace solve (comb 2 x 16),
+    the reference's CPU case end to end (L = 20), and the gradient of batched
+    evaluation (comb 2 x 12, chi 32, FP32, 2^20 points)."""
     import itensornumericalanalysis as ina
     from itensornumericalanalysis.workloads import uneven_mps_batch, upload_batch
 
@@ -260,23 +261,54 @@ def secondary_measurements(ctx, ws, rank, args) -> dict:
         if s.nv() not in ops:
             ops[s.nv()] = ina.first_derivative_operator(s)
     oplist = [ops[s.nv()] for s, _ in batch]
-    ina.operate_batched(oplist[:8], fs[:8], cutoff=1e-10)  # warm-up (allocator, kernels)
-    ctx.kernel_stats(reset=True)
-    ctx.set_timing(True)
-    t, res = _timed(lambda: ina.operate_batched(oplist, fs, cutoff=1e-10))
-    ctx.set_timing(False)
-    st = ctx.kernel_stats(reset=True)
-    t = max_over_ranks(t, ws)
-    fl = {k: v["flops"] for k, v in st.items()}
+    Xc5 = np.random.default_rng(0).random(256)
+    c5 = {}
+    for prec in ("f64", "mixed"):
+        ina.operate_batched(oplist[:8], fs[:8], cutoff=1e-10, precision=prec)  # warm-up
+        ctx.kernel_stats(reset=True)
+        ctx.set_timing(True)
+        t, res = _timed(lambda: ina.operate_batched(oplist, fs, cutoff=1e-10, precision=prec))
+        ctx.set_timing(False)
+        st = ctx.kernel_stats(reset=True)
+        t = max_over_ranks(t, ws)
+        c5[prec] = {
+            "value": ws * len(fs) / t, "unit": "MPS/s", "s_per_batch": t,
+            "max_bond_after": max(r.maxlinkdim() for r in res),
+            "kernel_ms": {k: round(v["ms"], 2) for k, v in sorted(st.items(), key=lambda kv: -kv[1]["ms"])[:6]},
+            "vals": [r.evaluate_batch(Xc5) for r in res[:64]],
+        }
+        del res
+    va, vb = c5["f64"].pop("vals"), c5["mixed"].pop("vals")
+    err = max(float(np.max(np.abs(a - b)) / max(np.max(np.abs(a)), 1e-300)) for a, b in zip(va, vb))
     out["mpo_apply_truncate"] = {
-        "value": ws * len(fs) / t, "unit": "MPS/s", "batch": len(fs), "s_per_batch": t,
-        "precision": "f64 (plain; the mixed apply path is not built)",
-        "max_bond_after": max(r.maxlinkdim() for r in res),
-        "kernel_ms": {k: round(v["ms"], 2) for k, v in sorted(st.items(), key=lambda kv: -kv[1]["ms"])[:6]},
-        "fp64_tflops": sum(v["flops"] for k, v in st.items() if k in ("qr_f64", "svd_f64", "gemm_f64"))
-        / t / 1e12,
+        "value": c5["mixed"]["value"], "unit": "MPS/s", "batch": len(fs),
+        "precision": "mixed (FP32-preconditioned Jacobi, FP64 polish and QR)",
+        "mixed": c5["mixed"], "fp64_plain": c5["f64"],
+        "mixed_over_fp64": c5["mixed"]["value"] / c5["f64"]["value"],
+        "rel_err_mixed_vs_fp64": err,
+        "rel_err_what": "max over 64 MPS of max|g_mixed - g_f64| / max|g_f64| at 256 points",
     }
-    del res, fs
+    del fs
+    # --- config 2: 2-D Laplace solve on a comb, 2 x 16 bits ---------------------
+    L2 = 16
+    s2 = ina.continuous_siteinds(ina.named_comb_tree((2, L2)),
+                                 [[(1, j) for j in range(L2, 0, -1)], [(2, j) for j in range(1, L2 + 1)]])
+    b2 = ina.sin_itn(s2, k=np.pi, dim=1) * ina.sin_itn(s2, k=np.pi, dim=2)
+    A2 = ina.laplacian_operator(s2)
+
+    def solve2():
+        return ina.linsolve(A2, b2, nsweeps=2, maxdim=64, cutoff=1e-20, tol=1e-8)
+
+    solve2()
+    t2, x2 = _timed(solve2)
+    X2 = np.random.default_rng(2).random((4096, 2))
+    exact2 = -np.sin(np.pi * X2[:, 0]) * np.sin(np.pi * X2[:, 1]) / (2 * np.pi**2)
+    got2 = x2.evaluate_batch(X2, [1, 2])
+    out["laplace_linsolve"] = {
+        "value": t2, "unit": "s", "what": "linsolve(laplacian, sin(pi x) sin(pi y)), 2 sweeps, maxdim 64, cutoff 1e-20",
+        "rel_residual": x2.rel_residual, "maxlinkdim": x2.maxlinkdim(),
+        "max_err_vs_continuum": float(np.max(np.abs(got2 - exact2)) / np.max(np.abs(exact2))),
+    }
     # --- config 1: the reference's CPU case on the GPU ---------------------------
     L = 20
     s = ina.continuous_siteinds(ina.named_grid((L, 1)))
