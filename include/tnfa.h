@@ -273,16 +273,22 @@ typedef struct {
   int32_t maxdim;       /* bond cap of the solution                               */
   double cutoff;        /* truncation of the two-site updates                     */
   double tol;           /* stop when ||A x - b|| / ||b|| <= tol                   */
-  int32_t krylov_dim;   /* local solver iterations per two-site update           */
-  int32_t precision;    /* tnfa_precision of the local contractions               */
+  int32_t krylov_dim;   /* reserved (local systems are solved densely)            */
+  int32_t precision;    /* reserved (FP64)                                        */
   double a0, a1;        /* solve (a0 + a1*A) x = b                                */
+  int32_t refinements;  /* iterative-refinement steps after the sweeps            */
+  double refine_cutoff; /* truncation of residuals and corrections in refinement  */
 } tnfa_linsolve_params;
 
-/* Solve (a0 + a1 A) x = b by two-site alternating sweeps with a local
- * Krylov solver; x0 seeds the sweep.  Replaces ITensorNetworks.linsolve as
- * named for the Laplace solve (examples/2d_laplace_solver.jl:33-34 uses the
- * same sweep machinery through dmrg).  rel_residual receives the final
- * ||(a0 + a1 A) x - b|| / ||b|| computed exactly in FP64. */
+/* Solve (a0 + a1 A) x = b on a path-shaped tree by two-site alternating
+ * sweeps (dense FP64 LU per two-site system, truncated SVD split); x0 seeds
+ * the sweep.  Then up to `refinements` steps of iterative refinement: r = b -
+ * (a0 + a1 A) x formed exactly and truncated with refine_cutoff, the same
+ * sweeps solve for a correction e, x <- truncate(x + e, refine_cutoff).
+ * Replaces ITensorNetworks.linsolve as named for the Laplace solve
+ * (examples/2d_laplace_solver.jl:33-34 uses the same sweep machinery through
+ * dmrg).  rel_residual receives the final ||(a0 + a1 A) x - b|| / ||b||
+ * computed exactly in FP64. */
 int tnfa_linsolve(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnfa_net* x0,
                   const tnfa_linsolve_params* params, tnfa_net** x, double* rel_residual);
 

@@ -1137,9 +1137,9 @@ void abi(tnfa_ctx* ctx, int status) {
   if (status != TNFA_OK) fail(status, ctx->last_error);
 }
 
-// ||(a0 + a1 A) x - b|| / ||b||, every network in the path layout.
-double residual(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, Work<double>& x, double a0,
-                double a1, double bnorm) {
+// (a0 + a1 A) x - b as a network (bond dims add up; nothing truncated).
+tnfa_net* residual_network(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, Work<double>& x,
+                           double a0, double a1) {
   NetHold xr(store_work(x, TNFA_F64));
   Work<double> ax = apply_exact<double>(ctx, A, xr.p);
   NetHold y(store_work(ax, TNFA_F64));
@@ -1148,10 +1148,20 @@ double residual(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, Work<double
   abi(ctx, tnfa_net_copy(ctx, b, &bneg.p));
   abi(ctx, tnfa_net_scale(ctx, bneg.p, 0, -1.0, 0.0));
   NetHold r1(direct_sum_ext(ctx, y.p, bneg.p));
-  if (a0 == 0.0) return qr_norm(ctx, r1.p) / bnorm;
+  if (a0 == 0.0) {
+    tnfa_net* out = r1.p;
+    r1.p = nullptr;
+    return out;
+  }
   abi(ctx, tnfa_net_scale(ctx, xr.p, 0, a0, 0.0));
-  NetHold r2(direct_sum_ext(ctx, r1.p, xr.p));
-  return qr_norm(ctx, r2.p) / bnorm;
+  return direct_sum_ext(ctx, r1.p, xr.p);
+}
+
+// ||(a0 + a1 A) x - b|| / ||b|| (A, b and x on one layout).
+double residual(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, Work<double>& x, double a0,
+                double a1, double bnorm) {
+  NetHold r(residual_network(ctx, A, b, x, a0, a1));
+  return qr_norm(ctx, r.p) / bnorm;
 }
 
 }  // namespace
@@ -1256,6 +1266,40 @@ tnfa_net* linsolve_path(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, con
   for (int k = 0; k < L; ++k) pos[ord[k]] = k;
   Work<double> wb = relayout<double>(ctx, xp.p->topo, xp.p->d, back, pos);
   return store_work(wb, TNFA_F64);
+}
+
+// linsolve_path followed by iterative refinement on the caller's layout.
+tnfa_net* linsolve_refined(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnfa_net* x0,
+                           const tnfa_linsolve_params& prm, double* rel_res) {
+  double res = 0.0;
+  NetHold x(linsolve_path(ctx, A, b, x0, prm, &res));
+  if (prm.refinements > 0 && res > prm.tol) {
+    const double bnorm = qr_norm(ctx, b);
+    const tnfa_trunc_params tr{prm.refine_cutoff, prm.maxdim, 1, 0, TNFA_PREC_F64};
+    tnfa_linsolve_params pe = prm;
+    pe.refinements = 0;
+    pe.tol = 0.0;
+    for (int k = 0; k < prm.refinements && res > prm.tol; ++k) {
+      // e solves (a0 + a1 A) e = b - (a0 + a1 A) x
+      Work<double> xw = load_work<double>(ctx, x.p);
+      NetHold r(residual_network(ctx, A, b, xw, prm.a0, prm.a1));
+      abi(ctx, tnfa_net_scale(ctx, r.p, 0, -1.0, 0.0));
+      NetHold rt(truncate_net(ctx, r.p, tr));
+      double eres = 0.0;
+      NetHold e(linsolve_path(ctx, A, rt.p, rt.p, pe, &eres));
+      NetHold sum(direct_sum_ext(ctx, x.p, e.p));
+      NetHold xn(truncate_net(ctx, sum.p, tr));
+      Work<double> xnw = load_work<double>(ctx, xn.p);
+      const double rn = residual(ctx, A, b, xnw, prm.a0, prm.a1, bnorm);
+      if (!(rn < res)) break;  // no progress: keep the previous solution
+      std::swap(x.p, xn.p);
+      res = rn;
+    }
+  }
+  if (rel_res) *rel_res = res;
+  tnfa_net* out = x.p;
+  x.p = nullptr;
+  return out;
 }
 
 void inner_product(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, bool conjF, double* out) {
@@ -1378,7 +1422,9 @@ int tnfa_linsolve(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnf
   TNFA_CHECK(params->maxdim >= 0 && params->cutoff >= 0 && params->tol >= 0, TNFA_ERR_INVALID_ARGUMENT,
              "negative linsolve parameter");
   double rr = 0;
-  *x = linsolve_path(ctx, A, b, x0, *params, &rr);
+  TNFA_CHECK(params->refinements >= 0 && params->refine_cutoff >= 0, TNFA_ERR_INVALID_ARGUMENT,
+             "negative refinement parameter");
+  *x = linsolve_refined(ctx, A, b, x0, *params, &rr);
   if (rel_residual) *rel_residual = rr;
   TNFA_API_END
 }

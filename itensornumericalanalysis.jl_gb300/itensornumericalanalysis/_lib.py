@@ -89,6 +89,8 @@ class LinsolveParams(C.Structure):
         ("precision", C.c_int32),
         ("a0", C.c_double),
         ("a1", C.c_double),
+        ("refinements", C.c_int32),
+        ("refine_cutoff", C.c_double),
     ]
 
 

@@ -15,7 +15,8 @@ from .truncation import PRECISIONS
 
 def linsolve(A, b, x0=None, a0: float = 0.0, a1: float = 1.0, nsweeps: int = 10,
              maxdim: int | None = None, cutoff: float = 1e-14, tol: float = 1e-10,
-             krylov_dim: int = 0, precision: str = "f64"):
+             krylov_dim: int = 0, precision: str = "f64", refinements: int = 0,
+             refine_cutoff: float = 1e-28):
     """Solve (a0 + a1 A) x = b for x, A an ITensorNetworkOperator and b an
     ITensorNetworkFunction on the same path-shaped tree (a comb of two
     dimensions is a path).
@@ -27,11 +28,18 @@ def linsolve(A, b, x0=None, a0: float = 0.0, a1: float = 1.0, nsweeps: int = 10,
     ||(a0 + a1 A) x - b|| / ||b|| <= tol; that residual, evaluated exactly in
     FP64, is stored on the result as ``x.rel_residual``.  ``x0`` (default b)
     seeds the sweep.
+
+    ``refinements`` > 0 adds iterative refinement: the residual b - (a0 +
+    a1 A) x is formed exactly, truncated with ``refine_cutoff``, the same
+    sweeps solve for a correction, and x + correction is truncated with
+    ``refine_cutoff`` again -- for ill-conditioned operators (the 1/h^2
+    Laplacian) this recovers the digits the sweep's own truncation loses.
     """
     if x0 is None:
         x0 = b
     p = _lib.LinsolveParams(int(nsweeps), int(maxdim or 0), float(cutoff), float(tol),
-                            int(krylov_dim), PRECISIONS[precision], float(a0), float(a1))
+                            int(krylov_dim), PRECISIONS[precision], float(a0), float(a1),
+                            int(refinements), float(refine_cutoff))
     h = C.c_void_p()
     res = C.c_double(0.0)
     b.ctx.call("tnfa_linsolve", A.handle, b.handle, x0.handle, C.byref(p), C.byref(h),

@@ -99,6 +99,21 @@ def test_poisson_sine_source(ina):
     assert x.maxlinkdim() <= 16
 
 
+def test_refinement_lowers_residual(ina):
+    """Iterative refinement on the 1/h^2 Laplacian (2 x 8 bits): one step takes
+    the residual left by the truncated sweep down by orders of magnitude."""
+    L = 8
+    g = ina.named_comb_tree((2, L))
+    s = ina.continuous_siteinds(g, [[(1, j) for j in range(L, 0, -1)],
+                                    [(2, j) for j in range(1, L + 1)]])
+    b = ina.sin_itn(s, k=np.pi, dim=1) * ina.sin_itn(s, k=np.pi, dim=2)
+    A = ina.laplacian_operator(s)
+    x0 = ina.linsolve(A, b, nsweeps=2, maxdim=24, cutoff=1e-20, tol=0.0)
+    x1 = ina.linsolve(A, b, nsweeps=2, maxdim=24, cutoff=1e-20, tol=0.0, refinements=2)
+    assert x1.rel_residual < 1e-2 * x0.rel_residual, (x0.rel_residual, x1.rel_residual)
+    assert x1.rel_residual < 1e-8
+
+
 def test_maxdim_caps_solution(ina):
     L = 8
     s = ina.continuous_siteinds(ina.named_path_graph(L))
