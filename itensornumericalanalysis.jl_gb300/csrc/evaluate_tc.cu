@@ -86,6 +86,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
       : "memory");
 }
 
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
 // 1024 bytes (SBO), version 1.
 __device__ __forceinline__ uint64_t sw128_desc(const void* base) {
@@ -393,6 +402,255 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Second formulation for a vertex with two children (chi_a in {64, 128},
+// chi2 in {64, 128}): contract the second child first,
+//   Y[p, (a, b)] = sum_c m2[p, c] T_s[a][b][c]           (tensor cores)
+//   out[p, a]    = sum_b m1[p, b] Y[p, (a, b)]            (epilogue, CUDA cores)
+// The A operand is then the m2 rows of the tile -- written to shared memory
+// once (hi and lo BF16, K = chi2) and reused by every MMA -- and B streams
+// T_s as N-tiles of 256 rows (a, b) x 64 columns c through a 3-D TMA box
+// {64 c, 256 / chi_a b, chi_a a}.  Per N-tile the MMA warp issues
+// 3 x 4 x (chi2 / 64) MMAs of M = 128, N = 256 into one of two TMEM buffers
+// (2 x 256 columns); the eight epilogue warps read the other buffer and fold
+// it into per-thread accumulators out[p, a] with m1[p, b].  Compared to the
+// Kronecker formulation this removes the per-chunk A writes (producers ran
+// 32 KB per 6.3 MFLOP through shared memory) and halves the A reads per flop
+// (N = 256), the shared-memory traffic that bounded the tensor pipe at ~60 %.
+//
+// Roles (320 threads): warps 0-7 build A then run the epilogue (thread: row
+// m = 32 (w % 4) + lane, half h = w / 4 of the 256 columns); warp 8 TMA;
+// warp 9 MMA.  Every wait is bounded; a timeout sets an error bit, stops the
+// role's loop and the CTA still releases TMEM.
+constexpr int T2_N = 256;
+
+template <int CHIA, int CHI2>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_contract_tc2(const __grid_constant__ CUtensorMap map_hi,
+                   const __grid_constant__ CUtensorMap map_lo, const TcParams P) {
+  constexpr int NBT = T2_N / CHIA;            // values of b per N-tile
+  constexpr int KCH = CHI2 / TC_KC;           // K chunks per N-tile
+  constexpr int A_CHUNK = TC_M * TC_KC * 2;   // 16 KB: 128 rows x 64 BF16
+  constexpr int A_BYTES = 2 * KCH * A_CHUNK;  // hi and lo, all chunks
+  constexpr int B_BYTES = T2_N * TC_KC * 2;   // 32 KB per chunk and part
+  constexpr int STAGES = 2;
+  constexpr int STAGE_BYTES = 2 * B_BYTES;
+  constexpr int ACC = CHIA / 2;               // accumulators per thread
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], tfull[2], tempty[2],
+      a_ready;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ float rowmax[2][TC_M];
+  __shared__ int sh_abort;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* Asm = smem;
+  unsigned char* Bsm = smem + A_BYTES;
+
+  const int blk = blockIdx.x;
+  const int ng = P.ngroups;
+  if (blk >= P.tile_start[ng]) return;
+  int g = 0;
+  while (g + 1 < ng && P.tile_start[g + 1] <= blk) ++g;
+  const int row0 = P.grp_off[g] + (blk - P.tile_start[g]) * TC_M;
+  const int nrows = min(TC_M, P.grp_off[g] + P.grp_cnt[g] - row0);
+  if (nrows <= 0) return;
+  const int ntiles = P.chi1 / NBT;
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], TC_PRODUCERS);
+    }
+    mbar_init(&a_ready, TC_PRODUCERS);
+    sh_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 8) {  // TMEM: two accumulators of 256 FP32 columns
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_sh)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base_sh;
+
+  if (warp < 8) {
+    // ------------------------------------------- A = m2 rows, then epilogue ----
+    const int m = (warp & 3) * 32 + lane;
+    const int h = warp >> 2;
+    const bool valid = m < nrows;
+    const int p = valid ? (P.perm ? P.perm[row0 + m] : row0 + m) : 0;
+    const float* m2row =
+        P.m2_S ? P.m2_ptr + (int64_t)P.m2_S[p] * CHI2 : P.m2_ptr + (int64_t)p * CHI2;
+    // thread (m, h) writes columns [32h, 32h + 32) of every 64-wide chunk
+#pragma unroll
+    for (int kc = 0; kc < KCH; ++kc) {
+      unsigned char* Ahi = Asm + kc * 2 * A_CHUNK;
+      unsigned char* Alo = Ahi + A_CHUNK;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float x[8];
+        if (valid) {
+          const float4 u = *reinterpret_cast<const float4*>(m2row + kc * 64 + 32 * h + q * 8);
+          const float4 w = *reinterpret_cast<const float4*>(m2row + kc * 64 + 32 * h + q * 8 + 4);
+          x[0] = u.x, x[1] = u.y, x[2] = u.z, x[3] = u.w, x[4] = w.x, x[5] = w.y, x[6] = w.z, x[7] = w.w;
+        } else {
+#pragma unroll
+          for (int t = 0; t < 8; ++t) x[t] = 0.f;
+        }
+        uint32_t hw[4], lw[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          __nv_bfloat162 hh = __floats2bfloat162_rn(x[2 * t], x[2 * t + 1]);
+          float2 hf = __bfloat1622float2(hh);
+          hw[t] = *reinterpret_cast<uint32_t*>(&hh);
+          lw[t] = pack_bf16(x[2 * t] - hf.x, x[2 * t + 1] - hf.y);
+        }
+        const int chunk = (4 * h + q) ^ (m & 7);
+        const int off = m * 128 + chunk * 16;
+        *reinterpret_cast<uint4*>(Ahi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *reinterpret_cast<uint4*>(Alo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+      }
+    }
+    fence_proxy_async();
+    mbar_arrive(&a_ready);
+
+    const float* m1row =
+        P.m1_S ? P.m1_ptr + (int64_t)P.m1_S[p] * P.chi1 : P.m1_ptr + (int64_t)p * P.chi1;
+    const int e_in = valid ? ((P.m1_exp ? P.m1_exp[p] : 0) + (P.m2_exp ? P.m2_exp[p] : 0)) : 0;
+    float acc[ACC];
+#pragma unroll
+    for (int i = 0; i < ACC; ++i) acc[i] = 0.f;
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    bool ok = true;
+    float mb[NBT], mbn[NBT];
+#pragma unroll
+    for (int i = 0; i < NBT; ++i) mbn[i] = valid ? m1row[i] : 0.f;
+    for (int t = 0; t < ntiles; ++t) {
+#pragma unroll
+      for (int i = 0; i < NBT; ++i) mb[i] = mbn[i];
+      if (t + 1 < ntiles) {
+#pragma unroll
+        for (int i = 0; i < NBT; ++i) mbn[i] = valid ? m1row[(t + 1) * NBT + i] : 0.f;
+      }
+      const int buf = t & 1;
+      if (!mbar_wait(&tfull[buf], (t >> 1) & 1)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        float v[32];
+        tmem_ld32(tmem + lane_base + (uint32_t)(buf * T2_N + h * 128 + cc * 32), v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int jl = cc * 32 + j;  // column within this half
+          acc[jl / NBT] = fmaf(v[j], mb[jl % NBT], acc[jl / NBT]);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(&tempty[buf]);
+    }
+    if (!ok) {
+      atomicOr(P.err, TC_ERR_TIMEOUT);
+      sh_abort = 1;
+    }
+    // power-of-two row normalisation across both halves, then store
+    float mx = 0.f;
+#pragma unroll
+    for (int i = 0; i < ACC; ++i) mx = fmaxf(mx, fabsf(acc[i]));
+    rowmax[h][m] = mx;
+    asm volatile("bar.sync 1, 256;" ::: "memory");
+    mx = fmaxf(rowmax[0][m], rowmax[1][m]);
+    int ex = 0;
+    if (mx > 0.f) frexpf(mx, &ex);
+    if (valid && ok) {
+      float* dst = P.out + (int64_t)p * CHIA + h * ACC;
+#pragma unroll
+      for (int i = 0; i < ACC; i += 4)
+        *reinterpret_cast<float4*>(dst + i) = make_float4(
+            scalbnf(acc[i], -ex), scalbnf(acc[i + 1], -ex), scalbnf(acc[i + 2], -ex), scalbnf(acc[i + 3], -ex));
+      if (h == 0) P.out_exp[p] = e_in + ex;
+    }
+  } else if (warp == 8) {
+    // ------------------------------------------------------------ TMA ----
+    if (lane == 0) {
+      bool ok = true;
+      const int nst = ntiles * KCH;
+      for (int si = 0; si < nst; ++si) {
+        const int s = si % STAGES, use = si / STAGES;
+        if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        unsigned char* Bhi = Bsm + s * STAGE_BYTES;
+        unsigned char* Blo = Bhi + B_BYTES;
+        const int t = si / KCH, kc = si % KCH;
+        mbar_arrive_expect_tx(&full_bar[s], 2 * B_BYTES);
+        tma_load_3d(Bhi, &map_hi, &full_bar[s], kc * TC_KC, t * NBT, g * CHIA);
+        tma_load_3d(Blo, &map_lo, &full_bar[s], kc * TC_KC, t * NBT, g * CHIA);
+      }
+      if (!ok) atomicOr(P.err, TC_ERR_TIMEOUT);
+    }
+  } else {
+    // ------------------------------------------------------------ MMA ----
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16(TC_M, T2_N);
+      bool ok = mbar_wait(&a_ready, 0);
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int t = 0; t < ntiles && ok; ++t) {
+        const int buf = t & 1;
+        if (t >= 2 && !mbar_wait(&tempty[buf], ((t >> 1) - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t dcol = tmem + (uint32_t)(buf * T2_N);
+        for (int kc = 0; kc < KCH; ++kc) {
+          const int si = t * KCH + kc;
+          const int s = si % STAGES, use = si / STAGES;
+          if (!mbar_wait(&full_bar[s], use & 1)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          unsigned char* Ahi = Asm + kc * 2 * A_CHUNK;
+          unsigned char* Alo = Ahi + A_CHUNK;
+          unsigned char* Bhi = Bsm + s * STAGE_BYTES;
+          unsigned char* Blo = Bhi + B_BYTES;
+          const uint64_t dah = sw128_desc(Ahi), dal = sw128_desc(Alo);
+          const uint64_t dbh = sw128_desc(Bhi), dbl = sw128_desc(Blo);
+#pragma unroll
+          for (int k = 0; k < TC_KC / 16; ++k) {
+            const uint64_t adv = (uint64_t)(k * 32) >> 4;
+            mma_bf16(dcol, dah + adv, dbh + adv, idesc, (kc | k) != 0);
+            mma_bf16(dcol, dah + adv, dbl + adv, idesc, 1);
+            mma_bf16(dcol, dal + adv, dbh + adv, idesc, 1);
+          }
+          mma_commit(&empty_bar[s]);
+        }
+        if (ok) mma_commit(&tfull[buf]);
+      }
+      if (!ok) atomicOr(P.err, TC_ERR_TIMEOUT);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 8) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  }
+}
+
 // BF16 hi / lo split of the FP32 tensors, per-vertex offsets padded to 64
 // elements so every vertex base is 128-byte aligned for TMA.
 __global__ void k_split_bf16(const float* __restrict__ src, __nv_bfloat16* __restrict__ hi,
@@ -439,6 +697,35 @@ CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int box_rows) {
   TNFA_CHECK(r == CUDA_SUCCESS, TNFA_ERR_CUDA,
              "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
   return m;
+}
+
+// 3-D map of one vertex's slice stack T[s][a][b][c] (BF16): dims {chi2,
+// chi1, S * chi_a}, box {64, 256 / chi_a, chi_a}.
+CUtensorMap make_map3(const void* base, int chi2, int chi1, int64_t sa, int box_b, int box_a) {
+  auto enc = get_encode();
+  TNFA_CHECK(enc != nullptr, TNFA_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  CUtensorMap m;
+  cuuint64_t dims[3] = {(cuuint64_t)chi2, (cuuint64_t)chi1, (cuuint64_t)sa};
+  cuuint64_t strides[2] = {(cuuint64_t)chi2 * 2, (cuuint64_t)chi2 * chi1 * 2};
+  cuuint32_t box[3] = {(cuuint32_t)TC_KC, (cuuint32_t)box_b, (cuuint32_t)box_a};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides,
+                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  TNFA_CHECK(r == CUDA_SUCCESS, TNFA_ERR_CUDA,
+             "cuTensorMapEncodeTiled (3-D) failed with code " + std::to_string((int)r));
+  return m;
+}
+
+template <int CHIA, int CHI2>
+void launch_tc2(tnfa_ctx* ctx, const CUtensorMap& mh, const CUtensorMap& ml, const TcParams& p,
+                unsigned grid) {
+  constexpr int KCH = CHI2 / TC_KC;
+  const int smem = 2 * KCH * TC_M * TC_KC * 2 + 2 * 2 * T2_N * TC_KC * 2 + 1024;
+  TNFA_CUDA(cudaFuncSetAttribute(k_contract_tc2<CHIA, CHI2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem));
+  k_contract_tc2<CHIA, CHI2><<<grid, TC_THREADS, smem, ctx->stream>>>(mh, ml, p);
+  TNFA_LAUNCH_CHECK();
 }
 
 template <int N, int CHI2, int STAGES, bool BILIN>
@@ -539,6 +826,18 @@ void tc_contract_vertex(tnfa_ctx* ctx, const tnfa_net* net, int v, const VertexJ
   KernelScope ks(ctx, "contract_tc", 2.0 * j.Pc * (double)j.K * j.chi_a,
                  4.0 * ((double)j.Pc * (p.chi1 + p.chi2 + j.chi_a)) +
                      4.0 * j.site_dim * (double)j.chi_a * j.K);
+  // two children: contract the second child first (k_contract_tc2) unless
+  // TNFA_TC_KRON selects the Kronecker formulation
+  static const bool kron = getenv("TNFA_TC_KRON") && *getenv("TNFA_TC_KRON") == '1';
+  if (!bilin && !kron && j.nchild == 2 && p.chi1 % (T2_N / N) == 0) {
+    const int nbt = T2_N / N;
+    CUtensorMap h3 = make_map3(hi, p.chi2, p.chi1, (int64_t)j.site_dim * N, nbt, N);
+    CUtensorMap l3 = make_map3(lo, p.chi2, p.chi1, (int64_t)j.site_dim * N, nbt, N);
+    if (N == 128 && p.chi2 == 128) return launch_tc2<128, 128>(ctx, h3, l3, p, grid);
+    if (N == 128 && p.chi2 == 64) return launch_tc2<128, 64>(ctx, h3, l3, p, grid);
+    if (N == 64 && p.chi2 == 128) return launch_tc2<64, 128>(ctx, h3, l3, p, grid);
+    if (N == 64 && p.chi2 == 64) return launch_tc2<64, 64>(ctx, h3, l3, p, grid);
+  }
   if (!bilin) {
     if (N == 128 && p.chi2 == 128) launch_tc<128, 128, 3, false>(ctx, mh, ml, p, grid);
     else if (N == 128 && p.chi2 == 64) launch_tc<128, 64, 3, false>(ctx, mh, ml, p, grid);
