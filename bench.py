@@ -431,12 +431,17 @@ def main():
         st = stats[fam]
         tc = fam == "contract_tc"
         achieved = st["flops"] / (st["ms"] / 1e3) / 1e12
-        peak = peaks["bf16_tflops"]
+        # the kernel runs back to back for the whole ~2 s step, under the power
+        # cap: the sustained cuBLAS figure is the denominator; burst beside it
+        peak = peaks["bf16_tflops_sustained"]
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": None, "kernel": fam,
                 "kernel_share": st["ms"] / sum(v["ms"] for v in stats.values()),
-                "peak_source": "MEASURED_PEAKS.json bf16 burst" if "fallback" not in peaks
-                else "fallback", "split_passes_not_counted": 3 if tc else 1}
+                "peak_source": ("MEASURED_PEAKS.json bf16 sustained (kernel timed inside a long step)"
+                                if "fallback" not in peaks else "fallback"),
+                "frac_of_burst_peak": achieved / peaks["bf16_tflops"],
+                "split_passes_not_counted": 3 if tc else 1,
+                "tensor_work_with_split_passes": achieved * (3 if tc else 1)}
     launches = sum(v["launches"] for v in stats.values()) // args.steps
 
     # end to end: pinned host X -> device -> result back, through the C ABI
