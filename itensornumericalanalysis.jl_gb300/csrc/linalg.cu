@@ -1037,6 +1037,10 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     if (!tall[q]) adj.push_back({R[q].p, J[q].p, n[q], n[q], n[q], n[q], 1, 1});
   copy_blocks<T, T>(ctx, adj);
   const JacobiOpts opts{1e-10, cutoff > 0 ? cutoff * 1e-2 : 0.0};
+  // the polish starts from FP32-converged columns (offsets ~1e-7), already in
+  // the quadratic regime: the sweep whose rotations were all below 1e-6
+  // leaves ~1e-12, so it is the last one
+  const JacobiOpts polish{1e-6, opts.small_rel};
   // (2) Jacobi on the core: U (cm x ku); extra[q] = weight outside U's span
   std::vector<double> extra(nj, 0.0);
   std::vector<SvdJob> sj;
@@ -1089,7 +1093,9 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
         s32.push_back({C32[q].p, U32[q].p, S32[q].as<double>(), V32[q].p, m, k, sw32[q].as<int>()});
       }
       copy_blocks<double, float>(ctx, down);
-      jacobi<float>(ctx, s32, 60, JacobiOpts{0.0, opts.small_rel}, "svd_f32");
+      // pass 1 only has to split kept from dropped directions and hand pass 2
+      // a nearly diagonal start: stop at 1e-4; pass 2 runs to FP32 accuracy
+      jacobi<float>(ctx, s32, 60, JacobiOpts{pass == 0 ? 1e-4 : 0.0, opts.small_rel}, "svd_f32");
       if (pass == 0) {
         // keep the FP32 directions that a 10^6 times smaller cutoff would
         // keep (all of them without a cutoff).  What pass 1 drops cannot be
@@ -1161,7 +1167,7 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
       S[q] = DBuf(ctx, (size_t)ku[q] * sizeof(double));
       sj.push_back({X[q].p, U[q].p, S[q].as<double>(), nullptr, cm[q], ku[q], sw[q].as<int>()});
     }
-    jacobi<T>(ctx, sj, 60, opts, "svd_polish_f64");
+    jacobi<T>(ctx, sj, 60, polish, "svd_polish_f64");
   }
   // (3) ranks on the host
   for (size_t q = 0; q < nj; ++q) {
