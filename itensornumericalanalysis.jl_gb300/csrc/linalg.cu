@@ -1168,6 +1168,33 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
       sj.push_back({X[q].p, U[q].p, S[q].as<double>(), nullptr, cm[q], ku[q], sw[q].as<int>()});
     }
     jacobi<T>(ctx, sj, 60, polish, "svd_polish_f64");
+    // Diagnostics (TNFA_DEBUG_DIR with TNFA_DEBUG_SWEEPS=k): the FP64 core of
+    // every mixed job whose polish took k sweeps or more, with its polish input
+    static const char* dbg = getenv("TNFA_DEBUG_DIR");
+    static const int thr = getenv("TNFA_DEBUG_SWEEPS") ? atoi(getenv("TNFA_DEBUG_SWEEPS")) : 0;
+    if (dbg && *dbg && thr > 0) {
+      static int counter = 0;
+      for (size_t q = 0; q < nj && counter < 32; ++q) {
+        int swq = 0;
+        TNFA_CUDA(cudaMemcpyAsync(&swq, sw[q].p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (swq >= 0 && swq < thr) continue;
+        const int m = cm[q], k = n[q], c = ku[q];
+        std::vector<double> hc((size_t)m * k), hx((size_t)m * c);
+        TNFA_CUDA(cudaMemcpyAsync(hc.data(), core[q], hc.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        TNFA_CUDA(cudaMemcpyAsync(hx.data(), X[q].p, hx.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+        char path[1024];
+        snprintf(path, sizeof path, "%s/mixed_core_%d.bin", dbg, counter++);
+        if (FILE* fp = fopen(path, "wb")) {
+          int hdr[4] = {m, k, c, swq};
+          fwrite(hdr, sizeof(int), 4, fp);
+          fwrite(hc.data(), 8, hc.size(), fp);
+          fwrite(hx.data(), 8, hx.size(), fp);
+          fclose(fp);
+        }
+      }
+    }
   }
   // (3) ranks on the host
   for (size_t q = 0; q < nj; ++q) {
