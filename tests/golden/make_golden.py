@@ -113,9 +113,49 @@ def complex_fixture():
     np.savez_compressed(HERE / "complex_cosh_comb2x3.npz", Z=Z, values=vals, k=k, a=a, c=c)
 
 
+def _pack(flat, shapes):
+    return np.concatenate(flat), np.array([np.pad(sh, (0, 5 - len(sh)), constant_values=0) for sh in shapes])
+
+
+def partial_fixture():
+    """A random 3-variable comb (3, 3), chi 3, digits round robin; the dense
+    left Riemann sums over subsets of the variables (src/integration.jl:35-54)."""
+    from itensornumericalanalysis.graphs import named_comb_tree
+    g = named_comb_tree((3, 3))
+    s, flat, shapes = canonical_random(g, 3, 3, seed=104)
+    net = to_oracle(s, flat, shapes, O.comb_tree_graph((3, 3)))
+    so = net.s
+    order = sorted((i for v in so.verts for i in so.site[v]), key=lambda i: so.info[i][:2])
+    F = O.dense(net, order).reshape(8, 8, 8)
+    t, sh = _pack(flat, shapes)
+    np.savez_compressed(HERE / "partial_comb3x3_chi3.npz", tensors=t, shapes=sh,
+                        p2=F.mean(axis=1), p23=F.mean(axis=(1, 2)), p13=F.mean(axis=(0, 2)),
+                        p1_sum=F.sum(axis=0))
+
+
+def linsolve_fixture(L=9):
+    """d2/dx2 x = b on a 9-bit path (Dirichlet, scaled), b random with bond 2:
+    the dense FP64 solution with the oracle's stencil matrix."""
+    from itensornumericalanalysis.graphs import named_grid
+    g = named_grid((L, 1))
+    s, flat, shapes = canonical_random(g, 1, 2, seed=105)
+    net = to_oracle(s, flat, shapes, O.path_graph(L))
+    B, _ = O.dense_grid_1d(net)
+    N = 2**L
+    eye = np.eye(N).reshape((2,) * L + (N,))
+    M = O.apply_terms_dense(O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2), eye,
+                            {(1, k): k - 1 for k in range(1, L + 1)}).reshape(N, N)
+    x = np.linalg.solve(M, B.real)
+    t, sh = _pack(flat, shapes)
+    np.savez_compressed(HERE / f"linsolve_path{L}.npz", tensors=t, shapes=sh, b_grid=B.real, x_grid=x,
+                        cond=np.linalg.cond(M))
+
+
 if __name__ == "__main__":
     random_tree_fixture()
     config1_fixture()
     shift_fixture()
     complex_fixture()
+    partial_fixture()
+    linsolve_fixture()
     print("fixtures written to", HERE)

@@ -53,3 +53,44 @@ def test_complex_fixture_matches_analytic():
     # the digit map truncates each part to 3 binary digits
     zq = np.floor(Z.real * 8) / 8 + 1j * np.floor(Z.imag * 8) / 8
     assert np.allclose(d["values"], c * np.cosh(k * zq + a), rtol=1e-12)
+
+
+def _fixture_tensors(d, s):
+    flat, ts, off = d["tensors"], {}, 0
+    for v, sh in zip(s.layout.order, d["shapes"]):
+        sh = tuple(int(x) for x in sh if x > 0)
+        n = int(np.prod(sh))
+        ts[v] = flat[off:off + n].reshape(sh)
+        off += n
+    return ts
+
+
+def test_partial_fixture_is_oracle_output():
+    import sys
+    sys.path.insert(0, str(G))
+    from make_golden import to_oracle
+    from itensornumericalanalysis.graphs import named_comb_tree
+    from itensornumericalanalysis.indexmap import continuous_siteinds
+    d = np.load(G / "partial_comb3x3_chi3.npz")
+    s = continuous_siteinds(named_comb_tree((3, 3)), map_dimension=3)
+    ts = _fixture_tensors(d, s)
+    shapes = [ts[v].shape for v in s.layout.order]
+    net = to_oracle(s, [ts[v].ravel() for v in s.layout.order], shapes, O.comb_tree_graph((3, 3)))
+    so = net.s
+    order = sorted((i for v in so.verts for i in so.site[v]), key=lambda i: so.info[i][:2])
+    F = O.dense(net, order).reshape(8, 8, 8)
+    assert np.allclose(F.mean(axis=1), d["p2"], atol=1e-14)
+    # the fixtures are consistent with each other
+    assert np.allclose(d["p2"].mean(axis=1), d["p23"], atol=1e-14)
+    assert np.allclose(d["p1_sum"] / 8, F.mean(axis=0), atol=1e-14)
+
+
+def test_linsolve_fixture_solves_the_stencil():
+    d = np.load(G / "linsolve_path9.npz")
+    L = 9
+    N = 2**L
+    x = d["x_grid"]
+    # (x[i+1] - 2 x[i] + x[i-1]) 4^L = b[i], Dirichlet zeros outside the grid
+    xp = np.concatenate([[0.0], x, [0.0]])
+    lap = (xp[2:] - 2 * xp[1:-1] + xp[:-2]) * 4.0**L
+    assert np.max(np.abs(lap - d["b_grid"])) <= 1e-9 * np.max(np.abs(d["b_grid"]))

@@ -64,3 +64,41 @@ def test_complex_fixture(ina):
     f = ina.cosh_itn(s, k=complex(d["k"]), a=complex(d["a"]), c=complex(d["c"]))
     got = f.evaluate_batch(d["Z"].reshape(-1, 1))
     assert np.max(np.abs(got - d["values"])) <= 1e-12 * np.max(np.abs(d["values"]))
+
+
+def _fixture_net(ina, d, s):
+    flat, ts, off = d["tensors"], {}, 0
+    for v, sh in zip(s.layout.order, d["shapes"]):
+        sh = tuple(int(x) for x in sh if x > 0)
+        n = int(np.prod(sh))
+        ts[v] = flat[off:off + n].reshape(sh)
+        off += n
+    return ina.ITensorNetworkFunction.from_tensors(s, ts)
+
+
+def test_partial_fixture(ina):
+    d = np.load(G / "partial_comb3x3_chi3.npz")
+    s = ina.continuous_siteinds(ina.named_comb_tree((3, 3)), map_dimension=3)
+    f = _fixture_net(ina, d, s)
+    g = np.arange(8) / 8.0
+    mesh = lambda k: np.stack(np.meshgrid(*([g] * k), indexing="ij"), axis=-1).reshape(-1, k)
+    cases = [([2], [1, 3], d["p2"], False), ([2, 3], [1], d["p23"], False),
+             ([1, 3], [2], d["p13"], False), ([1], [2, 3], d["p1_sum"], True)]
+    for dims, keep, ref, take_sum in cases:
+        h = ina.partial_integrate(f, dims, take_sum=take_sum)
+        got = h.evaluate_batch(mesh(len(keep)), keep)
+        assert np.max(np.abs(got - ref.reshape(-1))) <= 1e-12 * np.max(np.abs(ref)), dims
+
+
+def test_linsolve_fixture(ina):
+    d = np.load(G / "linsolve_path9.npz")
+    L = 9
+    s = ina.continuous_siteinds(ina.named_grid((L, 1)))
+    b = _fixture_net(ina, d, s)
+    xs = np.arange(2**L) / 2.0**L
+    assert np.max(np.abs(b.evaluate_batch(xs) - d["b_grid"])) <= 1e-12 * np.max(np.abs(d["b_grid"]))
+    x = ina.linsolve(ina.second_derivative_operator(s), b, nsweeps=4, cutoff=0.0, tol=1e-13)
+    ref = d["x_grid"]
+    # forward error <= cond * residual; cond ~ 1e5 here
+    assert np.max(np.abs(x.evaluate_batch(xs) - ref)) <= 1e-9 * np.max(np.abs(ref))
+    assert x.rel_residual < 1e-12
