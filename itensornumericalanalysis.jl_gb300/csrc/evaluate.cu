@@ -1006,45 +1006,30 @@ __device__ inline void atomic_add_T<cplx>(cplx* a, cplx v) {
   atomicAdd(&a->im, v.im);
 }
 
-// Each CTA walks `tpc` consecutive tiles (a tile: TP points of one site
-// value) for a 256-wide block of K and keeps its sums in registers, flushing
-// them with one atomic per K entry whenever the site value changes and at the
-// end: the atomics per entry drop from one per 64 points to one per
-// tpc * 64 points.
 template <class T, int TP>
-__global__ void __launch_bounds__(256) k_grad_acc(const VertexJob<T> j, T* __restrict__ dT, int tpc) {
+__global__ void __launch_bounds__(256) k_grad_acc(const VertexJob<T> j, T* __restrict__ dT) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  int row0, nrows, g;
+  if (!locate_tile(j, TP, blockIdx.x, row0, nrows, g)) return;
   int sumdim = 0;
   for (int c = 0; c < j.nchild; ++c) sumdim += j.ch[c].dim;
   T* rows = (T*)smem_raw;
   T* scale = rows + (int64_t)sumdim * TP;
   int* pts = (int*)(scale + TP);
   int* eacc = pts + TP;
-  const int k = blockIdx.y * blockDim.x + threadIdx.x;
-  T acc = Sc<T>::zero();
-  int gcur = -1;
-  for (int tt = 0; tt < tpc; ++tt) {
-    int row0, nrows, g;
-    // uniform across the CTA: every thread sees the same tile
-    if (!locate_tile(j, TP, blockIdx.x * tpc + tt, row0, nrows, g)) continue;
-    if (g != gcur) {
-      if (gcur >= 0 && k < j.K) atomic_add_T<T>(dT + (int64_t)gcur * j.K + k, acc);
-      acc = Sc<T>::zero();
-      gcur = g;
-    }
-    __syncthreads();  // the previous tile's rows are no longer read
-    for (int r = threadIdx.x; r < TP; r += blockDim.x) {
-      pts[r] = r < nrows ? (j.perm ? j.perm[row0 + r] : row0 + r) : 0;
-      eacc[r] = 0;
-    }
-    __syncthreads();
-    load_children(j, pts, nrows, TP, rows, eacc);
-    for (int r = threadIdx.x; r < nrows; r += blockDim.x) scale[r] = Sc<T>::scale2(Sc<T>::one(), eacc[r]);
-    __syncthreads();
-    if (k < j.K)
-      for (int r = 0; r < nrows; ++r) acc = Sc<T>::fma(scale[r], kr_entry(j, rows, TP, r, k), acc);
+  for (int r = threadIdx.x; r < TP; r += blockDim.x) {
+    pts[r] = r < nrows ? (j.perm ? j.perm[row0 + r] : row0 + r) : 0;
+    eacc[r] = 0;
   }
-  if (gcur >= 0 && k < j.K) atomic_add_T<T>(dT + (int64_t)gcur * j.K + k, acc);
+  __syncthreads();
+  load_children(j, pts, nrows, TP, rows, eacc);
+  for (int r = threadIdx.x; r < nrows; r += blockDim.x) scale[r] = Sc<T>::scale2(Sc<T>::one(), eacc[r]);
+  __syncthreads();
+  const int k = blockIdx.y * blockDim.x + threadIdx.x;
+  if (k >= j.K) return;
+  T acc = Sc<T>::zero();
+  for (int r = 0; r < nrows; ++r) acc = Sc<T>::fma(scale[r], kr_entry(j, rows, TP, r, k), acc);
+  atomic_add_T<T>(dT + (int64_t)g * j.K + k, acc);
 }
 
 template <class T>
@@ -1284,14 +1269,9 @@ void vjp_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, const double
       if (sm > 48 * 1024)
         TNFA_CUDA(cudaFuncSetAttribute(k_grad_acc<T, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sm));
-      const int64_t ntiles = (Pc + TP - 1) / TP + j.ngroups;
-      const int64_t kblocks = (K + 255) / 256;
-      // about eight CTAs per SM in total
-      const int64_t want = std::max<int64_t>(1, 8 * (int64_t)ctx->sm_count / kblocks);
-      const int tpc = (int)std::max<int64_t>(1, (ntiles + want - 1) / want);
-      dim3 grid((unsigned)((ntiles + tpc - 1) / tpc), (unsigned)kblocks);
+      dim3 grid((unsigned)((Pc + TP - 1) / TP + j.ngroups), (unsigned)((K + 255) / 256));
       KernelScope ks(ctx, "grad_acc", 2.0 * Pc * (double)K, 0.0);
-      k_grad_acc<T, TP><<<grid, 256, sm, ctx->stream>>>(j, dT + Tp.off[v], tpc);
+      k_grad_acc<T, TP><<<grid, 256, sm, ctx->stream>>>(j, dT + Tp.off[v]);
       TNFA_LAUNCH_CHECK();
     }
   }
