@@ -358,8 +358,15 @@ template <class T>
 void qr(tnfa_ctx* ctx, const std::vector<QrJob>& jobs) {
   if (jobs.empty()) return;
   std::vector<QrJob> big, small;
+  // clusters for large factorisations, and for every job of at least 32
+  // columns when the batch is too small to fill the GPU (see svd_big)
+  const bool few = jobs.size() * 8 <= (size_t)ctx->sm_count;
   for (const auto& j : jobs)
-    ((double)j.m * j.n * std::min(j.m, j.n) >= 4.0e6 && std::min(j.m, j.n) >= 64 ? big : small).push_back(j);
+    (((double)j.m * j.n * std::min(j.m, j.n) >= 4.0e6 && std::min(j.m, j.n) >= 64) ||
+             (few && std::min(j.m, j.n) >= 32)
+         ? big
+         : small)
+        .push_back(j);
   for (int pass = 0; pass < 2; ++pass) {
     const std::vector<QrJob>& js = pass == 0 ? big : small;
     if (js.empty()) continue;
@@ -646,8 +653,13 @@ __global__ void __launch_bounds__(512) k_jacobi(const SvdJob* __restrict__ jobs,
 constexpr int SVD_CLUSTER = 8;  // CTAs (SMs) per large matrix
 
 // A job goes to the cluster kernel when its Jacobi work is large enough to
-// pay for a cluster barrier per round.
-inline bool svd_big(const SvdJob& j) { return j.n >= 96 && (double)j.m * j.n * j.n >= 2.0e6; }
+// pay for a cluster barrier per round -- or, in a batch too small to fill the
+// GPU with one CTA per job (the tail of an uneven batch), when it has enough
+// column pairs to share between the CTAs of a cluster.
+inline bool svd_big(const SvdJob& j, size_t njobs, int sms) {
+  if (j.n >= 96 && (double)j.m * j.n * j.n >= 2.0e6) return true;
+  return njobs * 8 <= (size_t)sms && j.n >= 32;
+}
 
 template <class T, bool CL, int MAXR>
 void launch_jacobi(tnfa_ctx* ctx, const SvdJob* d, T* work, const int64_t* woff, int* flags, int njobs,
@@ -679,7 +691,7 @@ template <class T>
 void jacobi(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, JacobiOpts stop_rel,
             const char* family) {
   std::vector<SvdJob> big, small;
-  for (const auto& j : jobs) (svd_big(j) ? big : small).push_back(j);
+  for (const auto& j : jobs) (svd_big(j, jobs.size(), ctx->sm_count) ? big : small).push_back(j);
   for (int pass = 0; pass < 2; ++pass) {
     const std::vector<SvdJob>& js = pass == 0 ? big : small;
     if (js.empty()) continue;
