@@ -72,6 +72,7 @@ from .integration import integrate, partial_integrate
 from .network import ITensorNetworkFunction, calculate_fx, evaluate, inner
 from .operate import operate, operate_batched
 from .solvers import linsolve
+from .tci import interpolate
 from .truncation import truncate, truncate_batched
 
 __version__ = "0.1.0"

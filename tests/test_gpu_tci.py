@@ -1,0 +1,36 @@
+"""Tensor cross interpolation into device networks
+(ext/ITensorNumericalAnalysisTCIExt/tci_util.jl:21-55)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_interpolate_1d(ina):
+    s = ina.continuous_siteinds(ina.named_path_graph(20))
+    f = lambda X: np.exp(-X[:, 0]) * np.sin(20 * X[:, 0]) + X[:, 0] ** 2
+    g = ina.interpolate(f, s, tol=1e-12, maxbonddim=32)
+    X = np.random.default_rng(0).random((4000, 1))
+    assert np.max(np.abs(g.evaluate_batch(X) - f(X))) < 1e-9
+    assert g.maxlinkdim() <= 12
+
+
+def test_interpolate_2d_comb(ina):
+    L = 10
+    s = ina.continuous_siteinds(ina.named_comb_tree((2, L)),
+                                [[(1, j) for j in range(L, 0, -1)], [(2, j) for j in range(1, L + 1)]])
+    f = lambda X: np.cos(3 * X[:, 0] + 2 * X[:, 1])
+    g = ina.interpolate(f, s, tol=1e-12, maxbonddim=16)
+    X = np.random.default_rng(1).random((4000, 2))
+    assert np.max(np.abs(g.evaluate_batch(X, [1, 2]) - f(X))) < 1e-9
+
+
+def test_interpolate_a_network(ina):
+    """A device network as the black box: the interpolant reproduces it with
+    the same bond dimension (exp + sin has QTT rank 3)."""
+    s = ina.continuous_siteinds(ina.named_path_graph(16))
+    h = ina.exp_itn(s, k=-1.0) + ina.sin_itn(s, k=2 * np.pi)
+    g = ina.interpolate(h, s, tol=1e-13)
+    X = np.random.default_rng(2).random((2000, 1))
+    assert np.max(np.abs(g.evaluate_batch(X) - h.evaluate_batch(X))) < 1e-10
+    assert g.maxlinkdim() <= 3
