@@ -53,3 +53,44 @@ def test_tci_exact_low_rank_2d():
     idx = np.random.default_rng(3).integers(0, 2, (1000, 2 * L))
     assert np.max(np.abs(_mps_values(cores, idx) - sample(idx))) < 1e-10
     assert info["ranks"][L - 1] == 2
+
+
+def test_interpolate_layout_through_the_oracle(monkeypatch):
+    """interpolate() hands the device layout [site, parent, children] to the
+    library; intercept it and contract those tensors with the oracle."""
+    import itensornumericalanalysis as ina
+    from itensornumericalanalysis.network import ITensorNetworkFunction
+
+    captured = {}
+
+    def fake_from_tensors(cls, s, ts, ctx=None, legs=None, dtype=None):
+        captured["s"], captured["ts"] = s, ts
+
+        class Dummy:
+            pass
+        return Dummy()
+
+    monkeypatch.setattr(ITensorNetworkFunction, "from_tensors", classmethod(fake_from_tensors))
+    L = 6
+    g = ina.named_comb_tree((2, L))
+    s = ina.continuous_siteinds(g, [[(1, j) for j in range(L, 0, -1)], [(2, j) for j in range(1, L + 1)]])
+    f = lambda X: np.exp(X[:, 0] - 2 * X[:, 1]) + X[:, 0] * X[:, 1]
+    ina.interpolate(f, s, tol=1e-13)
+    ts = captured["ts"]
+    lay = s.layout
+    X = np.random.default_rng(4).random((50, 2))
+    X = np.floor(X * 2**L) / 2**L  # grid points: the interpolant is exact there
+
+    def value(x):
+        iv = s.calculate_ind_values([x[0], x[1]], [1, 2])
+
+        def up(i):  # vector over vertex i's parent bond
+            v = lay.order[i]
+            T = ts[v][iv[s.legs[v][0]]]  # [parent, children...]
+            for c in reversed(lay.children[i]):
+                T = T @ up(c)
+            return T
+        return float(up(0)[0])
+
+    got = np.array([value(x) for x in X])
+    assert np.max(np.abs(got - f(X))) < 1e-11
