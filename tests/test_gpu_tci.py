@@ -10,7 +10,8 @@ def test_interpolate_1d(ina):
     s = ina.continuous_siteinds(ina.named_path_graph(20))
     f = lambda X: np.exp(-X[:, 0]) * np.sin(20 * X[:, 0]) + X[:, 0] ** 2
     g = ina.interpolate(f, s, tol=1e-12, maxbonddim=32)
-    X = np.random.default_rng(0).random((4000, 1))
+    # compare on grid points: the network holds f on the 2^20 digit grid
+    X = np.floor(np.random.default_rng(0).random((4000, 1)) * 2**20) / 2**20
     assert np.max(np.abs(g.evaluate_batch(X) - f(X))) < 1e-9
     assert g.maxlinkdim() <= 12
 
@@ -21,7 +22,7 @@ def test_interpolate_2d_comb(ina):
                                 [[(1, j) for j in range(L, 0, -1)], [(2, j) for j in range(1, L + 1)]])
     f = lambda X: np.cos(3 * X[:, 0] + 2 * X[:, 1])
     g = ina.interpolate(f, s, tol=1e-12, maxbonddim=16)
-    X = np.random.default_rng(1).random((4000, 2))
+    X = np.floor(np.random.default_rng(1).random((4000, 2)) * 2**L) / 2**L
     assert np.max(np.abs(g.evaluate_batch(X, [1, 2]) - f(X))) < 1e-9
 
 
