@@ -292,6 +292,24 @@ typedef struct {
 int tnfa_linsolve(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnfa_net* x0,
                   const tnfa_linsolve_params* params, tnfa_net** x, double* rel_residual);
 
+typedef struct {
+  int32_t nsweeps;      /* maximum number of sweeps                               */
+  int32_t maxdim;       /* bond cap of the state                                  */
+  double cutoff;        /* truncation of the two-site updates                     */
+  double tol;           /* stop when the energy changes by <= tol (relative)     */
+  int32_t krylov_dim;   /* Lanczos vectors per restart (0: 30)                    */
+  int32_t restarts;     /* Lanczos restarts per two-site update                   */
+} tnfa_dmrg_params;
+
+/* Lowest eigenpair of a symmetric operator H on a path-shaped tree by two-site
+ * DMRG sweeps: the two-site operator is assembled densely on the device,
+ * Lanczos (full re-orthogonalisation, restarts) finds its lowest eigenvector,
+ * a truncated SVD splits it, and the state is kept normalised.  Replaces
+ * ITensorNetworks.dmrg as called by examples/2d_laplace_solver.jl:33-34
+ * (nsites = 2, normalize = true).  energy receives the final eigenvalue. */
+int tnfa_dmrg(tnfa_ctx* ctx, const tnfa_net* H, const tnfa_net* psi0, const tnfa_dmrg_params* params,
+              tnfa_net** psi, double* energy);
+
 /* ---- differentiation ----------------------------------------------------- */
 
 /* Vector-Jacobian product of batched evaluation: dtensors += sum_p dout[p] *

@@ -976,6 +976,7 @@ struct LinsolveState {
   // environments at bond k (between vertices k-1 and k; k = 0 and L are the
   // open ends): LA/RA [bra][operator][ket], Lb/Rb [x bond][b bond]
   std::vector<Dense> LA, RA, Lb, Rb;
+  bool has_b = true;  // false: no right-hand side (eigenproblem)
   int bond(const Work<double>& w, int k) const { return k >= 1 && k < L ? w.topo.link[k] : 1; }
 };
 
@@ -994,6 +995,7 @@ void left_env(LinsolveState& S, int i) {
   Dense t2 = mm(ctx, t1p.p(), Ap.p(), l * r, d * wr, wl * d, 0, 0, {l, r, d, wr});  // [l'][r][o][wr]
   Dense t2p = permuted(ctx, t2.p(), t2.shp, {2, 0, 3, 1});                // [o][l'][wr][r]
   S.LA[i + 1] = mm(ctx, xi, t2p.p(), r, wr * r, d * l, 1, 0, {r, wr, r});
+  if (!S.has_b) return;
   Dense bp = permuted(ctx, S.b.t[i].as<double>(), {d, bl, br}, {1, 0, 2});  // [bl][s][br]
   Dense u1 = mm(ctx, S.Lb[i].p(), bp.p(), l, d * br, bl, 0, 0, {l, d, br});   // [l'][s][br]
   Dense u1p = permuted(ctx, u1.p(), u1.shp, {1, 0, 2});                   // [s][l'][br]
@@ -1016,6 +1018,7 @@ void right_env(LinsolveState& S, int i) {
   Dense t2p = permuted(ctx, t2.p(), t2.shp, {0, 3, 1, 2});                // [o][r'][wl][l]
   Dense xp = permuted(ctx, xi, {d, l, r}, {1, 0, 2});                     // [l'][o][r']
   S.RA[i] = mm(ctx, xp.p(), t2p.p(), l, wl * l, d * r, 0, 0, {l, wl, l});
+  if (!S.has_b) return;
   Dense v1 = mm(ctx, S.b.t[i].as<double>(), S.Rb[i + 1].p(), d * bl, r, br, 0, 1, {d, bl, r});
   Dense v1p = permuted(ctx, v1.p(), v1.shp, {0, 2, 1});                   // [s][r'][bl]
   S.Rb[i] = mm(ctx, xp.p(), v1p.p(), l, bl, d * r, 0, 0, {l, bl});
@@ -1031,14 +1034,16 @@ __global__ void k_shift_diag(double* H, int n, double a0, double a1) {
 constexpr int kLocalDenseMax = 8192;  // largest two-site system solved densely
 
 // Solve the projected system at bond (i, i+1); returns v [l][s1][s2][r].
-Dense local_solve(LinsolveState& S, int i, double a0, double a1) {
+// a0 I + a1 LA_i A_i A_{i+1} RA_{i+2} as a dense n x n matrix, rows
+// [l' s1' s2' r'] and columns [l s1 s2 r].
+Dense local_H(LinsolveState& S, int i, double a0, double a1, const char* what) {
   tnfa_ctx* ctx = S.ctx;
   const int d = S.d;
   const int l = S.bond(S.x, i), r = S.bond(S.x, i + 2);
   const int wl = S.bond(S.A, i), wm = S.bond(S.A, i + 1), wr = S.bond(S.A, i + 2);
   const int64_t n64 = (int64_t)l * d * d * r;
   TNFA_CHECK(n64 <= kLocalDenseMax, TNFA_ERR_UNSUPPORTED,
-             "linsolve: two-site system of dimension " + std::to_string(n64) +
+             std::string(what) + ": two-site problem of dimension " + std::to_string(n64) +
                  " above the dense limit " + std::to_string(kLocalDenseMax) + " (lower maxdim)");
   const int n = (int)n64;
   // H[l' s1' s2' r'][l s1 s2 r] = LA_i A_i A_{i+1} RA_{i+2}
@@ -1053,6 +1058,15 @@ Dense local_solve(LinsolveState& S, int i, double a0, double a1) {
   Dense H = permuted(ctx, Hr.p(), Hr.shp, {0, 2, 4, 6, 1, 3, 5, 7});
   k_shift_diag<<<grid_for(n64 * n64, 256, 8192), 256, 0, ctx->stream>>>(H.p(), n, a0, a1);
   TNFA_LAUNCH_CHECK();
+  return H;
+}
+
+Dense local_solve(LinsolveState& S, int i, double a0, double a1) {
+  tnfa_ctx* ctx = S.ctx;
+  const int d = S.d;
+  const int l = S.bond(S.x, i), r = S.bond(S.x, i + 2);
+  const int n = l * d * d * r;
+  Dense H = local_H(S, i, a0, a1, "linsolve");
   // g[l][s1][s2][r] = Lb_i b_i b_{i+1} Rb_{i+2}
   const int bl = S.bond(S.b, i), bm = S.bond(S.b, i + 1), br = S.bond(S.b, i + 2);
   Dense b1 = permuted(ctx, S.b.t[i].as<double>(), {d, bl, bm}, {1, 0, 2});      // [bl][s][bm]
@@ -1108,6 +1122,135 @@ void store_two_site(LinsolveState& S, int i, const Dense& v, const tnfa_trunc_pa
     S.x.topo.link[i + 1] = kq;
   }
   S.x.topo.finalize();
+}
+
+// ------------------------------------------------------------------ dmrg --
+// Lowest eigenpair of the dense symmetric local operator by Lanczos with full
+// re-orthogonalisation (two classical Gram-Schmidt passes per step, as GEMMs
+// on the device) and restarts from the Ritz vector; the small projected
+// matrix is diagonalised on the host by cyclic Jacobi.
+
+__global__ void k_scale_copy(double* __restrict__ dst, const double* __restrict__ src, int64_t n, double a) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = a * src[i];
+}
+
+// Smallest eigenvalue of the symmetric m x m matrix T (row-major) and its
+// eigenvector, by cyclic Jacobi rotations.
+void sym_eig_min(std::vector<double> T, int m, double& theta, std::vector<double>& y) {
+  std::vector<double> Vm((size_t)m * m, 0.0);
+  for (int i = 0; i < m; ++i) Vm[(size_t)i * m + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) (i == j ? tot : off) += T[(size_t)i * m + j] * T[(size_t)i * m + j];
+    if (off <= 1e-30 * (tot + off)) break;
+    for (int p = 0; p < m - 1; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        const double apq = T[(size_t)p * m + q];
+        if (apq == 0.0) continue;
+        const double app = T[(size_t)p * m + p], aqq = T[(size_t)q * m + q];
+        const double tau = (aqq - app) / (2.0 * apq);
+        const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+        const double c = 1.0 / std::sqrt(1.0 + t * t), sn = t * c;
+        for (int k = 0; k < m; ++k) {  // rows / columns p, q of T
+          const double tkp = T[(size_t)k * m + p], tkq = T[(size_t)k * m + q];
+          T[(size_t)k * m + p] = c * tkp - sn * tkq;
+          T[(size_t)k * m + q] = sn * tkp + c * tkq;
+        }
+        for (int k = 0; k < m; ++k) {
+          const double tpk = T[(size_t)p * m + k], tqk = T[(size_t)q * m + k];
+          T[(size_t)p * m + k] = c * tpk - sn * tqk;
+          T[(size_t)q * m + k] = sn * tpk + c * tqk;
+        }
+        for (int k = 0; k < m; ++k) {
+          const double vkp = Vm[(size_t)k * m + p], vkq = Vm[(size_t)k * m + q];
+          Vm[(size_t)k * m + p] = c * vkp - sn * vkq;
+          Vm[(size_t)k * m + q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+  int best = 0;
+  for (int i = 1; i < m; ++i)
+    if (T[(size_t)i * m + i] < T[(size_t)best * m + best]) best = i;
+  theta = T[(size_t)best * m + best];
+  y.assign(m, 0.0);
+  for (int k = 0; k < m; ++k) y[k] = Vm[(size_t)k * m + best];
+}
+
+double dev_dot(tnfa_ctx* ctx, const double* a, const double* b, int n, DBuf& scratch) {
+  la::gemm<double>(ctx, {la::GemmJob{a, b, scratch.p, 1, 1, n, n, 1, 1, 0, 0, 1.0, 0.0}});
+  double h = 0.0;
+  TNFA_CUDA(cudaMemcpyAsync(&h, scratch.p, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  return h;
+}
+
+// v (device, n): start vector in, lowest eigenvector out (unit norm).
+double lanczos_min(tnfa_ctx* ctx, const double* H, int n, double* v, int kdim, int restarts, double tol) {
+  kdim = std::max(2, std::min(kdim, n));
+  DBuf V(ctx, (size_t)(kdim + 1) * n * 8), w(ctx, (size_t)n * 8), h(ctx, (size_t)(kdim + 1) * 8), one(ctx, 8);
+  double theta = 0.0;
+  for (int rs = 0; rs <= restarts; ++rs) {
+    double nv = std::sqrt(dev_dot(ctx, v, v, n, one));
+    TNFA_CHECK(nv > 0 && std::isfinite(nv), TNFA_ERR_NOT_CONVERGED, "dmrg: zero or non-finite start vector");
+    const unsigned g = grid_for(n, 256, 1024);
+    k_scale_copy<<<g, 256, 0, ctx->stream>>>(V.as<double>(), v, n, 1.0 / nv);
+    TNFA_LAUNCH_CHECK();
+    std::vector<double> T((size_t)kdim * kdim, 0.0);
+    int m = 0;
+    double beta_last = 0.0;
+    for (int j = 0; j < kdim; ++j) {
+      const double* vj = V.as<double>() + (int64_t)j * n;
+      la::gemm<double>(ctx, {la::GemmJob{H, vj, w.p, n, 1, n, n, 1, 1, 0, 0, 1.0, 0.0}});
+      std::vector<double> hh(j + 1, 0.0);
+      for (int pass = 0; pass < 2; ++pass) {  // w -= V^T (V w), twice
+        la::gemm<double>(ctx, {la::GemmJob{V.p, w.p, h.p, j + 1, 1, n, n, 1, 1, 0, 0, 1.0, 0.0}});
+        la::gemm<double>(ctx, {la::GemmJob{V.p, h.p, w.p, n, 1, j + 1, n, 1, 1, 1, 0, -1.0, 1.0}});
+        std::vector<double> hp(j + 1);
+        TNFA_CUDA(cudaMemcpyAsync(hp.data(), h.p, (j + 1) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (int k = 0; k <= j; ++k) hh[k] += hp[k];
+      }
+      for (int k = 0; k <= j; ++k) {
+        T[(size_t)k * kdim + j] = hh[k];
+        T[(size_t)j * kdim + k] = hh[k];
+      }
+      m = j + 1;
+      const double beta = std::sqrt(std::max(0.0, dev_dot(ctx, w.as<double>(), w.as<double>(), n, one)));
+      beta_last = beta;
+      if (j + 1 == kdim || beta <= 1e-14 * (std::fabs(hh[j]) + 1e-300)) break;
+      T[(size_t)j * kdim + j + 1] = T[(size_t)(j + 1) * kdim + j] = beta;
+      k_scale_copy<<<g, 256, 0, ctx->stream>>>(V.as<double>() + (int64_t)(j + 1) * n, w.as<double>(), n, 1.0 / beta);
+      TNFA_LAUNCH_CHECK();
+    }
+    std::vector<double> Tm((size_t)m * m);
+    for (int a = 0; a < m; ++a)
+      for (int b = 0; b < m; ++b) Tm[(size_t)a * m + b] = T[(size_t)a * kdim + b];
+    std::vector<double> y;
+    sym_eig_min(Tm, m, theta, y);
+    // v = V^T y
+    DBuf dy(ctx, (size_t)m * 8);
+    TNFA_CUDA(cudaMemcpyAsync(dy.p, y.data(), m * 8, cudaMemcpyHostToDevice, ctx->stream));
+    la::gemm<double>(ctx, {la::GemmJob{V.p, dy.p, v, n, 1, m, n, 1, 1, 1, 0, 1.0, 0.0}});
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+    const double resid = beta_last * std::fabs(y[m - 1]);
+    if (resid <= tol * std::max(1.0, std::fabs(theta)) || m < kdim) break;
+  }
+  const double nv = std::sqrt(dev_dot(ctx, v, v, n, one));
+  k_scale_copy<<<grid_for(n, 256, 1024), 256, 0, ctx->stream>>>(v, v, n, 1.0 / nv);
+  TNFA_LAUNCH_CHECK();
+  return theta;
+}
+
+// x_i x_{i+1} as v [l][s1][s2][r].
+Dense two_site(LinsolveState& S, int i) {
+  tnfa_ctx* ctx = S.ctx;
+  const int d = S.d;
+  const int l = S.bond(S.x, i), k = S.bond(S.x, i + 1), r = S.bond(S.x, i + 2);
+  Dense a = permuted(ctx, S.x.t[i].as<double>(), {d, l, k}, {1, 0, 2});      // [l][s1][k]
+  Dense b = permuted(ctx, S.x.t[i + 1].as<double>(), {d, k, r}, {1, 0, 2});  // [k][s2][r]
+  return mm(ctx, a.p(), b.p(), l * d, d * r, k, 0, 0, {l, d, d, r});
 }
 
 // ||net|| through a QR sweep toward the root (backward stable).
@@ -1302,6 +1445,75 @@ tnfa_net* linsolve_refined(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, 
   return out;
 }
 
+// Two-site DMRG for the lowest eigenpair of a symmetric operator on a path.
+tnfa_net* dmrg_path(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* x0, const tnfa_dmrg_params& prm,
+                    double* energy) {
+  TNFA_CHECK(A->dtype == TNFA_F64 && x0->dtype == TNFA_F64, TNFA_ERR_DTYPE, "dmrg works on FP64 networks");
+  check_same_tree(A->topo, x0->topo, "dmrg (H, psi0)");
+  TNFA_CHECK(x0->topo.V >= 2, TNFA_ERR_UNSUPPORTED, "dmrg needs at least two vertices");
+  for (int v = 0; v < x0->topo.V; ++v)
+    TNFA_CHECK(x0->topo.nlegs[v] == 1, TNFA_ERR_UNSUPPORTED, "dmrg needs one site leg per vertex");
+  for (int l = 0; l < x0->topo.leg_off[x0->topo.V]; ++l) {
+    TNFA_CHECK(A->topo.leg_kind[l] == TNFA_LEG_OPERATOR && x0->topo.leg_kind[l] != TNFA_LEG_OPERATOR,
+               TNFA_ERR_INVALID_ARGUMENT, "dmrg(H, psi0): H an operator, psi0 a function");
+    TNFA_CHECK(x0->topo.leg_dim[l] == x0->topo.leg_dim[0] &&
+                   A->topo.leg_dim[l] == x0->topo.leg_dim[l] * x0->topo.leg_dim[l],
+               TNFA_ERR_SHAPE, "dmrg: site dimensions of H and psi0 disagree");
+  }
+  const std::vector<int> ord = path_order(x0->topo);
+  const int L = x0->topo.V;
+  LinsolveState S{ctx, L, x0->topo.leg_dim[0],
+                  relayout<double>(ctx, x0->topo, x0->d, path_topo(x0->topo, ord), ord),
+                  relayout<double>(ctx, A->topo, A->d, path_topo(A->topo, ord), ord),
+                  Work<double>{ctx, Topo{}, {}}, {}, {}, {}, {}};
+  S.has_b = false;
+  orthogonalize_to_roots(S.x);
+  S.x.topo.finalize();
+  S.LA.resize(L + 1);
+  S.RA.resize(L + 1);
+  S.LA[0] = ones(ctx, {1, 1, 1});
+  S.RA[L] = ones(ctx, {1, 1, 1});
+  for (int i = L - 1; i >= 2; --i) right_env(S, i);
+  const tnfa_trunc_params tp{prm.cutoff, prm.maxdim, 1, 0, TNFA_PREC_F64};
+  TruncStats st;
+  double E = 0.0, Eprev = 0.0;
+  for (int sweep = 0; sweep < std::max(1, prm.nsweeps); ++sweep) {
+    for (int dir = 0; dir < 2; ++dir) {
+      for (int step = 0; step + 1 < L; ++step) {
+        const int i = dir == 0 ? step : L - 2 - step;
+        Dense H = local_H(S, i, 0.0, 1.0, "dmrg");
+        Dense v = two_site(S, i);
+        const int n = (int)(S.bond(S.x, i) * S.d * S.d * S.bond(S.x, i + 2));
+        E = lanczos_min(ctx, H.p(), n, v.p(), prm.krylov_dim > 0 ? prm.krylov_dim : 30,
+                        std::max(0, prm.restarts), 1e-12);
+        store_two_site(S, i, v, tp, st, dir == 0);
+        // keep the state normalised after truncation: rescale the centre
+        const int c = dir == 0 ? i + 1 : i;
+        const double nc = host_norm<double>(ctx, S.x.t[c], S.x.size(c));
+        if (nc > 0)
+          k_scale_copy<<<grid_for(S.x.size(c), 256, 1024), 256, 0, ctx->stream>>>(
+              S.x.t[c].as<double>(), S.x.t[c].as<double>(), S.x.size(c), 1.0 / nc);
+        if (dir == 0) left_env(S, i);
+        else right_env(S, i + 1);
+      }
+    }
+    if (sweep > 0 && std::fabs(E - Eprev) <= prm.tol * std::max(1.0, std::fabs(E))) break;
+    Eprev = E;
+  }
+  if (energy) *energy = E;
+  NetHold xp(store_work(S.x, TNFA_F64));
+  Topo back = x0->topo;
+  for (int k = 1; k < L; ++k) {
+    const int c = ord[k], cp = ord[k - 1];
+    (back.parent[c] == cp ? back.link[c] : back.link[cp]) = S.x.topo.link[k];
+  }
+  back.finalize();
+  std::vector<int> pos(L);
+  for (int k = 0; k < L; ++k) pos[ord[k]] = k;
+  Work<double> wb = relayout<double>(ctx, xp.p->topo, xp.p->d, back, pos);
+  return store_work(wb, TNFA_F64);
+}
+
 void inner_product(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, bool conjF, double* out) {
   TNFA_CHECK(f->dtype == g->dtype, TNFA_ERR_DTYPE, "inner: element types differ");
   if (f->dtype == TNFA_F64) contract_pair<double>(ctx, f, g, conjF, out);
@@ -1426,6 +1638,19 @@ int tnfa_linsolve(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnf
              "negative refinement parameter");
   *x = linsolve_refined(ctx, A, b, x0, *params, &rr);
   if (rel_residual) *rel_residual = rr;
+  TNFA_API_END
+}
+
+int tnfa_dmrg(tnfa_ctx* ctx, const tnfa_net* H, const tnfa_net* psi0, const tnfa_dmrg_params* params,
+              tnfa_net** psi, double* energy) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(H, "dmrg H");
+  require_net(psi0, "dmrg psi0");
+  TNFA_CHECK(params && psi, TNFA_ERR_INVALID_ARGUMENT, "null params or out");
+  TNFA_CHECK(params->maxdim >= 0 && params->cutoff >= 0 && params->tol >= 0, TNFA_ERR_INVALID_ARGUMENT,
+             "negative dmrg parameter");
+  *psi = dmrg_path(ctx, H, psi0, *params, energy);
   TNFA_API_END
 }
 

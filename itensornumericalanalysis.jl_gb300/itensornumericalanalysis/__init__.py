@@ -71,7 +71,7 @@ from .grad import TTNEvaluate, evaluate_vjp
 from .integration import integrate, partial_integrate
 from .network import ITensorNetworkFunction, calculate_fx, evaluate, inner
 from .operate import operate, operate_batched
-from .solvers import linsolve
+from .solvers import dmrg, linsolve
 from .tci import interpolate
 from .truncation import truncate, truncate_batched
 

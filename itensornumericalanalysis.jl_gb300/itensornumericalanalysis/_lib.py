@@ -79,6 +79,17 @@ class TruncParams(C.Structure):
     ]
 
 
+class DmrgParams(C.Structure):
+    _fields_ = [
+        ("nsweeps", C.c_int32),
+        ("maxdim", C.c_int32),
+        ("cutoff", C.c_double),
+        ("tol", C.c_double),
+        ("krylov_dim", C.c_int32),
+        ("restarts", C.c_int32),
+    ]
+
+
 class LinsolveParams(C.Structure):
     _fields_ = [
         ("nsweeps", C.c_int32),
@@ -146,6 +157,7 @@ SIGNATURES = {
     "tnfa_truncate_batched": (C.c_int, [_P, _I32, _PP, C.POINTER(TruncParams), _PP]),
     "tnfa_inner": (C.c_int, [_P, _P, _P, _PD]),
     "tnfa_linsolve": (C.c_int, [_P, _P, _P, _P, C.POINTER(LinsolveParams), _PP, _PD]),
+    "tnfa_dmrg": (C.c_int, [_P, _P, _P, C.POINTER(DmrgParams), _PP, _PD]),
     "tnfa_evaluate_vjp": (
         C.c_int,
         [_P, _P, _P, _I64, _I32, _PI32, C.c_int, _P, C.c_int, _P, C.c_int],

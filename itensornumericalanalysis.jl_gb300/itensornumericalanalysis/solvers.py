@@ -47,3 +47,22 @@ def linsolve(A, b, x0=None, a0: float = 0.0, a1: float = 1.0, nsweeps: int = 10,
     x = b._wrap(h)
     x.rel_residual = float(res.value)
     return x
+
+
+def dmrg(H, psi0, nsweeps: int = 10, maxdim: int | None = None, cutoff: float = 1e-12,
+         tol: float = 1e-12, krylov_dim: int = 30, restarts: int = 4, nsites: int = 2,
+         normalize: bool = True):
+    """Lowest eigenpair of the symmetric operator H, (energy, psi), by two-site
+    DMRG sweeps from psi0 on a path-shaped tree (examples/2d_laplace_solver.jl
+    calls ITensorNetworks.dmrg with nsites = 2 and normalize = true; those are
+    the only modes here).  The two-site operator is built densely on the
+    device and Lanczos with full re-orthogonalisation finds its lowest
+    eigenvector; the split is an SVD truncated with cutoff / maxdim."""
+    if nsites != 2 or not normalize:
+        raise ValueError("dmrg: nsites = 2 with normalize = True only")
+    p = _lib.DmrgParams(int(nsweeps), int(maxdim or 0), float(cutoff), float(tol), int(krylov_dim),
+                        int(restarts))
+    h = C.c_void_p()
+    e = C.c_double(0.0)
+    psi0.ctx.call("tnfa_dmrg", H.handle, psi0.handle, C.byref(p), C.byref(h), C.byref(e))
+    return float(e.value), psi0._wrap(h)

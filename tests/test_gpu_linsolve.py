@@ -130,3 +130,25 @@ def test_non_path_rejected(ina):
     A = ina.second_derivative_operator(s)
     with pytest.raises(ina.TnfaError, match="path"):
         ina.linsolve(A, b)
+
+
+def test_dmrg_lowest_laplacian_mode(ina):
+    """examples/2d_laplace_solver.jl on a 2 x 5 comb: DMRG finds the lowest
+    eigenpair of the unscaled Laplacian (eigenvalues of the dense stencil
+    matrix; the most negative one is approached as the grid grows)."""
+    L = 5
+    g = ina.named_comb_tree((2, L))
+    s = ina.continuous_siteinds(g, [[(1, j) for j in range(L, 0, -1)],
+                                    [(2, j) for j in range(1, L + 1)]])
+    A = ina.laplacian_operator(s, scale=False)
+    psi0 = ina.rand_itn(s, link_space=3, rng=75)
+    E, psi = ina.dmrg(A, psi0, nsweeps=8, maxdim=32, cutoff=1e-14)
+    terms = (O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2, dim=1, scale=False)
+             + O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2, dim=2, scale=False))
+    axis_of = {(1, k): k - 1 for k in range(1, L + 1)}
+    axis_of.update({(2, k): L + k - 1 for k in range(1, L + 1)})
+    M = _dense_operator(terms, 2 * L, axis_of)
+    w, V = np.linalg.eigh((M + M.T) / 2)
+    assert abs(E - w[0]) < 1e-9 * abs(w[0]), (E, w[:3])
+    v = psi.evaluate_batch(_grid_2d(L), [1, 2])
+    assert abs(abs(v @ V[:, 0]) / np.linalg.norm(v) - 1) < 1e-8
