@@ -977,7 +977,9 @@ struct LinsolveState {
   // open ends): LA/RA [bra][operator][ket], Lb/Rb [x bond][b bond]
   std::vector<Dense> LA, RA, Lb, Rb;
   bool has_b = true;  // false: no right-hand side (eigenproblem)
-  int bond(const Work<double>& w, int k) const { return k >= 1 && k < L ? w.topo.link[k] : 1; }
+  int bond(const Work<double>& w, int k) const {
+    return k >= 1 && k < L && k < (int)w.topo.link.size() ? w.topo.link[k] : 1;
+  }
 };
 
 // LA_{i+1} and Lb_{i+1} from LA_i, Lb_i and the left-orthonormal x_i.
@@ -986,7 +988,6 @@ void left_env(LinsolveState& S, int i) {
   const int d = S.d;
   const int l = S.bond(S.x, i), r = S.bond(S.x, i + 1);
   const int wl = S.bond(S.A, i), wr = S.bond(S.A, i + 1);
-  const int bl = S.bond(S.b, i), br = S.bond(S.b, i + 1);
   const double* xi = S.x.t[i].as<double>();
   Dense xp = permuted(ctx, xi, {d, l, r}, {1, 0, 2});                     // [l][s][r]
   Dense t1 = mm(ctx, S.LA[i].p(), xp.p(), l * wl, d * r, l, 0, 0, {l, wl, d, r});  // [l'][wl][s][r]
@@ -996,6 +997,7 @@ void left_env(LinsolveState& S, int i) {
   Dense t2p = permuted(ctx, t2.p(), t2.shp, {2, 0, 3, 1});                // [o][l'][wr][r]
   S.LA[i + 1] = mm(ctx, xi, t2p.p(), r, wr * r, d * l, 1, 0, {r, wr, r});
   if (!S.has_b) return;
+  const int bl = S.bond(S.b, i), br = S.bond(S.b, i + 1);
   Dense bp = permuted(ctx, S.b.t[i].as<double>(), {d, bl, br}, {1, 0, 2});  // [bl][s][br]
   Dense u1 = mm(ctx, S.Lb[i].p(), bp.p(), l, d * br, bl, 0, 0, {l, d, br});   // [l'][s][br]
   Dense u1p = permuted(ctx, u1.p(), u1.shp, {1, 0, 2});                   // [s][l'][br]
@@ -1008,7 +1010,6 @@ void right_env(LinsolveState& S, int i) {
   const int d = S.d;
   const int l = S.bond(S.x, i), r = S.bond(S.x, i + 1);
   const int wl = S.bond(S.A, i), wr = S.bond(S.A, i + 1);
-  const int bl = S.bond(S.b, i), br = S.bond(S.b, i + 1);
   const double* xi = S.x.t[i].as<double>();
   Dense Rp = permuted(ctx, S.RA[i + 1].p(), S.RA[i + 1].shp, {2, 0, 1});  // [r][r'][wr]
   Dense t1 = mm(ctx, xi, Rp.p(), d * l, r * wr, r, 0, 0, {d, l, r, wr});  // [s][l][r'][wr]
@@ -1019,6 +1020,7 @@ void right_env(LinsolveState& S, int i) {
   Dense xp = permuted(ctx, xi, {d, l, r}, {1, 0, 2});                     // [l'][o][r']
   S.RA[i] = mm(ctx, xp.p(), t2p.p(), l, wl * l, d * r, 0, 0, {l, wl, l});
   if (!S.has_b) return;
+  const int bl = S.bond(S.b, i), br = S.bond(S.b, i + 1);
   Dense v1 = mm(ctx, S.b.t[i].as<double>(), S.Rb[i + 1].p(), d * bl, r, br, 0, 1, {d, bl, r});
   Dense v1p = permuted(ctx, v1.p(), v1.shp, {0, 2, 1});                   // [s][r'][bl]
   S.Rb[i] = mm(ctx, xp.p(), v1p.p(), l, bl, d * r, 0, 0, {l, bl});
