@@ -1,10 +1,15 @@
-// Batched dense linear algebra kernels (FP64 real and complex128).
+// Batched dense linear algebra kernels (FP64 real and complex128; FP32 for
+// the first passes of the mixed factorisation).
 //
-//   permute  : general tensor transpose (up to 10 axes)
-//   gemm     : tiled SIMT GEMM, 64x64 tiles, op(A) op(B) with N/T/C
-//   qr       : Householder QR, one CTA per matrix, column-major workspace
-//   svd      : one-sided Jacobi (Hestenes) SVD, round-robin pair ordering,
-//              one CTA per matrix, columns contiguous in the workspace
+//   permute      : general tensor transpose (up to 10 axes)
+//   gemm         : tiled SIMT GEMM, 64x64 tiles, op(A) op(B) with N/T/C
+//   qr           : Householder QR, one CTA per matrix or an 8-CTA cluster
+//                  per large matrix, column-major workspace
+//   jacobi       : one-sided Jacobi (Hestenes) SVD, round-robin pairs, one
+//                  CTA or an 8-CTA cluster per matrix, register-cached columns
+//   trunc_factor : the SVD step of truncation (QR + Jacobi without V, plain
+//                  or FP32-preconditioned)
+//   lu_solve     : blocked LU with partial pivoting for one dense system
 // Every problem of a batch may have its own shape; one launch covers them all.
 #include <algorithm>
 #include <cmath>
@@ -769,13 +774,6 @@ void jacobi(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, Jaco
   }
 }
 
-template <class T>
-void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps) {
-  if (jobs.empty()) return;
-  jacobi<T>(ctx, jobs, max_sweeps, JacobiOpts{1e-10, 0.0},
-            sizeof(T) == 8 ? "svd_f64" : (sizeof(T) == 4 ? "svd_f32" : "svd_c128"));
-
-}
 
 // ------------------------------------------------------------------ lu --
 constexpr int LU_NB = 32;
@@ -1281,9 +1279,6 @@ template void gemm<double>(tnfa_ctx*, const std::vector<GemmJob>&);
 template void gemm<cplx>(tnfa_ctx*, const std::vector<GemmJob>&);
 template void qr<double>(tnfa_ctx*, const std::vector<QrJob>&);
 template void qr<cplx>(tnfa_ctx*, const std::vector<QrJob>&);
-template void svd<double>(tnfa_ctx*, const std::vector<SvdJob>&, int);
-template void svd<cplx>(tnfa_ctx*, const std::vector<SvdJob>&, int);
-template void svd<float>(tnfa_ctx*, const std::vector<SvdJob>&, int);
 template void trunc_factor<double>(tnfa_ctx*, const std::vector<FactorJob>&, double, int, int, int,
                                    std::vector<FactorResult>&);
 template void trunc_factor<cplx>(tnfa_ctx*, const std::vector<FactorJob>&, double, int, int, int,

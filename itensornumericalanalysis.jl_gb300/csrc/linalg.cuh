@@ -46,10 +46,10 @@ struct QrJob {
 template <class T>
 void qr(tnfa_ctx* ctx, const std::vector<QrJob>& jobs);
 
-// One-sided Jacobi SVD of A (m x n, m >= n, lda = n, read only):
-// A = U diag(S) V^H with U (m x n, orthonormal columns where S > 0), S (n,
-// real, descending), V (n x n; not accumulated when V is null).  sweeps
-// receives the sweep count, or -1 when the sweep cap was reached.
+// One job of the one-sided Jacobi SVD used by trunc_factor: A (m x n, m >=
+// n, lda = n, read only) = U diag(S) V^H with U (m x n, orthonormal columns
+// where S > 0), S (n, real, descending), V (n x n; not accumulated when V is
+// null).  sweeps receives the sweep count, or -1 when the sweep cap was hit.
 struct SvdJob {
   const void* A;
   void* U;
@@ -58,8 +58,6 @@ struct SvdJob {
   int m, n;
   int* sweeps;
 };
-template <class T>
-void svd(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps = 60);
 
 // Solve A x = b for one dense n x n FP64 system (A row-major, destroyed; b
 // overwritten by x): blocked right-looking LU with partial pivoting (panel
