@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <functional>
 #include <numeric>
 
 #include "evaluate.cuh"
@@ -1026,6 +1027,12 @@ void right_env(LinsolveState& S, int i) {
   S.Rb[i] = mm(ctx, xp.p(), v1p.p(), l, bl, d * r, 0, 0, {l, bl});
 }
 
+// y += a x
+__global__ void k_axpy(double* __restrict__ y, const double* __restrict__ x, int64_t n, double a) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] += a * x[i];
+}
+
 __global__ void k_shift_diag(double* H, int n, double a0, double a1) {
   const int64_t nn = (int64_t)n * n;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn;
@@ -1033,9 +1040,16 @@ __global__ void k_shift_diag(double* H, int n, double a0, double a1) {
     H[i] = a1 * H[i] + ((i / n) == (i % n) ? a0 : 0.0);
 }
 
-constexpr int kLocalDenseMax = 8192;  // largest two-site system solved densely
+constexpr int kLocalDenseMax = 8192;    // largest two-site system solved densely
+constexpr int kLocalDenseSmall = 4096;  // above this the eigensolver goes matrix-free
 
-// Solve the projected system at bond (i, i+1); returns v [l][s1][s2][r].
+// TNFA_LOCAL_MATRIX_FREE=1 selects the matrix-free two-site operator at every
+// size (the dense one is the default where it fits).
+bool force_matrix_free() {
+  static const bool on = getenv("TNFA_LOCAL_MATRIX_FREE") && *getenv("TNFA_LOCAL_MATRIX_FREE") == '1';
+  return on;
+}
+
 // a0 I + a1 LA_i A_i A_{i+1} RA_{i+2} as a dense n x n matrix, rows
 // [l' s1' s2' r'] and columns [l s1 s2 r].
 Dense local_H(LinsolveState& S, int i, double a0, double a1, const char* what) {
@@ -1063,23 +1077,6 @@ Dense local_H(LinsolveState& S, int i, double a0, double a1, const char* what) {
   return H;
 }
 
-Dense local_solve(LinsolveState& S, int i, double a0, double a1) {
-  tnfa_ctx* ctx = S.ctx;
-  const int d = S.d;
-  const int l = S.bond(S.x, i), r = S.bond(S.x, i + 2);
-  const int n = l * d * d * r;
-  Dense H = local_H(S, i, a0, a1, "linsolve");
-  // g[l][s1][s2][r] = Lb_i b_i b_{i+1} Rb_{i+2}
-  const int bl = S.bond(S.b, i), bm = S.bond(S.b, i + 1), br = S.bond(S.b, i + 2);
-  Dense b1 = permuted(ctx, S.b.t[i].as<double>(), {d, bl, bm}, {1, 0, 2});      // [bl][s][bm]
-  Dense G1 = mm(ctx, S.Lb[i].p(), b1.p(), l, d * bm, bl, 0, 0, {l, d, bm});
-  Dense b2 = permuted(ctx, S.b.t[i + 1].as<double>(), {d, bm, br}, {1, 0, 2});  // [bm][s][br]
-  Dense G2 = mm(ctx, G1.p(), b2.p(), l * d, d * br, bm, 0, 0, {l, d, d, br});
-  Dense g = mm(ctx, G2.p(), S.Rb[i + 2].p(), l * d * d, r, br, 0, 1, {l, d, d, r});
-  TNFA_CHECK(la::lu_solve(ctx, H.p(), g.p(), n), TNFA_ERR_NOT_CONVERGED,
-             "linsolve: singular two-site system at bond " + std::to_string(i + 1));
-  return g;
-}
 
 // Write v [l][s1][s2][r] back as x_i x_{i+1} through a truncated SVD; the
 // centre ends in x_{i+1} (toward_right) or in x_i.
@@ -1125,6 +1122,45 @@ void store_two_site(LinsolveState& S, int i, const Dense& v, const tnfa_trunc_pa
   }
   S.x.topo.finalize();
 }
+
+// Matrix-free two-site operator: y = a0 v + a1 LA_i A_i A_{i+1} RA_{i+2} v
+// for v [l][s1][s2][r], as four GEMMs and three transposes per product; the
+// operator pieces are transposed once per two-site problem.  Used when the
+// dense two-site matrix would be large.
+struct LocalOp {
+  tnfa_ctx* ctx;
+  int l, r, d, wl, wm, wr;
+  double a0, a1;
+  const double* LA;  // [l'][wl][l]
+  Dense A1p, A2p, RAp;
+  LocalOp(LinsolveState& S, int i, double a0_, double a1_) : ctx(S.ctx), a0(a0_), a1(a1_) {
+    d = S.d;
+    l = S.bond(S.x, i);
+    r = S.bond(S.x, i + 2);
+    wl = S.bond(S.A, i);
+    wm = S.bond(S.A, i + 1);
+    wr = S.bond(S.A, i + 2);
+    LA = S.LA[i].p();
+    A1p = permuted(ctx, S.A.t[i].as<double>(), {d, d, wl, wm}, {2, 1, 0, 3});      // [wl][in][o][wm]
+    A2p = permuted(ctx, S.A.t[i + 1].as<double>(), {d, d, wm, wr}, {2, 1, 0, 3});  // [wm][in][o][wr]
+    RAp = permuted(ctx, S.RA[i + 2].p(), S.RA[i + 2].shp, {1, 2, 0});              // [wr][r][r']
+  }
+  int n() const { return l * d * d * r; }
+  void operator()(const double* v, double* y) const {
+    Dense t1 = mm(ctx, LA, v, l * wl, d * d * r, l, 0, 0, {l, wl, d, d, r});        // [l'][wl][s1][s2][r]
+    Dense t1p = permuted(ctx, t1.p(), t1.shp, {0, 3, 4, 1, 2});                      // [l'][s2][r][wl][s1]
+    Dense t2 = mm(ctx, t1p.p(), A1p.p(), l * d * r, d * wm, wl * d, 0, 0, {l, d, r, d, wm});  // [l'][s2][r][s1'][wm]
+    Dense t2p = permuted(ctx, t2.p(), t2.shp, {0, 2, 3, 4, 1});                      // [l'][r][s1'][wm][s2]
+    Dense t3 = mm(ctx, t2p.p(), A2p.p(), l * r * d, d * wr, wm * d, 0, 0, {l, r, d, d, wr});  // [l'][r][s1'][s2'][wr]
+    Dense t3p = permuted(ctx, t3.p(), t3.shp, {0, 2, 3, 4, 1});                      // [l'][s1'][s2'][wr][r]
+    la::gemm<double>(ctx, {la::GemmJob{t3p.p(), RAp.p(), y, l * d * d, r, wr * r, wr * r, r, r, 0, 0, a1, 0.0}});
+    if (a0 != 0.0) {
+      const int64_t nn = n();
+      k_axpy<<<grid_for(nn, 256, 1024), 256, 0, ctx->stream>>>(y, v, nn, a0);
+      TNFA_LAUNCH_CHECK();
+    }
+  }
+};
 
 // ------------------------------------------------------------------ dmrg --
 // Lowest eigenpair of the dense symmetric local operator by Lanczos with full
@@ -1188,8 +1224,10 @@ double dev_dot(tnfa_ctx* ctx, const double* a, const double* b, int n, DBuf& scr
   return h;
 }
 
+using MatVec = std::function<void(const double*, double*)>;  // y = H x on the device
+
 // v (device, n): start vector in, lowest eigenvector out (unit norm).
-double lanczos_min(tnfa_ctx* ctx, const double* H, int n, double* v, int kdim, int restarts, double tol) {
+double lanczos_min(tnfa_ctx* ctx, const MatVec& H, int n, double* v, int kdim, int restarts, double tol) {
   kdim = std::max(2, std::min(kdim, n));
   DBuf V(ctx, (size_t)(kdim + 1) * n * 8), w(ctx, (size_t)n * 8), h(ctx, (size_t)(kdim + 1) * 8), one(ctx, 8);
   double theta = 0.0;
@@ -1204,7 +1242,7 @@ double lanczos_min(tnfa_ctx* ctx, const double* H, int n, double* v, int kdim, i
     double beta_last = 0.0;
     for (int j = 0; j < kdim; ++j) {
       const double* vj = V.as<double>() + (int64_t)j * n;
-      la::gemm<double>(ctx, {la::GemmJob{H, vj, w.p, n, 1, n, n, 1, 1, 0, 0, 1.0, 0.0}});
+      H(vj, w.as<double>());
       std::vector<double> hh(j + 1, 0.0);
       for (int pass = 0; pass < 2; ++pass) {  // w -= V^T (V w), twice
         la::gemm<double>(ctx, {la::GemmJob{V.p, w.p, h.p, j + 1, 1, n, n, 1, 1, 0, 0, 1.0, 0.0}});
@@ -1245,6 +1283,80 @@ double lanczos_min(tnfa_ctx* ctx, const double* H, int n, double* v, int kdim, i
   return theta;
 }
 
+// Solve A x = g (device vectors of length n) by restarted GMRES(m) from the
+// given x, Arnoldi with two classical Gram-Schmidt passes, Givens rotations
+// on the host; stops when the residual estimate is <= tol |g|.
+void gmres(tnfa_ctx* ctx, const MatVec& A, int n, const double* g, double* x, int m, int restarts,
+           double tol) {
+  m = std::max(1, std::min(m, n));
+  DBuf V(ctx, (size_t)(m + 1) * n * 8), w(ctx, (size_t)n * 8), h(ctx, (size_t)(m + 1) * 8), one(ctx, 8);
+  const double gn = std::sqrt(dev_dot(ctx, g, g, n, one));
+  if (gn == 0.0) {
+    TNFA_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, ctx->stream));
+    return;
+  }
+  const unsigned gr = grid_for(n, 256, 1024);
+  for (int rs = 0; rs <= restarts; ++rs) {
+    // r = g - A x
+    A(x, w.as<double>());
+    k_scale_copy<<<gr, 256, 0, ctx->stream>>>(w.as<double>(), w.as<double>(), n, -1.0);
+    k_axpy<<<gr, 256, 0, ctx->stream>>>(w.as<double>(), g, n, 1.0);
+    TNFA_LAUNCH_CHECK();
+    const double beta = std::sqrt(dev_dot(ctx, w.as<double>(), w.as<double>(), n, one));
+    if (beta <= tol * gn) return;
+    k_scale_copy<<<gr, 256, 0, ctx->stream>>>(V.as<double>(), w.as<double>(), n, 1.0 / beta);
+    TNFA_LAUNCH_CHECK();
+    std::vector<double> Hh((size_t)(m + 1) * m, 0.0), cs(m, 0.0), sn(m, 0.0), sv(m + 1, 0.0);
+    sv[0] = beta;
+    int k = 0;
+    for (int j = 0; j < m; ++j) {
+      A(V.as<double>() + (int64_t)j * n, w.as<double>());
+      std::vector<double> hh(j + 1, 0.0);
+      for (int pass = 0; pass < 2; ++pass) {
+        la::gemm<double>(ctx, {la::GemmJob{V.p, w.p, h.p, j + 1, 1, n, n, 1, 1, 0, 0, 1.0, 0.0}});
+        la::gemm<double>(ctx, {la::GemmJob{V.p, h.p, w.p, n, 1, j + 1, n, 1, 1, 1, 0, -1.0, 1.0}});
+        std::vector<double> hp(j + 1);
+        TNFA_CUDA(cudaMemcpyAsync(hp.data(), h.p, (j + 1) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (int q = 0; q <= j; ++q) hh[q] += hp[q];
+      }
+      const double hn = std::sqrt(std::max(0.0, dev_dot(ctx, w.as<double>(), w.as<double>(), n, one)));
+      for (int q = 0; q <= j; ++q) Hh[(size_t)q * m + j] = hh[q];
+      Hh[(size_t)(j + 1) * m + j] = hn;
+      for (int q = 0; q < j; ++q) {  // earlier rotations on the new column
+        const double a = Hh[(size_t)q * m + j], b = Hh[(size_t)(q + 1) * m + j];
+        Hh[(size_t)q * m + j] = cs[q] * a + sn[q] * b;
+        Hh[(size_t)(q + 1) * m + j] = -sn[q] * a + cs[q] * b;
+      }
+      const double a = Hh[(size_t)j * m + j], b = Hh[(size_t)(j + 1) * m + j];
+      const double rr = std::hypot(a, b);
+      cs[j] = rr > 0 ? a / rr : 1.0;
+      sn[j] = rr > 0 ? b / rr : 0.0;
+      Hh[(size_t)j * m + j] = rr;
+      Hh[(size_t)(j + 1) * m + j] = 0.0;
+      sv[j + 1] = -sn[j] * sv[j];
+      sv[j] = cs[j] * sv[j];
+      k = j + 1;
+      if (std::fabs(sv[j + 1]) <= tol * gn || hn <= 1e-300) break;
+      k_scale_copy<<<gr, 256, 0, ctx->stream>>>(V.as<double>() + (int64_t)(j + 1) * n, w.as<double>(), n,
+                                                1.0 / hn);
+      TNFA_LAUNCH_CHECK();
+    }
+    // y = R^-1 s, x += V^T y
+    std::vector<double> y(k, 0.0);
+    for (int q = k - 1; q >= 0; --q) {
+      double t = sv[q];
+      for (int c = q + 1; c < k; ++c) t -= Hh[(size_t)q * m + c] * y[c];
+      y[q] = Hh[(size_t)q * m + q] != 0.0 ? t / Hh[(size_t)q * m + q] : 0.0;
+    }
+    DBuf dy(ctx, (size_t)k * 8);
+    TNFA_CUDA(cudaMemcpyAsync(dy.p, y.data(), k * 8, cudaMemcpyHostToDevice, ctx->stream));
+    la::gemm<double>(ctx, {la::GemmJob{V.p, dy.p, x, n, 1, k, n, 1, 1, 1, 0, 1.0, 1.0}});
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (std::fabs(sv[k]) <= tol * gn) return;
+  }
+}
+
 // x_i x_{i+1} as v [l][s1][s2][r].
 Dense two_site(LinsolveState& S, int i) {
   tnfa_ctx* ctx = S.ctx;
@@ -1253,6 +1365,34 @@ Dense two_site(LinsolveState& S, int i) {
   Dense a = permuted(ctx, S.x.t[i].as<double>(), {d, l, k}, {1, 0, 2});      // [l][s1][k]
   Dense b = permuted(ctx, S.x.t[i + 1].as<double>(), {d, k, r}, {1, 0, 2});  // [k][s2][r]
   return mm(ctx, a.p(), b.p(), l * d, d * r, k, 0, 0, {l, d, d, r});
+}
+
+// Solve the projected system at bond (i, i+1); returns v [l][s1][s2][r].
+Dense local_solve(LinsolveState& S, int i, double a0, double a1) {
+  tnfa_ctx* ctx = S.ctx;
+  const int d = S.d;
+  const int l = S.bond(S.x, i), r = S.bond(S.x, i + 2);
+  const int64_t n64 = (int64_t)l * d * d * r;
+  TNFA_CHECK(n64 < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "linsolve: two-site system too large");
+  const int n = (int)n64;
+  // g[l][s1][s2][r] = Lb_i b_i b_{i+1} Rb_{i+2}
+  const int bl = S.bond(S.b, i), bm = S.bond(S.b, i + 1), br = S.bond(S.b, i + 2);
+  Dense b1 = permuted(ctx, S.b.t[i].as<double>(), {d, bl, bm}, {1, 0, 2});      // [bl][s][bm]
+  Dense G1 = mm(ctx, S.Lb[i].p(), b1.p(), l, d * bm, bl, 0, 0, {l, d, bm});
+  Dense b2 = permuted(ctx, S.b.t[i + 1].as<double>(), {d, bm, br}, {1, 0, 2});  // [bm][s][br]
+  Dense G2 = mm(ctx, G1.p(), b2.p(), l * d, d * br, bm, 0, 0, {l, d, d, br});
+  Dense g = mm(ctx, G2.p(), S.Rb[i + 2].p(), l * d * d, r, br, 0, 1, {l, d, d, r});
+  if (n64 <= kLocalDenseMax && !force_matrix_free()) {
+    Dense H = local_H(S, i, a0, a1, "linsolve");
+    TNFA_CHECK(la::lu_solve(ctx, H.p(), g.p(), n), TNFA_ERR_NOT_CONVERGED,
+               "linsolve: singular two-site system at bond " + std::to_string(i + 1));
+    return g;
+  }
+  // large two-site systems: matrix-free GMRES from the current two-site tensor
+  Dense x = two_site(S, i);
+  LocalOp op(S, i, a0, a1);
+  gmres(ctx, [&](const double* u, double* y) { op(u, y); }, n, g.p(), x.p(), 40, 20, 1e-12);
+  return x;
 }
 
 // ||net|| through a QR sweep toward the root (backward stable).
@@ -1483,11 +1623,25 @@ tnfa_net* dmrg_path(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* x0, const 
     for (int dir = 0; dir < 2; ++dir) {
       for (int step = 0; step + 1 < L; ++step) {
         const int i = dir == 0 ? step : L - 2 - step;
-        Dense H = local_H(S, i, 0.0, 1.0, "dmrg");
         Dense v = two_site(S, i);
-        const int n = (int)(S.bond(S.x, i) * S.d * S.d * S.bond(S.x, i + 2));
-        E = lanczos_min(ctx, H.p(), n, v.p(), prm.krylov_dim > 0 ? prm.krylov_dim : 30,
-                        std::max(0, prm.restarts), 1e-12);
+        const int64_t n64 = (int64_t)S.bond(S.x, i) * S.d * S.d * S.bond(S.x, i + 2);
+        TNFA_CHECK(n64 < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "dmrg: two-site problem too large");
+        const int n = (int)n64;
+        const int kd = prm.krylov_dim > 0 ? prm.krylov_dim : 30;
+        if (n64 <= kLocalDenseSmall && !force_matrix_free()) {
+          Dense H = local_H(S, i, 0.0, 1.0, "dmrg");
+          const double* Hp = H.p();
+          E = lanczos_min(
+              ctx,
+              [&](const double* x, double* y) {
+                la::gemm<double>(ctx, {la::GemmJob{Hp, x, y, n, 1, n, n, 1, 1, 0, 0, 1.0, 0.0}});
+              },
+              n, v.p(), kd, std::max(0, prm.restarts), 1e-12);
+        } else {
+          LocalOp op(S, i, 0.0, 1.0);
+          E = lanczos_min(ctx, [&](const double* x, double* y) { op(x, y); }, n, v.p(), kd,
+                          std::max(0, prm.restarts), 1e-12);
+        }
         store_two_site(S, i, v, tp, st, dir == 0);
         // keep the state normalised after truncation: rescale the centre
         const int c = dir == 0 ? i + 1 : i;

@@ -152,3 +152,48 @@ def test_dmrg_lowest_laplacian_mode(ina):
     assert abs(E - w[0]) < 1e-9 * abs(w[0]), (E, w[:3])
     v = psi.evaluate_batch(_grid_2d(L), [1, 2])
     assert abs(abs(v @ V[:, 0]) / np.linalg.norm(v) - 1) < 1e-8
+
+
+_MATFREE_SCRIPT = r"""
+import json, sys
+sys.path.insert(0, sys.argv[1]); sys.path.insert(0, sys.argv[2]); sys.path.insert(0, sys.argv[3])
+import numpy as np
+import itensornumericalanalysis as ina
+import oracle as O
+from test_gpu_linsolve import _dense_operator, _grid_2d, _check
+L = 4
+g = ina.named_comb_tree((2, L))
+s = ina.continuous_siteinds(g, [[(1, j) for j in range(L, 0, -1)], [(2, j) for j in range(1, L + 1)]])
+terms = (O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2, dim=1)
+         + O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2, dim=2))
+axis_of = {(1, k): k - 1 for k in range(1, L + 1)}
+axis_of.update({(2, k): L + k - 1 for k in range(1, L + 1)})
+M = _dense_operator(terms, 2 * L, axis_of)
+A = ina.laplacian_operator(s)
+b = ina.rand_itn(s, link_space=2, rng=76)
+x = ina.linsolve(A, b, a0=1.0, a1=-1e-3, nsweeps=4, cutoff=0.0, tol=1e-12)
+err, res = _check(M, 1.0, -1e-3, b.evaluate_batch(_grid_2d(L), [1, 2]), x.evaluate_batch(_grid_2d(L), [1, 2]), 0)
+Au = ina.laplacian_operator(s, scale=False)
+E, psi = ina.dmrg(Au, ina.rand_itn(s, link_space=3, rng=77), nsweeps=6, maxdim=32, cutoff=1e-14)
+Mu = _dense_operator([(c / 4.0**L, o) for c, o in terms], 2 * L, axis_of)
+w = np.linalg.eigvalsh((Mu + Mu.T) / 2)
+print(json.dumps({"lin_err": err, "lin_res": res, "E": E, "E_ref": float(w[0])}))
+"""
+
+
+def test_matrix_free_two_site_paths(ina):
+    """The matrix-free two-site operator (GMRES for linsolve, Lanczos for
+    dmrg), forced at every size, gives the dense answers."""
+    import json
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    here = Path(__file__).resolve().parent
+    env = dict(os.environ, TNFA_LOCAL_MATRIX_FREE="1")
+    r = subprocess.run([sys.executable, "-c", _MATFREE_SCRIPT, str(here.parent / "itensornumericalanalysis.jl_gb300"),
+                        str(here.parent), str(here)], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["lin_res"] < 1e-9 and out["lin_err"] < 1e-9, out
+    assert abs(out["E"] - out["E_ref"]) < 1e-9 * abs(out["E_ref"]), out
