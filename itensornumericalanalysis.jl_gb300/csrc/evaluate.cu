@@ -1261,30 +1261,17 @@ void vjp_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, const double
       j.chi_a = 1;
       j.site_dim = Tp.site_dim[v];
       j.Pc = Pc;
-      // tiles of 256 points when their rows fit in shared memory (more work
-      // per CTA against the latency of gathering the rows), else 64
-      auto smem_for = [&](int tp) {
-        return (size_t)sumdim * tp * sizeof(T) + tp * sizeof(T) + 2 * tp * sizeof(int);
-      };
-      const bool big = smem_for(256) <= 160 * 1024;
-      const int tp = big ? 256 : 64;
-      group_by_site(ctx, j, dS.as<uint8_t>() + (int64_t)v * Pcap, Pc, j.site_dim, tp, meta,
+      constexpr int TP = 64;
+      group_by_site(ctx, j, dS.as<uint8_t>() + (int64_t)v * Pcap, Pc, j.site_dim, TP, meta,
                     dperm.as<int>());
-      const size_t sm = smem_for(tp);
+      const size_t sm = (size_t)sumdim * TP * sizeof(T) + TP * sizeof(T) + 2 * TP * sizeof(int);
       TNFA_CHECK(sm <= 200 * 1024, TNFA_ERR_UNSUPPORTED, "bonds too large for the gradient kernel");
-      dim3 grid((unsigned)((Pc + tp - 1) / tp + j.ngroups), (unsigned)((K + 255) / 256));
+      if (sm > 48 * 1024)
+        TNFA_CUDA(cudaFuncSetAttribute(k_grad_acc<T, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sm));
+      dim3 grid((unsigned)((Pc + TP - 1) / TP + j.ngroups), (unsigned)((K + 255) / 256));
       KernelScope ks(ctx, "grad_acc", 2.0 * Pc * (double)K, 0.0);
-      if (big) {
-        if (sm > 48 * 1024)
-          TNFA_CUDA(cudaFuncSetAttribute(k_grad_acc<T, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sm));
-        k_grad_acc<T, 256><<<grid, 256, sm, ctx->stream>>>(j, dT + Tp.off[v]);
-      } else {
-        if (sm > 48 * 1024)
-          TNFA_CUDA(cudaFuncSetAttribute(k_grad_acc<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sm));
-        k_grad_acc<T, 64><<<grid, 256, sm, ctx->stream>>>(j, dT + Tp.off[v]);
-      }
+      k_grad_acc<T, TP><<<grid, 256, sm, ctx->stream>>>(j, dT + Tp.off[v]);
       TNFA_LAUNCH_CHECK();
     }
   }
