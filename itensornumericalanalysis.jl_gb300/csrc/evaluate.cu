@@ -1027,8 +1027,32 @@ __global__ void __launch_bounds__(256) k_grad_acc(const VertexJob<T> j, T* __res
   __syncthreads();
   const int k = blockIdx.y * blockDim.x + threadIdx.x;
   if (k >= j.K) return;
+  // this thread's entry of every child row, decoded once (kr_entry per row
+  // would redo the integer divisions for every point)
+  int base[EVAL_MAXC], dim[EVAL_MAXC];
+  {
+    int kk = k, off = sumdim;
+    for (int c = j.nchild - 1; c >= 0; --c) {
+      const int d = j.ch[c].dim;
+      off -= d;
+      base[c] = off * TP + kk % d;
+      dim[c] = d;
+      kk /= d;
+    }
+  }
   T acc = Sc<T>::zero();
-  for (int r = 0; r < nrows; ++r) acc = Sc<T>::fma(scale[r], kr_entry(j, rows, TP, r, k), acc);
+  if (j.nchild == 2) {
+    const T* p0 = rows + base[0];
+    const T* p1 = rows + base[1];
+    const int d0 = dim[0], d1 = dim[1];
+    for (int r = 0; r < nrows; ++r) acc = Sc<T>::fma(scale[r], p0[r * d0] * p1[r * d1], acc);
+  } else {
+    for (int r = 0; r < nrows; ++r) {
+      T a = scale[r];
+      for (int c = 0; c < j.nchild; ++c) a = a * rows[base[c] + r * dim[c]];
+      acc = acc + a;
+    }
+  }
   atomic_add_T<T>(dT + (int64_t)g * j.K + k, acc);
 }
 
