@@ -165,22 +165,35 @@ template <> struct Frexp<float> {
 // Load the message rows of every child for the tile's points into shared
 // memory (child c at rows + choff_c * tp, row-major tp x dim_c), rescale each
 // row by 2^-e so that its largest entry lies in [0.5, 1), and accumulate the
-// exponents of the tile's points into eacc.
+// exponents of the tile's points into eacc.  The gather issues LU loads per
+// thread before storing any, so that a tile's rows are in flight together
+// rather than one load latency per element.
 template <class T>
 __device__ void load_children(const VertexJob<T>& j, const int* pts, int nrows, int tp, T* rows,
                               int* eacc) {
+  constexpr int LU = 8;
   int off = 0;
   for (int c = 0; c < j.nchild; ++c) {
     const ChildSrc<T> s = j.ch[c];
     T* dst = rows + (int64_t)off * tp;
-    for (int idx = threadIdx.x; idx < tp * s.dim; idx += blockDim.x) {
-      int r = idx / s.dim, i = idx - r * s.dim;
-      T v = Sc<T>::zero();
-      if (r < nrows) {
-        int p = pts[r];
-        v = s.S ? s.ptr[(int64_t)s.S[p] * s.dim + i] : s.ptr[(int64_t)p * s.dim + i];
+    const int n = tp * s.dim;
+    for (int i0 = threadIdx.x; i0 < n; i0 += blockDim.x * LU) {
+      T v[LU];
+#pragma unroll
+      for (int u = 0; u < LU; ++u) {
+        const int idx = i0 + u * (int)blockDim.x;
+        const int r = idx / s.dim, i = idx - r * s.dim;
+        v[u] = Sc<T>::zero();
+        if (idx < n && r < nrows) {
+          const int p = pts[r];
+          v[u] = s.S ? s.ptr[(int64_t)s.S[p] * s.dim + i] : s.ptr[(int64_t)p * s.dim + i];
+        }
       }
-      dst[idx] = v;
+#pragma unroll
+      for (int u = 0; u < LU; ++u) {
+        const int idx = i0 + u * (int)blockDim.x;
+        if (idx < n) dst[idx] = v[u];
+      }
     }
     off += s.dim;
   }
@@ -222,11 +235,15 @@ __device__ inline T kr_entry(const VertexJob<T>& j, const T* rows, int tp, int r
   return a;
 }
 
-// General SIMT contraction: CTA tile = TP points x 128 output columns,
-// 256 threads, register micro-tile (TP/8) x 4, K streamed in chunks of 16.
-template <class T, int TP>
+// General SIMT contraction: CTA tile = TP points x TA output columns, 256
+// threads as (256 / (TA / 4)) row threads x (TA / 4) column threads, each
+// with a (TP / row threads) x 4 register micro-tile; K streamed in chunks of
+// 16.  TA follows the parent bond (32, 64 or 128) so that thin bonds do not
+// pay for idle columns.
+template <class T, int TP, int TA>
 __global__ void __launch_bounds__(256) k_contract_gemm(const VertexJob<T> j) {
-  constexpr int TA = 128, KC = 16, RM = TP / 8;
+  constexpr int KC = 16, CT = TA / 4, RT = 256 / CT, RM = TP / RT;
+  static_assert(RM >= 1 && RM * RT == TP, "tile rows must cover the row threads");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int row0, nrows, g;
   if (!locate_tile(j, TP, blockIdx.x, row0, nrows, g)) return;
@@ -246,7 +263,7 @@ __global__ void __launch_bounds__(256) k_contract_gemm(const VertexJob<T> j) {
   load_children(j, pts, nrows, TP, rows, eacc);
 
   const T* Bg = j.B + (int64_t)g * j.chi_a * j.K;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int tx = threadIdx.x % CT, ty = threadIdx.x / CT;
   T acc[RM][4];
 #pragma unroll
   for (int i = 0; i < RM; ++i)
@@ -271,7 +288,7 @@ __global__ void __launch_bounds__(256) k_contract_gemm(const VertexJob<T> j) {
 #pragma unroll
       for (int i = 0; i < RM; ++i) av[i] = As[kk * TP + ty * RM + i];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) bv[q] = Bs[kk * TA + tx + 32 * q];
+      for (int q = 0; q < 4; ++q) bv[q] = Bs[kk * TA + tx + CT * q];
 #pragma unroll
       for (int i = 0; i < RM; ++i)
 #pragma unroll
@@ -286,7 +303,7 @@ __global__ void __launch_bounds__(256) k_contract_gemm(const VertexJob<T> j) {
     int p = pts[r];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      int a = a0 + tx + 32 * q;
+      int a = a0 + tx + CT * q;
       if (a < j.chi_a) j.out[(int64_t)p * j.chi_a + a] = acc[i][q];
     }
   }
@@ -296,9 +313,9 @@ __global__ void __launch_bounds__(256) k_contract_gemm(const VertexJob<T> j) {
 
 // Narrow outputs (chi_a <= 16): one warp per point, lanes split K, shuffle
 // reduction.  Used at the roots (chi_a = 1) and on thin bonds.
-template <class T>
+template <class T, int NA>
 __global__ void __launch_bounds__(256) k_contract_narrow(const VertexJob<T> j) {
-  constexpr int TP = 8, NA = 16;
+  constexpr int TP = 8;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int row0, nrows, g;
   if (!locate_tile(j, TP, blockIdx.x, row0, nrows, g)) return;
@@ -319,16 +336,36 @@ __global__ void __launch_bounds__(256) k_contract_narrow(const VertexJob<T> j) {
   T acc[NA];
 #pragma unroll
   for (int q = 0; q < NA; ++q) acc[q] = Sc<T>::zero();
-  for (int k = lane; k < j.K; k += 32) {
-    T a = kr_entry(j, rows, TP, r, k);
+  const int dl = j.nchild ? j.ch[j.nchild - 1].dim : 1;
+  if (j.nchild >= 1 && j.nchild <= 2 && dl >= 16) {
+    // lanes over the last child's entries, a loop over the other child's:
+    // no index decoding in the loop
+    const int offl = sumdim - dl;
+    const int Ko = j.K / dl;
+    const T* ml = rows + (int64_t)offl * TP + (int64_t)r * dl;
+    const T* m0 = rows + (int64_t)r * (j.nchild == 2 ? j.ch[0].dim : 0);
+    for (int ko = 0; ko < Ko; ++ko) {
+      const T ao = j.nchild == 2 ? m0[ko] : Sc<T>::one();
+      const T* Bk = Bg + (int64_t)ko * dl;
+      for (int kl = lane; kl < dl; kl += 32) {
+        const T a = ao * ml[kl];
 #pragma unroll
-    for (int q = 0; q < NA; ++q)
-      if (q < j.chi_a) acc[q] = Sc<T>::fma(a, Bg[(int64_t)q * j.K + k], acc[q]);
+        for (int q = 0; q < NA; ++q)
+          acc[q] = Sc<T>::fma(a, q < j.chi_a ? Bk[(int64_t)q * j.K + kl] : Sc<T>::zero(), acc[q]);
+      }
+    }
+  } else {
+    for (int k = lane; k < j.K; k += 32) {
+      T a = kr_entry(j, rows, TP, r, k);
+#pragma unroll
+      for (int q = 0; q < NA; ++q)
+        acc[q] = Sc<T>::fma(a, q < j.chi_a ? Bg[(int64_t)q * j.K + k] : Sc<T>::zero(), acc[q]);
+    }
   }
   int p = pts[r];
 #pragma unroll
   for (int q = 0; q < NA; ++q) {
-    if (q >= j.chi_a) break;
+    if (q >= j.chi_a) continue;
     T v = acc[q];
     for (int o = 16; o; o >>= 1) {
       if constexpr (sizeof(T) == 16) {
@@ -431,6 +468,22 @@ static EvalPlan make_plan(const Topo& T) {
   return P;
 }
 
+// Tile of k_contract_gemm for a parent bond chi_a > 16 and children rows of
+// sumdim entries: TP x TA with TA the smallest of 32 / 64 / 128 covering
+// chi_a, and TP = 4096 / TA (a 4 x 4 micro-tile per thread) while the
+// children rows of the tile fit in shared memory, else TP = 1024 / TA (one
+// row per thread).
+struct GemmTile {
+  int tp, ta;
+};
+static GemmTile gemm_tile(int chi_a, int sumdim, size_t tsize) {
+  const size_t row_bytes = (size_t)sumdim * tsize;
+  const int ta = chi_a <= 32 ? 32 : chi_a <= 64 ? 64 : 128;
+  const int tp = 4096 / ta;
+  if (row_bytes * tp + (size_t)16 * (tp + ta) * tsize <= 160 * 1024) return {tp, ta};
+  return {1024 / ta, ta};
+}
+
 template <class T> struct FamilyName;
 template <> struct FamilyName<double> { static constexpr const char* v = "contract_f64"; };
 template <> struct FamilyName<float> { static constexpr const char* v = "contract_f32"; };
@@ -448,40 +501,33 @@ static void launch_contract(tnfa_ctx* ctx, const VertexJob<T>& j, int Pc) {
     size_t sm = (size_t)sumdim * TP * sizeof(T) + 2 * TP * sizeof(int);
     TNFA_CHECK(sm <= 200 * 1024, TNFA_ERR_UNSUPPORTED, "children bonds too large for evaluation");
     if (sm > 48 * 1024)
-      TNFA_CUDA(cudaFuncSetAttribute(k_contract_narrow<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sm));
+      for (auto kern : {k_contract_narrow<T, 1>, k_contract_narrow<T, 4>, k_contract_narrow<T, 16>})
+        TNFA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     unsigned gx = (unsigned)((Pc + TP - 1) / TP + j.ngroups);
-    k_contract_narrow<T><<<gx, 256, sm, ctx->stream>>>(j);
+    // accumulators per lane: as many as the parent bond, so that they stay in registers
+    if (j.chi_a == 1) k_contract_narrow<T, 1><<<gx, 256, sm, ctx->stream>>>(j);
+    else if (j.chi_a <= 4) k_contract_narrow<T, 4><<<gx, 256, sm, ctx->stream>>>(j);
+    else k_contract_narrow<T, 16><<<gx, 256, sm, ctx->stream>>>(j);
   } else {
-    constexpr int TA = 128, KC = 16;
-    size_t row_bytes = (size_t)sumdim * sizeof(T);
-    unsigned gy = (unsigned)((j.chi_a + TA - 1) / TA);
-    if (row_bytes * 32 + (size_t)KC * (32 + TA) * sizeof(T) <= 160 * 1024) {
-      constexpr int TP = 32;
-      size_t sm = row_bytes * TP + (size_t)KC * (TP + TA) * sizeof(T) + 2 * TP * sizeof(int);
+    const GemmTile t = gemm_tile(j.chi_a, sumdim, sizeof(T));
+    const size_t sm = (size_t)sumdim * sizeof(T) * t.tp + (size_t)16 * (t.tp + t.ta) * sizeof(T) +
+                      2 * t.tp * sizeof(int);
+    TNFA_CHECK(sm <= 200 * 1024, TNFA_ERR_UNSUPPORTED, "children bonds too large for evaluation");
+    dim3 grid((unsigned)((Pc + t.tp - 1) / t.tp + j.ngroups), (unsigned)((j.chi_a + t.ta - 1) / t.ta));
+    auto go = [&](auto kern) {
       if (sm > 48 * 1024)
-        TNFA_CUDA(cudaFuncSetAttribute(k_contract_gemm<T, TP>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      dim3 grid((unsigned)((Pc + TP - 1) / TP + j.ngroups), gy);
-      k_contract_gemm<T, TP><<<grid, 256, sm, ctx->stream>>>(j);
-    } else {
-      constexpr int TP = 8;
-      size_t sm = row_bytes * TP + (size_t)KC * (TP + TA) * sizeof(T) + 2 * TP * sizeof(int);
-      TNFA_CHECK(sm <= 200 * 1024, TNFA_ERR_UNSUPPORTED, "children bonds too large for evaluation");
-      if (sm > 48 * 1024)
-        TNFA_CUDA(cudaFuncSetAttribute(k_contract_gemm<T, TP>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      dim3 grid((unsigned)((Pc + TP - 1) / TP + j.ngroups), gy);
-      k_contract_gemm<T, TP><<<grid, 256, sm, ctx->stream>>>(j);
-    }
+        TNFA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      kern<<<grid, 256, sm, ctx->stream>>>(j);
+    };
+    if (t.ta == 32) t.tp == 128 ? go(k_contract_gemm<T, 128, 32>) : go(k_contract_gemm<T, 32, 32>);
+    else if (t.ta == 64) t.tp == 64 ? go(k_contract_gemm<T, 64, 64>) : go(k_contract_gemm<T, 16, 64>);
+    else t.tp == 32 ? go(k_contract_gemm<T, 32, 128>) : go(k_contract_gemm<T, 8, 128>);
   }
   TNFA_LAUNCH_CHECK();
 }
 
 static int contract_tile_rows(int chi_a, int sumdim, size_t tsize) {
-  if (chi_a <= 16) return 8;
-  size_t row_bytes = (size_t)sumdim * tsize;
-  return (row_bytes * 32 + (size_t)16 * (32 + 128) * tsize <= 160 * 1024) ? 32 : 8;
+  return chi_a <= 16 ? 8 : gemm_tile(chi_a, sumdim, tsize).tp;
 }
 
 template <class T>
@@ -1006,54 +1052,94 @@ __device__ inline void atomic_add_T<cplx>(cplx* a, cplx v) {
   atomicAdd(&a->im, v.im);
 }
 
-template <class T, int TP>
-__global__ void __launch_bounds__(256) k_grad_acc(const VertexJob<T> j, T* __restrict__ dT) {
+// dT_v[g][k] += sum over the points p of site value g of scale_p * prod_c m_c[p][k_c]
+// (k decoded as the mixed-radix tuple of the child entries, last child
+// fastest).  Each CTA walks a contiguous run of tiles of tiles_per_cta point
+// tiles, keeps its partial sums in registers and adds them to dT once per site
+// value it met, so the atomics on the few thousand dT entries stay far from
+// the point count.
+template <class T, int TP, int KQ>
+__global__ void __launch_bounds__(256) k_grad_acc(const VertexJob<T> j, T* __restrict__ dT,
+                                                  int tiles_per_cta) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  int row0, nrows, g;
-  if (!locate_tile(j, TP, blockIdx.x, row0, nrows, g)) return;
   int sumdim = 0;
   for (int c = 0; c < j.nchild; ++c) sumdim += j.ch[c].dim;
   T* rows = (T*)smem_raw;
   T* scale = rows + (int64_t)sumdim * TP;
   int* pts = (int*)(scale + TP);
   int* eacc = pts + TP;
-  for (int r = threadIdx.x; r < TP; r += blockDim.x) {
-    pts[r] = r < nrows ? (j.perm ? j.perm[row0 + r] : row0 + r) : 0;
-    eacc[r] = 0;
+  // KQ entries k = blockIdx.y * 256 KQ + threadIdx.x + 256 q per thread, each
+  // with its child row offsets decoded once
+  int kq[KQ], off0[KQ], off1[KQ];
+#pragma unroll
+  for (int q = 0; q < KQ; ++q) {
+    kq[q] = blockIdx.y * blockDim.x * KQ + threadIdx.x + blockDim.x * q;
+    int kk = kq[q] < j.K ? kq[q] : 0;
+    // the general product below decodes per point; two children (the common
+    // case: the outside message and one child) keep both offsets here
+    const int d1 = j.nchild > 1 ? j.ch[1].dim : 1;
+    off0[q] = (kk / d1);
+    off1[q] = j.ch[0].dim * TP + kk % d1;
   }
-  __syncthreads();
-  load_children(j, pts, nrows, TP, rows, eacc);
-  for (int r = threadIdx.x; r < nrows; r += blockDim.x) scale[r] = Sc<T>::scale2(Sc<T>::one(), eacc[r]);
-  __syncthreads();
-  const int k = blockIdx.y * blockDim.x + threadIdx.x;
-  if (k >= j.K) return;
-  // this thread's entry of every child row, decoded once (kr_entry per row
-  // would redo the integer divisions for every point)
-  int base[EVAL_MAXC], dim[EVAL_MAXC];
-  {
-    int kk = k, off = sumdim;
-    for (int c = j.nchild - 1; c >= 0; --c) {
-      const int d = j.ch[c].dim;
-      off -= d;
-      base[c] = off * TP + kk % d;
-      dim[c] = d;
-      kk /= d;
+  const int ntiles = j.tile_start[j.ngroups];
+  const int b0 = blockIdx.x * tiles_per_cta;
+  const int b1 = min(ntiles, b0 + tiles_per_cta);
+  T acc[KQ];
+#pragma unroll
+  for (int q = 0; q < KQ; ++q) acc[q] = Sc<T>::zero();
+  int gcur = -1;
+  for (int b = b0; b < b1; ++b) {
+    int row0, nrows, g;
+    if (!locate_tile(j, TP, b, row0, nrows, g)) continue;  // uniform over the CTA
+    if (g != gcur) {
+      if (gcur >= 0)
+#pragma unroll
+        for (int q = 0; q < KQ; ++q)
+          if (kq[q] < j.K) atomic_add_T<T>(dT + (int64_t)gcur * j.K + kq[q], acc[q]);
+#pragma unroll
+      for (int q = 0; q < KQ; ++q) acc[q] = Sc<T>::zero();
+      gcur = g;
+    }
+    __syncthreads();  // the previous tile's rows are no longer read
+    for (int r = threadIdx.x; r < TP; r += blockDim.x) {
+      pts[r] = r < nrows ? (j.perm ? j.perm[row0 + r] : row0 + r) : 0;
+      eacc[r] = 0;
+    }
+    __syncthreads();
+    load_children(j, pts, nrows, TP, rows, eacc);
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) scale[r] = Sc<T>::scale2(Sc<T>::one(), eacc[r]);
+    __syncthreads();
+    if (j.nchild == 2) {
+      const int d0 = j.ch[0].dim, d1 = j.ch[1].dim;
+      for (int r = 0; r < nrows; ++r) {
+        const T sc = scale[r];
+        const T* r0 = rows + r * d0;
+        const T* r1 = rows + r * d1;
+#pragma unroll
+        for (int q = 0; q < KQ; ++q) acc[q] = Sc<T>::fma(sc * r0[off0[q]], r1[off1[q]], acc[q]);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < KQ; ++q) {
+        if (kq[q] >= j.K) continue;
+        for (int r = 0; r < nrows; ++r) {
+          T a = scale[r];
+          int kk = kq[q], off = sumdim;
+          for (int c = j.nchild - 1; c >= 0; --c) {
+            const int d = j.ch[c].dim;
+            off -= d;
+            a = a * rows[off * TP + r * d + kk % d];
+            kk /= d;
+          }
+          acc[q] = acc[q] + a;
+        }
+      }
     }
   }
-  T acc = Sc<T>::zero();
-  if (j.nchild == 2) {
-    const T* p0 = rows + base[0];
-    const T* p1 = rows + base[1];
-    const int d0 = dim[0], d1 = dim[1];
-    for (int r = 0; r < nrows; ++r) acc = Sc<T>::fma(scale[r], p0[r * d0] * p1[r * d1], acc);
-  } else {
-    for (int r = 0; r < nrows; ++r) {
-      T a = scale[r];
-      for (int c = 0; c < j.nchild; ++c) a = a * rows[base[c] + r * dim[c]];
-      acc = acc + a;
-    }
-  }
-  atomic_add_T<T>(dT + (int64_t)g * j.K + k, acc);
+  if (gcur >= 0)
+#pragma unroll
+    for (int q = 0; q < KQ; ++q)
+      if (kq[q] < j.K) atomic_add_T<T>(dT + (int64_t)gcur * j.K + kq[q], acc[q]);
 }
 
 template <class T>
@@ -1290,12 +1376,22 @@ void vjp_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, const double
                     dperm.as<int>());
       const size_t sm = (size_t)sumdim * TP * sizeof(T) + TP * sizeof(T) + 2 * TP * sizeof(int);
       TNFA_CHECK(sm <= 200 * 1024, TNFA_ERR_UNSUPPORTED, "bonds too large for the gradient kernel");
+      constexpr int KQ = 4;
+      auto kern = k_grad_acc<T, TP, KQ>;
       if (sm > 48 * 1024)
-        TNFA_CUDA(cudaFuncSetAttribute(k_grad_acc<T, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)sm));
-      dim3 grid((unsigned)((Pc + TP - 1) / TP + j.ngroups), (unsigned)((K + 255) / 256));
+        TNFA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      // one wave of resident CTAs, each over a run of consecutive tiles
+      int occ = 0, nsm = 0, dev = 0;
+      TNFA_CUDA(cudaGetDevice(&dev));
+      TNFA_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      TNFA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, sm));
+      const int ntiles = (int)((Pc + TP - 1) / TP + j.ngroups);
+      const int ky = (int)((K + 256 * KQ - 1) / (256 * KQ));
+      const int want = std::max(1, std::max(occ, 1) * nsm / ky);
+      const int per = std::max(1, (ntiles + want - 1) / want);
+      dim3 grid((unsigned)((ntiles + per - 1) / per), (unsigned)ky);
       KernelScope ks(ctx, "grad_acc", 2.0 * Pc * (double)K, 0.0);
-      k_grad_acc<T, TP><<<grid, 256, sm, ctx->stream>>>(j, dT + Tp.off[v]);
+      kern<<<grid, 256, sm, ctx->stream>>>(j, dT + Tp.off[v], per);
       TNFA_LAUNCH_CHECK();
     }
   }
