@@ -44,9 +44,11 @@ from .elementary_operators import (
     map_to_zeros,
     multiply,
     operator_proj,
+    opsum_to_operator,
     second_derivative_operator,
     stencil,
     third_derivative_operator,
+    ttn,
 )
 from .graphs import (
     NamedGraph,

@@ -31,11 +31,19 @@ _OPS = {
 }
 
 
-def _op_matrix(name: str, base: int) -> np.ndarray:
+def _op_matrix(name, base: int) -> np.ndarray:
+    """A digit operator by name, or a base x base matrix M[out, in] given directly."""
+    if not isinstance(name, str):
+        m = np.asarray(name)
+        if m.shape != (base, base):
+            raise ValueError(f"a site operator on a base-{base} digit must be {base}x{base}")
+        return m
     if name == "I":
         return np.eye(base)
     if base != 2:
         raise ValueError("digit shift operators are defined for base 2")
+    if name not in _OPS:
+        raise ValueError(f"unknown digit operator {name!r}")
     return _OPS[name]
 
 
@@ -69,7 +77,8 @@ class ITensorNetworkOperator(ITensorNetworkFunction):
 
 # ------------------------------------------------------------ OpSums ----
 class OpSum:
-    """Sum of products of digit operators; a term maps (dim, digit) -> op name."""
+    """Sum of products of digit operators; a term maps (dim, digit) to an op
+    name ("D+", "D-", "Dup", "Ddn", "I") or a base x base matrix M[out, in]."""
 
     def __init__(self, terms=None):
         self.terms: list[tuple[complex, dict]] = list(terms or [])
@@ -141,14 +150,54 @@ def _site_op(s: IndsNetworkMap, v, ops: dict) -> np.ndarray:
     return t
 
 
+# Terms per direct-sum block: an OpSum longer than this is compiled block by
+# block, each block compressed, and the blocks summed with a compression
+# after every addition, so that no bond before compression exceeds a block
+# plus the running sum's rank.
+OPSUM_BLOCK = 64
+
+
 def opsum_to_operator(s: IndsNetworkMap, opsum: OpSum, cutoff: float = 1e-15,
                       scale_dims: dict | None = None, compress: bool = True):
-    """Block-diagonal direct sum of the OpSum's product terms (bond = number of
-    terms), coefficients on the first vertex, then compressed on the device."""
-    lay = s.layout
+    """The OpSum as a tree operator (ITensorNetworks' ttn(OpSum; cutoff), used
+    by src/elementary_operators.jl:114,119,151): a block-diagonal direct sum
+    of the product terms (bond = number of terms), coefficients on the first
+    vertex, then compressed on the device by truncation with the relative
+    cutoff.  Up to gauge this is the operator ttn(OpSum) returns; the ranks
+    are the SVD-minimal ones at that cutoff."""
     terms = opsum.terms
+    if not terms:
+        raise ValueError("an empty OpSum has no operator")
+    if compress and len(terms) > OPSUM_BLOCK:
+        op = None
+        for b0 in range(0, len(terms), OPSUM_BLOCK):
+            part = _direct_sum(s, terms[b0:b0 + OPSUM_BLOCK])
+            part = _compress(part, cutoff) if len(terms[b0:b0 + OPSUM_BLOCK]) > 1 else part
+            op = part if op is None else _compress(op + part, cutoff)
+        if scale_dims:
+            for v, f in scale_dims.items():
+                op.scale_vertex(v, f)
+        return op
+    op = _direct_sum(s, terms)
+    if scale_dims:
+        for v, f in scale_dims.items():
+            op.scale_vertex(v, f)
+    if compress and len(terms) > 1:
+        op = _compress(op, cutoff)
+    return op
+
+
+def ttn(opsum: OpSum, s: IndsNetworkMap, cutoff: float = 1e-15) -> "ITensorNetworkOperator":
+    """ITensorNetworks' ttn(os::OpSum, s; cutoff) as the reference calls it
+    (src/elementary_operators.jl:114,119,151)."""
+    return opsum_to_operator(s, opsum, cutoff=cutoff)
+
+
+def _direct_sum(s: IndsNetworkMap, terms) -> "ITensorNetworkOperator":
+    lay = s.layout
     T = len(terms)
-    real = all(np.isreal(c) for c, _ in terms)
+    real = all(np.isreal(c) and all(isinstance(o, str) or not np.iscomplexobj(o) for o in ops.values())
+               for c, ops in terms)
     dtype = float if real else complex
     ts = {}
     for i, v in enumerate(lay.order):
@@ -162,13 +211,7 @@ def opsum_to_operator(s: IndsNetworkMap, opsum: OpSum, cutoff: float = 1e-15,
             # += : a lone root (no bonds at all) sums the terms in place
             out[(Ellipsis,) + idx] += site[t] * (coef if i == 0 else 1.0)
         ts[v] = out
-    op = ITensorNetworkOperator.from_tensors(s, ts, legs=operator_legs(s))
-    if scale_dims:
-        for v, f in scale_dims.items():
-            op.scale_vertex(v, f)
-    if compress and T > 1:
-        op = _compress(op, cutoff)
-    return op
+    return ITensorNetworkOperator.from_tensors(s, ts, legs=operator_legs(s))
 
 
 def _compress(op: ITensorNetworkOperator, cutoff: float) -> ITensorNetworkOperator:

@@ -338,3 +338,48 @@ def test_batched_apply_matches_single(ina):
     for g, t in zip(outs, tr):
         a, b = t.evaluate_batch(X), g.evaluate_batch(X)
         assert np.linalg.norm(a - b) <= 1e-2 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("block", [8, 1000])
+def test_general_opsum_compiles_to_its_dense_operator(ina, block, monkeypatch):
+    """A long OpSum of digit operators and explicit 2 x 2 site matrices (the
+    ttn(OpSum) call of src/elementary_operators.jl:151, widened to arbitrary
+    product terms): the compiled operator applied to f equals the term-by-term
+    sum on the dense grid, whether it is compiled in one direct sum or in
+    blocks of 8 terms summed with recompression."""
+    import itensornumericalanalysis.elementary_operators as eo
+    from oracle.itn import OPS
+
+    monkeypatch.setattr(eo, "OPSUM_BLOCK", block)
+    L = 8
+    s = ina.continuous_siteinds(ina.named_path_graph(L))
+    f = ina.rand_itn(s, link_space=4, rng=90, normalize=True)
+    rng = np.random.default_rng(91)
+    names = ["D+", "D-", "Dup", "Ddn"]
+    opsum = ina.OpSum()
+    dense_terms = []
+    for _ in range(150):
+        digits = rng.choice(np.arange(1, L + 1), size=int(rng.integers(1, 4)), replace=False)
+        ops, mats = {}, {}
+        for k in digits:
+            if rng.random() < 0.3:
+                m = rng.standard_normal((2, 2))
+                ops[(1, int(k))], mats[int(k)] = m, m
+            else:
+                nm = names[int(rng.integers(0, 4))]
+                ops[(1, int(k))], mats[int(k)] = nm, OPS[nm]
+        c = float(rng.standard_normal())
+        opsum.add(c, ops)
+        dense_terms.append((c, mats))
+    op = ina.ttn(opsum, s, cutoff=1e-15)
+    g = ina.operate(op, f, cutoff=0.0)
+    xs = _grid(L)
+    F = f.evaluate_batch(xs).reshape((2,) * L)
+    G = np.zeros_like(F)
+    for c, mats in dense_terms:
+        H = F
+        for k, m in mats.items():  # digit k is axis k - 1 (most significant first)
+            H = np.moveaxis(np.tensordot(m, H, axes=([1], [k - 1])), 0, k - 1)
+        G = G + c * H
+    assert rel_err(g.evaluate_batch(xs), G.reshape(-1)) < 1e-10
+    assert op.maxlinkdim() <= 4 ** (L // 2)  # the rank bound of an operator on L / 2 digits
