@@ -182,6 +182,30 @@ int tnfa_evaluate_noalloc(tnfa_ctx* ctx, const tnfa_net* net, const double* X, i
                           int32_t n_dims, const int32_t* dims, void* out, int out_kind,
                           int precision);
 
+/* Captured evaluation for repeated calls on fixed device buffers: the
+ * kernel sequence of tnfa_evaluate_noalloc for n_points points read from X
+ * and written to out (both device pointers, fixed for the plan's life) is run
+ * once eagerly (validating the inputs; out holds its result), then captured
+ * into a CUDA graph over scratch the plan owns.  tnfa_eval_plan_launch
+ * enqueues one graph launch on the context's stream: it evaluates whatever X
+ * holds at that point in stream order and returns without waiting.
+ * tnfa_eval_plan_check waits for the stream and reports TNFA_ERR_DOMAIN if
+ * the last launch met a negative or non-finite coordinate.  The plan reads
+ * the network's tensors where they were at creation: the network must
+ * outlive the plan, and in-place changes to its values are seen by later
+ * launches.  No counterpart in the reference (one evaluate call per point,
+ * itensornetworkfunction.jl:96-112); it serves latency-bound loops
+ * (optimisers, samplers) that evaluate the same number of points many times.
+ * Precision as for tnfa_evaluate_noalloc.  Do not call from inside another
+ * stream capture. */
+typedef struct tnfa_eval_plan tnfa_eval_plan;
+int tnfa_eval_plan_create(tnfa_ctx* ctx, const tnfa_net* net, const double* X, int64_t n_points,
+                          int32_t n_dims, const int32_t* dims, void* out, int out_kind,
+                          int precision, tnfa_eval_plan** plan);
+int tnfa_eval_plan_launch(tnfa_ctx* ctx, tnfa_eval_plan* plan);
+int tnfa_eval_plan_check(tnfa_ctx* ctx, tnfa_eval_plan* plan);
+int tnfa_eval_plan_destroy(tnfa_eval_plan* plan);
+
 /* ---- integration -------------------------------------------------------- */
 
 /* Left Riemann sum over [0,1)^n: contract every site leg with the uniform

@@ -146,6 +146,7 @@ struct tnfa_ctx {
   size_t eval_budget = 0;  // bytes of device scratch an evaluate call may hold
   std::string last_error;
   bool timing = false;
+  bool capturing = false;  // a stream capture is open: no events, no syncs
   std::vector<tnfa::KernelFamily> families;
   std::vector<cudaEvent_t> event_pool;
 };

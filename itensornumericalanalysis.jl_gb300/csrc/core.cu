@@ -189,7 +189,7 @@ KernelScope::KernelScope(tnfa_ctx* c, const char* family, double fl, double byte
   f.launches += 1;
   f.flops += fl;
   f.bytes += bytes;
-  if (ctx->timing || trace_on()) {
+  if (!ctx->capturing && (ctx->timing || trace_on())) {
     e0 = take_event(ctx);
     e1 = take_event(ctx);
     if (e0 && e1) cudaEventRecord(e0, ctx->stream);

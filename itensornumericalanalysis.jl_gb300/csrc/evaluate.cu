@@ -823,6 +823,7 @@ extern "C" int tnfa_evaluate(tnfa_ctx* ctx, const tnfa_net* net, const double* X
 // tnfa_evaluate_noalloc: the same digitize / group / contract / combine
 // kernels as tnfa_evaluate, with every scratch buffer carved out of one
 // file-scope device array instead of the stream-ordered allocator.
+#include <array>
 #include <mutex>
 
 namespace tnfa {
@@ -862,39 +863,66 @@ struct Carve {
   }
 };
 
+// The pieces evaluate_noalloc_impl carves for P points, in order: digit
+// program, digits, permutation, group tables, error flag, message slots,
+// slot exponents, root values, root exponents.
+template <class T>
+std::array<size_t, 9> noalloc_sizes(const tnfa_net* net, const EvalPlan& plan, int64_t P,
+                                    size_t prog_entries) {
+  const Topo& Tp = net->topo;
+  const int V = Tp.V;
+  const int nroots = (int)plan.roots.size();
+  int maxsd = 1;
+  for (int v = 0; v < V; ++v) maxsd = std::max(maxsd, Tp.site_dim[v]);
+  const size_t slot_vals = (size_t)P * plan.chimax;
+  return {prog_entries * sizeof(DigitEntry),
+          (size_t)V * P,
+          (size_t)P * 4,
+          group_meta_ints(maxsd) * 4,
+          4,
+          (size_t)plan.nslots * slot_vals * sizeof(T),
+          (size_t)plan.nslots * P * sizeof(int),
+          (size_t)nroots * P * sizeof(T),
+          (size_t)nroots * P * sizeof(int)};
+}
+
+// Scratch bytes evaluate_noalloc_impl carves for P points (256-byte aligned pieces).
+template <class T>
+size_t noalloc_bytes(const tnfa_net* net, int64_t P, size_t prog_entries) {
+  Carve dry{nullptr, ~(size_t)0};
+  for (size_t s : noalloc_sizes<T>(net, make_plan(net->topo), P, prog_entries)) dry.take_off(s);
+  return dry.used;
+}
+
+// The evaluation kernels over scratch carved from [base, base + cap).  With
+// check, the digit program is copied in from the host and the call ends by
+// reading the error flag (a host sync); without it (stream capture), the
+// program must already sit at the start of the scratch and the call only
+// enqueues work.  *err_flag receives the device address of the error flag.
 template <class T>
 void evaluate_noalloc_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, const double* X,
                            int64_t P64, int ncols, const std::vector<DigitEntry>& prog, void* out,
-                           int out_kind) {
+                           int out_kind, unsigned char* base, size_t cap, bool check,
+                           int** err_flag = nullptr) {
   const Topo& Tp = net->topo;
   const int V = Tp.V;
   EvalPlan plan = make_plan(Tp);
   const int nroots = (int)plan.roots.size();
-  int maxsd = 1;
-  for (int v = 0; v < V; ++v) maxsd = std::max(maxsd, Tp.site_dim[v]);
   // Dry run of the carving to size the request before touching the device.
   const int64_t P = P64;
   const size_t slot_vals = (size_t)P * plan.chimax;
-  size_t sizes[] = {prog.size() * sizeof(DigitEntry),
-                    (size_t)V * P,
-                    (size_t)P * 4,
-                    group_meta_ints(maxsd) * 4,
-                    4,
-                    (size_t)plan.nslots * slot_vals * sizeof(T),
-                    (size_t)plan.nslots * P * sizeof(int),
-                    (size_t)nroots * P * sizeof(T),
-                    (size_t)nroots * P * sizeof(int)};
-  Carve dry{nullptr, NOALLOC_BYTES};
+  const std::array<size_t, 9> sizes = noalloc_sizes<T>(net, plan, P, prog.size());
+  Carve dry{nullptr, cap};
   for (size_t s : sizes) dry.take_off(s);
-  if (dry.used > NOALLOC_BYTES) {
+  if (dry.used > cap) {
     const size_t per_point = (dry.used - prog.size() * sizeof(DigitEntry)) / (size_t)std::max<int64_t>(P, 1) + 1;
     fail(TNFA_ERR_INVALID_ARGUMENT,
          "tnfa_evaluate_noalloc: " + std::to_string(P) + " points need " +
              std::to_string(dry.used) + " bytes of scratch, above the fixed " +
-             std::to_string(NOALLOC_BYTES) + "; this network allows about " +
-             std::to_string(NOALLOC_BYTES / per_point) + " points per call");
+             std::to_string(cap) + "; this network allows about " +
+             std::to_string(cap / per_point) + " points per call");
   }
-  Carve cv{noalloc_base(ctx->device), NOALLOC_BYTES};
+  Carve cv{base, cap};
   DigitEntry* dprog = (DigitEntry*)cv.take(sizes[0]);
   uint8_t* dS = (uint8_t*)cv.take(sizes[1]);
   int* dperm = (int*)cv.take(sizes[2]);
@@ -906,10 +934,12 @@ void evaluate_noalloc_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors,
   int* roote = (int*)cv.take(sizes[8]);
   const int Pc = (int)P;
   // the array keeps the previous call's contents: clear what must start at 0
+  if (err_flag) *err_flag = derr;
   TNFA_CUDA(cudaMemsetAsync(derr, 0, 4, ctx->stream));
   TNFA_CUDA(cudaMemsetAsync(dS, 0, (size_t)V * P, ctx->stream));
   if (!prog.empty()) {
-    TNFA_CUDA(cudaMemcpyAsync(dprog, prog.data(), sizes[0], cudaMemcpyHostToDevice, ctx->stream));
+    if (check)
+      TNFA_CUDA(cudaMemcpyAsync(dprog, prog.data(), sizes[0], cudaMemcpyHostToDevice, ctx->stream));
     k_digitize<<<grid_for(Pc, 256, 8 * 152 * 8), 256, 0, ctx->stream>>>(
         X, ncols, Pc, dprog, (int)prog.size(), dS, (int64_t)P, derr);
     TNFA_LAUNCH_CHECK();
@@ -977,6 +1007,7 @@ void evaluate_noalloc_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors,
   k_combine<T><<<grid_for(Pc, 256, 8192), 256, 0, ctx->stream>>>(rootv, roote, nroots, Pc, out,
                                                                    out_kind, P, 0);
   TNFA_LAUNCH_CHECK();
+  if (!check) return;
   int herr = 0;
   TNFA_CUDA(cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, ctx->stream));
   TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1006,23 +1037,158 @@ extern "C" int tnfa_evaluate_noalloc(tnfa_ctx* ctx, const tnfa_net* net, const d
     TNFA_CHECK(out_kind == TNFA_OUT_C128 && precision == TNFA_PREC_F64, TNFA_ERR_DTYPE,
                "complex networks: TNFA_OUT_C128 and TNFA_PREC_F64");
     evaluate_noalloc_impl<cplx>(ctx, net, (const cplx*)net->d, X, n_points, ncols, prog, out,
-                                out_kind);
+                                out_kind, noalloc_base(ctx->device), NOALLOC_BYTES, true);
   } else {
     TNFA_CHECK(out_kind == TNFA_OUT_F64 || out_kind == TNFA_OUT_F32 ||
                    out_kind == TNFA_OUT_F32_SCALED,
                TNFA_ERR_DTYPE, "real networks need a real output kind");
     if (precision == TNFA_PREC_F64 && net->dtype == TNFA_F64)
       evaluate_noalloc_impl<double>(ctx, net, (const double*)net->d, X, n_points, ncols, prog, out,
-                                    out_kind);
+                                    out_kind, noalloc_base(ctx->device), NOALLOC_BYTES, true);
     else if (precision == TNFA_PREC_F32 && net->dtype == TNFA_F32)
       evaluate_noalloc_impl<float>(ctx, net, (const float*)net->d, X, n_points, ncols, prog, out,
-                                   out_kind);
+                                   out_kind, noalloc_base(ctx->device), NOALLOC_BYTES, true);
     else
       fail(TNFA_ERR_UNSUPPORTED,
            "tnfa_evaluate_noalloc computes in the network's own type: TNFA_PREC_F64 on FP64 "
            "networks or TNFA_PREC_F32 on FP32 networks");
   }
   TNFA_API_END
+}
+
+// ------------------------------------------------ captured evaluation ----
+// tnfa_eval_plan: the no-allocation kernel sequence for fixed device buffers
+// (X, out) and a fixed point count, captured once into a CUDA graph over
+// scratch the plan owns, then replayed with one graph launch per call.  For
+// small batches evaluation is launch-bound (about four launches per vertex),
+// and the replay removes the per-launch host cost.
+struct tnfa_eval_plan {
+  tnfa_ctx* ctx = nullptr;
+  const tnfa_net* net = nullptr;
+  void* scratch = nullptr;
+  int* derr = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t n_points = 0;
+};
+
+namespace tnfa {
+namespace {
+void plan_free(tnfa_eval_plan* p) {
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->scratch) cudaFree(p->scratch);
+  if (p->ctx) ctx_release(p->ctx);
+  delete p;
+}
+
+template <class T>
+void plan_build(tnfa_eval_plan* p, const T* tensors, const double* X, int ncols,
+                const std::vector<DigitEntry>& prog, void* out, int out_kind) {
+  tnfa_ctx* ctx = p->ctx;
+  const size_t bytes = noalloc_bytes<T>(p->net, p->n_points, prog.size());
+  TNFA_CUDA(cudaMalloc(&p->scratch, bytes));
+  // one eager run: validates the inputs, sets kernel attributes, stages the
+  // digit program at the start of the scratch (where the capture expects it)
+  evaluate_noalloc_impl<T>(ctx, p->net, tensors, X, p->n_points, ncols, prog, out, out_kind,
+                           (unsigned char*)p->scratch, bytes, true, &p->derr);
+  cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  TNFA_CUDA(cudaStreamBeginCapture(ctx->stream, mode));
+  ctx->capturing = true;
+  try {
+    evaluate_noalloc_impl<T>(ctx, p->net, tensors, X, p->n_points, ncols, prog, out, out_kind,
+                             (unsigned char*)p->scratch, bytes, false);
+  } catch (...) {
+    ctx->capturing = false;
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(ctx->stream, &g);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    throw;
+  }
+  ctx->capturing = false;
+  TNFA_CUDA(cudaStreamEndCapture(ctx->stream, &p->graph));
+  TNFA_CUDA(cudaGraphInstantiate(&p->exec, p->graph, 0));
+}
+}  // namespace
+}  // namespace tnfa
+
+extern "C" int tnfa_eval_plan_create(tnfa_ctx* ctx, const tnfa_net* net, const double* X,
+                                     int64_t n_points, int32_t n_dims, const int32_t* dims,
+                                     void* out, int out_kind, int precision,
+                                     tnfa_eval_plan** plan) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(net, "eval_plan_create");
+  TNFA_CHECK(plan, TNFA_ERR_INVALID_ARGUMENT, "null plan");
+  *plan = nullptr;
+  TNFA_CHECK(n_points > 0 && n_points < (int64_t(1) << 31), TNFA_ERR_INVALID_ARGUMENT,
+             "n_points must be in [1, 2^31)");
+  TNFA_CHECK(X && out && (n_dims == 0 || dims), TNFA_ERR_INVALID_ARGUMENT, "null X, out or dims");
+  TNFA_CHECK(n_dims >= 0 && n_dims <= 64, TNFA_ERR_INVALID_ARGUMENT, "n_dims out of range");
+  for (int v = 0; v < net->topo.V; ++v)
+    TNFA_CHECK(net->topo.site_dim[v] <= 256, TNFA_ERR_UNSUPPORTED, "site dimension above 256");
+  int ncols = 0;
+  std::vector<DigitEntry> prog = make_digit_program(net->topo, n_dims, dims, &ncols);
+  tnfa_eval_plan* p = new tnfa_eval_plan;
+  p->ctx = ctx;
+  ctx->refs += 1;
+  p->net = net;
+  p->n_points = n_points;
+  try {
+    if (net->dtype == TNFA_C128) {
+      TNFA_CHECK(out_kind == TNFA_OUT_C128 && precision == TNFA_PREC_F64, TNFA_ERR_DTYPE,
+                 "complex networks: TNFA_OUT_C128 and TNFA_PREC_F64");
+      plan_build<cplx>(p, (const cplx*)net->d, X, ncols, prog, out, out_kind);
+    } else {
+      TNFA_CHECK(out_kind == TNFA_OUT_F64 || out_kind == TNFA_OUT_F32 ||
+                     out_kind == TNFA_OUT_F32_SCALED,
+                 TNFA_ERR_DTYPE, "real networks need a real output kind");
+      if (precision == TNFA_PREC_F64 && net->dtype == TNFA_F64)
+        plan_build<double>(p, (const double*)net->d, X, ncols, prog, out, out_kind);
+      else if (precision == TNFA_PREC_F32 && net->dtype == TNFA_F32)
+        plan_build<float>(p, (const float*)net->d, X, ncols, prog, out, out_kind);
+      else
+        fail(TNFA_ERR_UNSUPPORTED,
+             "an evaluation plan computes in the network's own type: TNFA_PREC_F64 on FP64 "
+             "networks or TNFA_PREC_F32 on FP32 networks");
+    }
+  } catch (...) {
+    plan_free(p);
+    throw;
+  }
+  *plan = p;
+  TNFA_API_END
+}
+
+extern "C" int tnfa_eval_plan_launch(tnfa_ctx* ctx, tnfa_eval_plan* plan) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  TNFA_CHECK(plan && plan->exec && plan->ctx == ctx, TNFA_ERR_INVALID_ARGUMENT,
+             "not a plan of this context");
+  TNFA_CUDA(cudaGraphLaunch(plan->exec, ctx->stream));
+  TNFA_API_END
+}
+
+extern "C" int tnfa_eval_plan_check(tnfa_ctx* ctx, tnfa_eval_plan* plan) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  TNFA_CHECK(plan && plan->derr && plan->ctx == ctx, TNFA_ERR_INVALID_ARGUMENT,
+             "not a plan of this context");
+  int herr = 0;
+  TNFA_CUDA(cudaMemcpyAsync(&herr, plan->derr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  TNFA_CHECK(herr == 0, TNFA_ERR_DOMAIN,
+             "a coordinate is negative or not finite (the digit map needs x >= 0)");
+  TNFA_API_END
+}
+
+extern "C" int tnfa_eval_plan_destroy(tnfa_eval_plan* plan) {
+  if (!plan) return TNFA_OK;
+  cudaStreamSynchronize(plan->ctx->stream);
+  tnfa::plan_free(plan);
+  return TNFA_OK;
 }
 
 // ----------------------------------------------- vector-Jacobian product ----

@@ -779,13 +779,19 @@ void jacobi(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, Jaco
 constexpr int LU_NB = 32;
 
 // Factor columns k..k+kb-1 (rows k..n-1); row swaps inside the panel only.
-__global__ void __launch_bounds__(512) k_lu_panel(double* A, int n, int k, int kb, int* piv,
+// For each column the pivot row's panel segment goes to shared memory and
+// every thread loads the whole panel segment of each of its rows at once
+// (LU_NB independent loads), so a column step costs one memory latency per
+// row a thread owns rather than one per entry.
+__global__ void __launch_bounds__(256) k_lu_panel(double* A, int n, int k, int kb, int* piv,
                                                   int* singular) {
   __shared__ double vmax[32];
   __shared__ int imax[32];
   __shared__ int p_sh;
+  __shared__ double prow[LU_NB];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int j = k; j < k + kb; ++j) {
+  for (int jj = 0; jj < kb; ++jj) {
+    const int j = k + jj;
     double best = -1.0;
     int bi = j;
     for (int r = j + threadIdx.x; r < n; r += blockDim.x) {
@@ -809,33 +815,44 @@ __global__ void __launch_bounds__(512) k_lu_panel(double* A, int n, int k, int k
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      double b = -1.0;
+      double bb = -1.0;
       int i = j;
       for (int w = 0; w < nw; ++w)
-        if (vmax[w] > b || (vmax[w] == b && imax[w] < i)) {
-          b = vmax[w];
+        if (vmax[w] > bb || (vmax[w] == bb && imax[w] < i)) {
+          bb = vmax[w];
           i = imax[w];
         }
       p_sh = i;
       piv[j] = i;
-      if (!(b > 0.0)) *singular = 1;
+      if (!(bb > 0.0)) *singular = 1;
     }
     __syncthreads();
     const int p = p_sh;
-    if (p != j)
-      for (int c = k + threadIdx.x; c < k + kb; c += blockDim.x) {
-        const double t = A[(int64_t)j * n + c];
-        A[(int64_t)j * n + c] = A[(int64_t)p * n + c];
-        A[(int64_t)p * n + c] = t;
+    if (threadIdx.x < kb) {
+      const int c = k + threadIdx.x;
+      const double tj = A[(int64_t)j * n + c], tp = A[(int64_t)p * n + c];
+      if (p != j) {
+        A[(int64_t)j * n + c] = tp;
+        A[(int64_t)p * n + c] = tj;
       }
+      prow[threadIdx.x] = tp;
+    }
     __syncthreads();
-    const double d = A[(int64_t)j * n + j];
+    const double d = prow[jj];
     if (d != 0.0) {
       for (int r = j + 1 + threadIdx.x; r < n; r += blockDim.x) {
-        double* row = A + (int64_t)r * n;
-        const double l = row[j] / d;
-        row[j] = l;
-        for (int c = j + 1; c < k + kb; ++c) row[c] -= l * A[(int64_t)j * n + c];
+        double* row = A + (int64_t)r * n + k;
+        double v[LU_NB];
+#pragma unroll
+        for (int c = 0; c < LU_NB; ++c) v[c] = (c >= jj && c < kb) ? row[c] : 0.0;
+        double vj = 0.0;  // v[jj] by selection, so that v stays in registers
+#pragma unroll
+        for (int c = 0; c < LU_NB; ++c) vj = c == jj ? v[c] : vj;
+        const double l = vj / d;
+#pragma unroll
+        for (int c = 0; c < LU_NB; ++c)
+          if (c > jj && c < kb) row[c] = v[c] - l * prow[c];
+        row[jj] = l;
       }
     }
     __syncthreads();
@@ -867,9 +884,12 @@ __global__ void k_lu_trsm(double* A, int n, int k, int kb) {
     }
 }
 
-// Swaps on b, then L y = b (unit diagonal) and U x = y, one CTA.
+// Swaps on b, then L y = b (unit diagonal) and U x = y, one CTA, by blocks
+// of 32 rows: the block's right-hand side first takes the product with the
+// solved part (all warps, one row each), then one warp solves the 32 x 32
+// triangle with shuffles.
 __global__ void __launch_bounds__(512) k_lu_subst(const double* A, int n, const int* piv, double* b) {
-  __shared__ double red[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if (threadIdx.x == 0)
     for (int j = 0; j < n; ++j) {
       const int p = piv[j];
@@ -880,18 +900,48 @@ __global__ void __launch_bounds__(512) k_lu_subst(const double* A, int n, const 
       }
     }
   __syncthreads();
-  for (int r = 1; r < n; ++r) {
-    double part = 0.0;
-    for (int t = threadIdx.x; t < r; t += blockDim.x) part += A[(int64_t)r * n + t] * b[t];
-    const double s = block_sum<double>(part, red);
-    if (threadIdx.x == 0) b[r] -= s;
+  // forward: rows r0..r0+31 after rows < r0 are final
+  for (int r0 = 0; r0 < n; r0 += 32) {
+    const int rb = min(32, n - r0);
+    for (int i = warp; i < rb; i += nw) {
+      const double* Ar = A + (int64_t)(r0 + i) * n;
+      double part = 0.0;
+      for (int t = lane; t < r0; t += 32) part += Ar[t] * b[t];
+      for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      if (lane == 0) b[r0 + i] -= part;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      double y = lane < rb ? b[r0 + lane] : 0.0;
+      for (int i = 0; i < rb; ++i) {
+        const double yi = __shfl_sync(0xffffffffu, y, i);
+        if (lane > i && lane < rb) y -= A[(int64_t)(r0 + lane) * n + r0 + i] * yi;
+      }
+      if (lane < rb) b[r0 + lane] = y;
+    }
     __syncthreads();
   }
-  for (int r = n - 1; r >= 0; --r) {
-    double part = 0.0;
-    for (int t = r + 1 + threadIdx.x; t < n; t += blockDim.x) part += A[(int64_t)r * n + t] * b[t];
-    const double s = block_sum<double>(part, red);
-    if (threadIdx.x == 0) b[r] = (b[r] - s) / A[(int64_t)r * n + r];
+  // backward: rows r0..r0+rb-1 (from the bottom) after rows >= r0 + rb are final
+  for (int r1 = n; r1 > 0; r1 -= 32) {
+    const int r0 = max(0, r1 - 32), rb = r1 - r0;
+    for (int i = warp; i < rb; i += nw) {
+      const double* Ar = A + (int64_t)(r0 + i) * n;
+      double part = 0.0;
+      for (int t = r1 + lane; t < n; t += 32) part += Ar[t] * b[t];
+      for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      if (lane == 0) b[r0 + i] -= part;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      double y = lane < rb ? b[r0 + lane] : 0.0;
+      for (int i = rb - 1; i >= 0; --i) {
+        const double di = A[(int64_t)(r0 + i) * n + r0 + i];
+        if (lane == i) y /= di;
+        const double yi = __shfl_sync(0xffffffffu, y, i);
+        if (lane < i) y -= A[(int64_t)(r0 + lane) * n + r0 + i] * yi;
+      }
+      if (lane < rb) b[r0 + lane] = y;
+    }
     __syncthreads();
   }
 }
@@ -903,7 +953,7 @@ bool lu_solve(tnfa_ctx* ctx, double* A, double* b, int n) {
   KernelScope ks(ctx, "lu_f64", 2.0 / 3.0 * (double)n * n * n, 0.0);
   for (int k = 0; k < n; k += LU_NB) {
     const int kb = std::min(LU_NB, n - k);
-    k_lu_panel<<<1, 512, 0, ctx->stream>>>(A, n, k, kb, piv.as<int>(), sing.as<int>());
+    k_lu_panel<<<1, 256, 0, ctx->stream>>>(A, n, k, kb, piv.as<int>(), sing.as<int>());
     k_lu_swap<<<grid_for(n, 256, 1024), 256, 0, ctx->stream>>>(A, n, k, kb, piv.as<int>());
     if (k + kb < n) {
       k_lu_trsm<<<grid_for(n - k - kb, 128, 1024), 128, 0, ctx->stream>>>(A, n, k, kb);

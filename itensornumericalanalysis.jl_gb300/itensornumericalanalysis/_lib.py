@@ -145,6 +145,13 @@ SIGNATURES = {
         C.c_int,
         [_P, _P, _P, _I64, _I32, _PI32, _P, C.c_int, C.c_int],
     ),
+    "tnfa_eval_plan_create": (
+        C.c_int,
+        [_P, _P, _P, _I64, _I32, _PI32, _P, C.c_int, C.c_int, _PP],
+    ),
+    "tnfa_eval_plan_launch": (C.c_int, [_P, _P]),
+    "tnfa_eval_plan_check": (C.c_int, [_P, _P]),
+    "tnfa_eval_plan_destroy": (C.c_int, [_P]),
     "tnfa_integrate": (C.c_int, [_P, _P, C.c_int, _PD]),
     "tnfa_integrate_operator": (C.c_int, [_P, _P, _P, C.c_int, _PD]),
     "tnfa_partial_integrate": (C.c_int, [_P, _P, _I32, _PI32, C.c_int, C.c_int, _PI32, _PP, _PI32]),

@@ -256,6 +256,29 @@ class ITensorNetworkFunction:
             return m, e
         return res
 
+    def evaluation_plan(self, X, out, dims=None, precision: str | None = None,
+                        out_kind: str = "f64") -> "EvaluationPlan":
+        """A captured evaluation (tnfa_eval_plan_create) of this network at the
+        rows of the CUDA tensor X (n_points x len(dims), float64, contiguous)
+        into the CUDA tensor out, replayed by EvaluationPlan.launch() with one
+        graph launch; X's contents may change between launches.  precision
+        defaults to the network's own type ("f64" for FP64 and complex
+        networks, "f32" for FP32 ones)."""
+        dims = self.s.dimensions() if dims is None else ([dims] if isinstance(dims, int) else list(dims))
+        if precision is None:
+            precision = "f32" if self.dtype == _lib.F32 else "f64"
+        kinds = {"f64": _lib.OUT_F64, "f32": _lib.OUT_F32, "f32_scaled": _lib.OUT_F32_SCALED,
+                 "c128": _lib.OUT_C128}
+        kind = _lib.OUT_C128 if self.is_complex else kinds[out_kind]
+        if not (X.is_cuda and out.is_cuda and X.is_contiguous() and out.is_contiguous()):
+            raise ValueError("an evaluation plan needs contiguous CUDA tensors for X and out")
+        P = X.shape[0]
+        h = C.c_void_p()
+        self._ctx.call("tnfa_eval_plan_create", self._h, C.c_void_p(X.data_ptr()), P, len(dims),
+                       _i32(dims), C.c_void_p(out.data_ptr()), kind,
+                       PRECISIONS[precision] if not self.is_complex else _lib.PREC_F64, C.byref(h))
+        return EvaluationPlan(self, h, X, out)
+
     def evaluate(self, xs, dims=None, **kw):
         """evaluate (src/itensornetworkfunction.jl:96-112): f at one point."""
         xs = [xs] if np.isscalar(xs) else list(xs)
@@ -365,3 +388,30 @@ def inner(f: ITensorNetworkFunction, g: ITensorNetworkFunction):
 def calculate_fx(f: ITensorNetworkFunction, X, dims=None, **kw) -> np.ndarray:
     """Batched evaluation (the name the GB300 API uses for evaluate over many points)."""
     return f.evaluate_batch(X, dims, **kw)
+
+
+class EvaluationPlan:
+    """A network's evaluation on fixed CUDA buffers, captured as a CUDA graph
+    (tnfa_eval_plan_*).  Holds the network, X and out alive."""
+
+    def __init__(self, f, handle, X, out):
+        self._f, self._h, self.X, self.out = f, handle, X, out
+
+    def launch(self) -> None:
+        """Enqueue one evaluation of the current X on the context's stream."""
+        self._f.ctx.call("tnfa_eval_plan_launch", self._h)
+
+    def check(self) -> None:
+        """Wait for the stream; raise TnfaError for a bad coordinate."""
+        self._f.ctx.call("tnfa_eval_plan_check", self._h)
+
+    def close(self) -> None:
+        if self._h is not None and self._h.value:
+            _lib.load().tnfa_eval_plan_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
