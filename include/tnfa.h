@@ -120,6 +120,20 @@ const char* tnfa_version(void);
  * in ms (0 when timing was off), flops and bytes.  reset != 0 clears the
  * counters afterwards. */
 int tnfa_ctx_set_timing(tnfa_ctx* ctx, int enable);
+
+/* Autotuning of interchangeable launch variants (the SIMT contraction's tile
+ * shape, the tensor-core evaluation's formulation).  The first call that
+ * meets a shape whose algorithmic work reaches min_work flops times every
+ * variant once on the context's stream and keeps the fastest for that shape;
+ * later calls reuse it.  enable: 1 on, 0 off (rule-based choice), -1 keep
+ * (the default comes from the environment variable TNFA_AUTOTUNE, on unless
+ * it is "0"); min_work < 0 keeps the threshold (default 2e9); forget != 0
+ * drops the kept choices.  No counterpart in the reference (its contractions
+ * are BLAS calls). */
+int tnfa_ctx_set_autotune(tnfa_ctx* ctx, int enable, double min_work, int forget);
+/* The kept choices, one line each: "<shape key> <variant> <ms per variant...>".
+ * Writes at most size bytes (NUL-terminated) and the full size into *needed. */
+int tnfa_ctx_tuning_report(tnfa_ctx* ctx, char* buf, int64_t size, int64_t* needed);
 int tnfa_ctx_kernel_stats(tnfa_ctx* ctx, int32_t max, char* names, int64_t* launches, double* ms,
                           double* flops, double* bytes, int32_t* n_families, int reset);
 

@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstring>
 #include <stdexcept>
+#include <functional>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -147,6 +149,11 @@ struct tnfa_ctx {
   std::string last_error;
   bool timing = false;
   bool capturing = false;  // a stream capture is open: no events, no syncs
+  // autotuning of interchangeable launch variants (tnfa::tune)
+  int autotune = -1;            // -1: from TNFA_AUTOTUNE (default on), 0 off, 1 on
+  double autotune_min_work = 2e9;  // algorithmic flops below which the rule choice stands
+  std::map<std::string, int> tuned;
+  std::map<std::string, std::vector<float>> tuned_ms;
   std::vector<tnfa::KernelFamily> families;
   std::vector<cudaEvent_t> event_pool;
 };
@@ -202,6 +209,20 @@ void require_ctx(const tnfa_ctx* ctx);
 
 // Element-type conversions on the device.
 void convert_f64_to_f32(tnfa_ctx* ctx, const double* src, float* dst, int64_t n);
+
+// Measured choice among ncand interchangeable variants of one launch (tile
+// shapes, formulations) that compute the same result.  The first call for a
+// key whose algorithmic work reaches ctx->autotune_min_work times every
+// variant once on the context's stream (CUDA events), keeps the fastest for
+// the key and leaves its result in place (re-running it when another variant
+// ran last); later calls run the kept variant directly.  Below the work
+// threshold, with autotuning off, or inside a stream capture, variant 0 (the
+// rule-based default) runs and nothing is recorded.  run(i) enqueues variant
+// i.  Returns the variant that produced the result.
+int tune(tnfa_ctx* ctx, const std::string& key, int ncand, double work,
+         const std::function<void(int)>& run);
+// The variant kept for key, or -1.
+int tuned_choice(const tnfa_ctx* ctx, const std::string& key);
 
 // Launch accounting: construct before a launch, destroy after it.  Counts
 // the launch and its algorithmic work; records CUDA events when timing is on.

@@ -175,6 +175,61 @@ FILE* trace_file() {
 
 bool trace_on() { return trace_file() != nullptr; }
 
+static bool autotune_on(tnfa_ctx* ctx) {
+  if (ctx->autotune < 0) {
+    const char* e = getenv("TNFA_AUTOTUNE");
+    ctx->autotune = (e && *e == '0') ? 0 : 1;
+  }
+  return ctx->autotune == 1;
+}
+
+int tuned_choice(const tnfa_ctx* ctx, const std::string& key) {
+  auto it = ctx->tuned.find(key);
+  return it == ctx->tuned.end() ? -1 : it->second;
+}
+
+int tune(tnfa_ctx* ctx, const std::string& key, int ncand, double work,
+         const std::function<void(int)>& run) {
+  if (ncand <= 1) {
+    run(0);
+    return 0;
+  }
+  const int kept = tuned_choice(ctx, key);
+  if (kept >= 0) {
+    run(kept);
+    return kept;
+  }
+  if (ctx->capturing || !autotune_on(ctx) || work < ctx->autotune_min_work) {
+    run(0);
+    return 0;
+  }
+  cudaEvent_t e0 = take_event(ctx), e1 = take_event(ctx);
+  TNFA_CHECK(e0 && e1, TNFA_ERR_CUDA, "autotune: no CUDA events");
+  std::vector<float> ms(ncand, -1.0f);
+  for (int i = 0; i < ncand; ++i) {
+    TNFA_CUDA(cudaEventRecord(e0, ctx->stream));
+    run(i);
+    TNFA_CUDA(cudaEventRecord(e1, ctx->stream));
+    TNFA_CUDA(cudaEventSynchronize(e1));
+    TNFA_CUDA(cudaEventElapsedTime(&ms[i], e0, e1));
+  }
+  ctx->event_pool.push_back(e0);
+  ctx->event_pool.push_back(e1);
+  int best = 0;
+  for (int i = 1; i < ncand; ++i)
+    if (ms[i] < ms[best]) best = i;
+  if (best != ncand - 1) run(best);
+  ctx->tuned[key] = best;
+  ctx->tuned_ms[key] = ms;
+  if (trace_on()) {
+    fprintf(trace_file(), "tnfa-tune %s ->%d", key.c_str(), best);
+    for (float m : ms) fprintf(trace_file(), " %.4f", m);
+    fprintf(trace_file(), "\n");
+    fflush(trace_file());
+  }
+  return best;
+}
+
 KernelScope::KernelScope(tnfa_ctx* c, const char* family, double fl, double bytes)
     : ctx(c), flops(fl) {
   fam = -1;
@@ -272,6 +327,38 @@ int tnfa_ctx_create(int device, void* stream, tnfa_ctx** out) {
 int tnfa_ctx_set_timing(tnfa_ctx* ctx, int enable) {
   if (!ctx) return TNFA_ERR_INVALID_ARGUMENT;
   ctx->timing = enable != 0;
+  return TNFA_OK;
+}
+
+int tnfa_ctx_set_autotune(tnfa_ctx* ctx, int enable, double min_work, int forget) {
+  if (!ctx) return TNFA_ERR_INVALID_ARGUMENT;
+  if (enable >= 0) ctx->autotune = enable != 0 ? 1 : 0;
+  if (min_work >= 0) ctx->autotune_min_work = min_work;
+  if (forget) {
+    ctx->tuned.clear();
+    ctx->tuned_ms.clear();
+  }
+  return TNFA_OK;
+}
+
+int tnfa_ctx_tuning_report(tnfa_ctx* ctx, char* buf, int64_t size, int64_t* needed) {
+  if (!ctx) return TNFA_ERR_INVALID_ARGUMENT;
+  std::string r;
+  for (const auto& kv : ctx->tuned) {
+    r += kv.first + " " + std::to_string(kv.second);
+    for (float m : ctx->tuned_ms[kv.first]) {
+      char b[32];
+      snprintf(b, sizeof b, " %.4f", m);
+      r += b;
+    }
+    r += "\n";
+  }
+  if (needed) *needed = (int64_t)r.size() + 1;
+  if (buf && size > 0) {
+    const size_t n = std::min<size_t>((size_t)size - 1, r.size());
+    memcpy(buf, r.data(), n);
+    buf[n] = 0;
+  }
   return TNFA_OK;
 }
 

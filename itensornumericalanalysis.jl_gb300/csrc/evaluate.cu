@@ -484,13 +484,28 @@ static GemmTile gemm_tile(int chi_a, int sumdim, size_t tsize) {
   return {1024 / ta, ta};
 }
 
+// Tiles worth timing against each other for one shape: the rule's choice
+// first, then a 4 x 4 micro-tile at each other column width that fits.
+static std::vector<GemmTile> gemm_tile_candidates(int chi_a, int sumdim, size_t tsize) {
+  std::vector<GemmTile> c{gemm_tile(chi_a, sumdim, tsize)};
+  const size_t row_bytes = (size_t)sumdim * tsize;
+  for (int ta : {32, 64, 128}) {
+    const int tp = 4096 / ta;
+    if (row_bytes * tp + (size_t)16 * (tp + ta) * tsize > 160 * 1024) continue;
+    if (tp == c[0].tp && ta == c[0].ta) continue;
+    c.push_back({tp, ta});
+  }
+  return c;
+}
+
 template <class T> struct FamilyName;
 template <> struct FamilyName<double> { static constexpr const char* v = "contract_f64"; };
 template <> struct FamilyName<float> { static constexpr const char* v = "contract_f32"; };
 template <> struct FamilyName<cplx> { static constexpr const char* v = "contract_c128"; };
 
 template <class T>
-static void launch_contract(tnfa_ctx* ctx, const VertexJob<T>& j, int Pc) {
+static void launch_contract(tnfa_ctx* ctx, const VertexJob<T>& j, int Pc,
+                            const GemmTile* tile = nullptr) {
   int sumdim = 0;
   for (int c = 0; c < j.nchild; ++c) sumdim += j.ch[c].dim;
   KernelScope ks(ctx, FamilyName<T>::v, 2.0 * Pc * (double)j.K * j.chi_a,
@@ -509,7 +524,7 @@ static void launch_contract(tnfa_ctx* ctx, const VertexJob<T>& j, int Pc) {
     else if (j.chi_a <= 4) k_contract_narrow<T, 4><<<gx, 256, sm, ctx->stream>>>(j);
     else k_contract_narrow<T, 16><<<gx, 256, sm, ctx->stream>>>(j);
   } else {
-    const GemmTile t = gemm_tile(j.chi_a, sumdim, sizeof(T));
+    const GemmTile t = tile ? *tile : gemm_tile(j.chi_a, sumdim, sizeof(T));
     const size_t sm = (size_t)sumdim * sizeof(T) * t.tp + (size_t)16 * (t.tp + t.ta) * sizeof(T) +
                       2 * t.tp * sizeof(int);
     TNFA_CHECK(sm <= 200 * 1024, TNFA_ERR_UNSUPPORTED, "children bonds too large for evaluation");
@@ -627,7 +642,17 @@ static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, 
         j.out_exp = dslote.as<int>() + (size_t)plan.slot[v] * Pcap;
       }
       const bool tc = use_tc && j.site_dim <= 256 && tc_vertex_eligible(j.nchild, cdims, j.chi_a);
-      const int tp = tc ? tc_tile_rows() : contract_tile_rows(j.chi_a, sumdim, sizeof(T));
+      // SIMT shapes: the tile kept by the autotuner for this shape, else the rule's
+      std::vector<GemmTile> cand;
+      std::string key;
+      int tp = tc ? tc_tile_rows() : contract_tile_rows(j.chi_a, sumdim, sizeof(T));
+      if (!tc && j.chi_a > 16) {
+        cand = gemm_tile_candidates(j.chi_a, sumdim, sizeof(T));
+        key = std::string("simt:") + FamilyName<T>::v + ":" + std::to_string(j.chi_a) + ":";
+        for (int i = 0; i < j.nchild; ++i) key += std::to_string(cdims[i]) + (i + 1 < j.nchild ? "x" : "");
+        const int kept = tuned_choice(ctx, key);
+        tp = cand[kept >= 0 ? kept : 0].tp;
+      }
       const int ng = j.site_dim;
       int* meta = dmeta.as<int>();
       j.ngroups = ng;
@@ -657,7 +682,20 @@ static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, 
           continue;
         }
       }
-      launch_contract<T>(ctx, j, Pc);
+      if (cand.empty()) {
+        launch_contract<T>(ctx, j, Pc);
+        continue;
+      }
+      int cur_tp = tp;
+      tune(ctx, key, (int)cand.size(), 2.0 * Pc * (double)j.K * j.chi_a, [&](int i) {
+        if (cand[i].tp != cur_tp) {  // tile table for this candidate's rows per tile
+          if (ng == 1) k_group_identity<<<1, 1, 0, ctx->stream>>>(meta, Pc, cand[i].tp);
+          else k_group_scan<<<1, 1, 0, ctx->stream>>>(meta, ng, cand[i].tp);
+          TNFA_LAUNCH_CHECK();
+          cur_tp = cand[i].tp;
+        }
+        launch_contract<T>(ctx, j, Pc, &cand[i]);
+      });
     }
     void* o = out_mem == TNFA_MEM_HOST ? dout.p : out;
     int64_t Pout = out_mem == TNFA_MEM_HOST ? Pc : P;

@@ -826,24 +826,34 @@ void tc_contract_vertex(tnfa_ctx* ctx, const tnfa_net* net, int v, const VertexJ
   KernelScope ks(ctx, "contract_tc", 2.0 * j.Pc * (double)j.K * j.chi_a,
                  4.0 * ((double)j.Pc * (p.chi1 + p.chi2 + j.chi_a)) +
                      4.0 * j.site_dim * (double)j.chi_a * j.K);
-  // two children: contract the second child first (k_contract_tc2) unless
-  // TNFA_TC_KRON selects the Kronecker formulation
-  static const bool kron = getenv("TNFA_TC_KRON") && *getenv("TNFA_TC_KRON") == '1';
-  if (!bilin && !kron && j.nchild == 2 && p.chi1 % (T2_N / N) == 0) {
-    const int nbt = T2_N / N;
-    CUtensorMap h3 = make_map3(hi, p.chi2, p.chi1, (int64_t)j.site_dim * N, nbt, N);
-    CUtensorMap l3 = make_map3(lo, p.chi2, p.chi1, (int64_t)j.site_dim * N, nbt, N);
-    if (N == 128 && p.chi2 == 128) return launch_tc2<128, 128>(ctx, h3, l3, p, grid);
-    if (N == 128 && p.chi2 == 64) return launch_tc2<128, 64>(ctx, h3, l3, p, grid);
-    if (N == 64 && p.chi2 == 128) return launch_tc2<64, 128>(ctx, h3, l3, p, grid);
-    if (N == 64 && p.chi2 == 64) return launch_tc2<64, 64>(ctx, h3, l3, p, grid);
-  }
-  if (!bilin) {
+  // Two children: the second child first (k_contract_tc2) or the Kronecker
+  // formulation (k_contract_tc); the autotuner times both per shape, the
+  // default is tc2, and TNFA_TC_KRON=1 forces the Kronecker form.
+  static const bool kron_only = getenv("TNFA_TC_KRON") && *getenv("TNFA_TC_KRON") == '1';
+  auto kron = [&]() {
     if (N == 128 && p.chi2 == 128) launch_tc<128, 128, 3, false>(ctx, mh, ml, p, grid);
     else if (N == 128 && p.chi2 == 64) launch_tc<128, 64, 3, false>(ctx, mh, ml, p, grid);
     else if (N == 64 && p.chi2 == 128) launch_tc<64, 128, 4, false>(ctx, mh, ml, p, grid);
     else if (N == 64 && p.chi2 == 64) launch_tc<64, 64, 4, false>(ctx, mh, ml, p, grid);
     else fail(TNFA_ERR_UNSUPPORTED, "tensor-core shape");
+  };
+  if (!bilin && !kron_only && j.nchild == 2 && p.chi1 % (T2_N / N) == 0) {
+    const int nbt = T2_N / N;
+    CUtensorMap h3 = make_map3(hi, p.chi2, p.chi1, (int64_t)j.site_dim * N, nbt, N);
+    CUtensorMap l3 = make_map3(lo, p.chi2, p.chi1, (int64_t)j.site_dim * N, nbt, N);
+    auto tc2 = [&]() {
+      if (N == 128 && p.chi2 == 128) launch_tc2<128, 128>(ctx, h3, l3, p, grid);
+      else if (N == 128 && p.chi2 == 64) launch_tc2<128, 64>(ctx, h3, l3, p, grid);
+      else if (N == 64 && p.chi2 == 128) launch_tc2<64, 128>(ctx, h3, l3, p, grid);
+      else launch_tc2<64, 64>(ctx, h3, l3, p, grid);
+    };
+    const std::string key = "tc:" + std::to_string(N) + ":" + std::to_string(p.chi1) + "x" +
+                            std::to_string(p.chi2);
+    tune(ctx, key, 2, 2.0 * j.Pc * (double)j.K * j.chi_a, [&](int i) { i == 0 ? tc2() : kron(); });
+    return;
+  }
+  if (!bilin) {
+    kron();
   } else {
     if (N == 128 && p.chi2 == 128) launch_tc<128, 128, 3, true>(ctx, mh, ml, p, grid);
     else if (N == 128 && p.chi2 == 64) launch_tc<128, 64, 3, true>(ctx, mh, ml, p, grid);

@@ -120,6 +120,8 @@ SIGNATURES = {
     "tnfa_ctx_synchronize": (C.c_int, [_P]),
     "tnfa_last_error_string": (C.c_char_p, [_P]),
     "tnfa_ctx_set_timing": (C.c_int, [_P, C.c_int]),
+    "tnfa_ctx_set_autotune": (C.c_int, [_P, C.c_int, C.c_double, C.c_int]),
+    "tnfa_ctx_tuning_report": (C.c_int, [_P, C.c_char_p, _I64, C.POINTER(_I64)]),
     "tnfa_ctx_kernel_stats": (
         C.c_int,
         [_P, _I32, C.c_char_p, C.POINTER(_I64), _PD, _PD, _PD, _PI32, C.c_int],
@@ -217,6 +219,25 @@ class Context:
 
     def set_timing(self, enable: bool) -> None:
         self.check(self.lib.tnfa_ctx_set_timing(self.handle, int(enable)))
+
+    def set_autotune(self, enable: bool | None = None, min_work: float | None = None,
+                     forget: bool = False) -> None:
+        """Autotuning of launch variants (tnfa_ctx_set_autotune); None keeps a setting."""
+        self.check(self.lib.tnfa_ctx_set_autotune(
+            self.handle, -1 if enable is None else int(enable),
+            -1.0 if min_work is None else float(min_work), int(forget)))
+
+    def tuning_report(self) -> dict:
+        """shape key -> (kept variant, [ms of each variant when timed])."""
+        need = _I64()
+        self.check(self.lib.tnfa_ctx_tuning_report(self.handle, None, 0, C.byref(need)))
+        buf = C.create_string_buffer(int(need.value))
+        self.check(self.lib.tnfa_ctx_tuning_report(self.handle, buf, need.value, C.byref(need)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            parts = line.split()
+            out[parts[0]] = (int(parts[1]), [float(x) for x in parts[2:]])
+        return out
 
     def kernel_stats(self, reset: bool = False) -> dict:
         """family -> {launches, ms, flops, bytes} since the last reset."""
