@@ -859,6 +859,208 @@ __global__ void __launch_bounds__(256) k_lu_panel(double* A, int n, int k, int k
   }
 }
 
+// The same panel factorisation with the panel (rows k..n-1, kb columns) held
+// in shared memory, row stride kb + 1 doubles: one read and one write-back of
+// the panel, every column step in shared memory.  1024 threads.
+__global__ void __launch_bounds__(1024) k_lu_panel_smem(double* A, int n, int k, int kb, int* piv,
+                                                        int* singular) {
+  extern __shared__ __align__(16) double P[];
+  __shared__ double vmax[32];
+  __shared__ int imax[32];
+  __shared__ int p_sh;
+  const int rows = n - k, ld = kb + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = threadIdx.x; i < rows * kb; i += blockDim.x) {
+    const int r = i / kb, c = i - r * kb;
+    P[r * ld + c] = A[(int64_t)(k + r) * n + k + c];
+  }
+  __syncthreads();
+  for (int jj = 0; jj < kb; ++jj) {
+    double best = -1.0;
+    int bi = jj;
+    for (int r = jj + threadIdx.x; r < rows; r += blockDim.x) {
+      const double a = fabs(P[r * ld + jj]);
+      if (a > best) {
+        best = a;
+        bi = r;
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      vmax[warp] = best;
+      imax[warp] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double bb = -1.0;
+      int i = jj;
+      for (int w = 0; w < nw; ++w)
+        if (vmax[w] > bb || (vmax[w] == bb && imax[w] < i)) {
+          bb = vmax[w];
+          i = imax[w];
+        }
+      p_sh = i;
+      piv[k + jj] = k + i;
+      if (!(bb > 0.0)) *singular = 1;
+    }
+    __syncthreads();
+    const int pr = p_sh;
+    if (pr != jj && threadIdx.x < kb) {
+      const double t = P[jj * ld + threadIdx.x];
+      P[jj * ld + threadIdx.x] = P[pr * ld + threadIdx.x];
+      P[pr * ld + threadIdx.x] = t;
+    }
+    __syncthreads();
+    const double d = P[jj * ld + jj];
+    if (d != 0.0)
+      for (int r = jj + 1 + threadIdx.x; r < rows; r += blockDim.x) {
+        double* row = P + r * ld;
+        const double l = row[jj] / d;
+        row[jj] = l;
+        for (int c = jj + 1; c < kb; ++c) row[c] -= l * P[jj * ld + c];
+      }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < rows * kb; i += blockDim.x) {
+    const int r = i / kb, c = i - r * kb;
+    A[(int64_t)(k + r) * n + k + c] = P[r * ld + c];
+  }
+}
+
+// Register-resident panel for at most 2 x 512 rows and LU_RB = 16 columns:
+// thread t owns rows t and t + 512 of the panel, their 16 entries in
+// registers for the whole factorisation.  A column step is a register pivot
+// search, an exchange of the two swapped rows through shared memory, and a
+// register update against the pivot row broadcast from shared memory.
+constexpr int LU_RB = 16;
+__global__ void __launch_bounds__(512) k_lu_panel_reg(double* A, int n, int k, int kb, int* piv,
+                                                      int* singular) {
+  __shared__ double prow[LU_RB], jrow[LU_RB];
+  __shared__ double vmax[16];
+  __shared__ int imax[16];
+  __shared__ int p_sh;
+  const int rows = n - k;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double v[2][LU_RB];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int r = threadIdx.x + h * 512;
+#pragma unroll
+    for (int c = 0; c < LU_RB; ++c)
+      v[h][c] = (r < rows && c < kb) ? A[(int64_t)(k + r) * n + k + c] : 0.0;
+  }
+  for (int jj = 0; jj < kb; ++jj) {
+    // pivot: the largest |entry| of column jj among rows >= jj
+    double best = -1.0;
+    int bi = jj;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int r = threadIdx.x + h * 512;
+      double a = 0.0;
+#pragma unroll
+      for (int c = 0; c < LU_RB; ++c) a = c == jj ? v[h][c] : a;
+      a = fabs(a);
+      if (r >= jj && r < rows && a > best) {
+        best = a;
+        bi = r;
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      vmax[warp] = best;
+      imax[warp] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double bb = -1.0;
+      int i = jj;
+      for (int w = 0; w < nw; ++w)
+        if (vmax[w] > bb || (vmax[w] == bb && imax[w] < i)) {
+          bb = vmax[w];
+          i = imax[w];
+        }
+      p_sh = i;
+      piv[k + jj] = k + i;
+      if (!(bb > 0.0)) *singular = 1;
+    }
+    __syncthreads();
+    const int pr = p_sh;
+    // rows jj and pr trade places: their owners publish them in shared
+    // memory (prow = the new row jj), then each takes the other's values
+    const int hp = pr >> 9, tp = pr & 511;
+    const int hj = jj >> 9, tj = jj & 511;
+    if (threadIdx.x == tp) {
+#pragma unroll
+      for (int c = 0; c < LU_RB; ++c) prow[c] = hp ? v[1][c] : v[0][c];
+    }
+    if (pr != jj && threadIdx.x == tj) {
+#pragma unroll
+      for (int c = 0; c < LU_RB; ++c) jrow[c] = hj ? v[1][c] : v[0][c];
+    }
+    __syncthreads();
+    if (pr != jj) {
+      if (threadIdx.x == tj) {
+#pragma unroll
+        for (int c = 0; c < LU_RB; ++c) {
+          if (hj) v[1][c] = prow[c];
+          else v[0][c] = prow[c];
+        }
+      }
+      if (threadIdx.x == tp) {
+#pragma unroll
+        for (int c = 0; c < LU_RB; ++c) {
+          if (hp) v[1][c] = jrow[c];
+          else v[0][c] = jrow[c];
+        }
+      }
+    }
+    const double d = prow[jj];
+    if (d != 0.0) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = threadIdx.x + h * 512;
+        if (r > jj && r < rows) {
+          double a = 0.0;
+#pragma unroll
+          for (int c = 0; c < LU_RB; ++c) a = c == jj ? v[h][c] : a;
+          const double l = a / d;
+#pragma unroll
+          for (int c = 0; c < LU_RB; ++c) {
+            if (c > jj) v[h][c] -= l * prow[c];
+            if (c == jj) v[h][c] = l;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int r = threadIdx.x + h * 512;
+    if (r < rows)
+#pragma unroll
+      for (int c = 0; c < LU_RB; ++c)
+        if (c < kb) A[(int64_t)(k + r) * n + k + c] = v[h][c];
+  }
+}
+
+// Shared-memory panel: rows x (kb + 1) doubles within this budget.
+constexpr size_t LU_SMEM_PANEL = 220 * 1024;
+
 // Apply the panel's row swaps to the columns outside it.
 __global__ void k_lu_swap(double* A, int n, int k, int kb, const int* piv) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
@@ -874,14 +1076,28 @@ __global__ void k_lu_swap(double* A, int n, int k, int kb, const int* piv) {
   }
 }
 
-// U12 = L11^{-1} A12 (unit lower triangular L11), one column per thread.
-__global__ void k_lu_trsm(double* A, int n, int k, int kb) {
-  for (int c = k + kb + blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
-    for (int r = k + 1; r < k + kb; ++r) {
-      double acc = A[(int64_t)r * n + c];
-      for (int t = k; t < r; ++t) acc -= A[(int64_t)r * n + t] * A[(int64_t)t * n + c];
-      A[(int64_t)r * n + c] = acc;
-    }
+// U12 = L11^{-1} A12 with L11 (unit lower, kb <= KB) in shared memory and each
+// thread's column of A12 in registers.
+template <int KB>
+__global__ void __launch_bounds__(128) k_lu_trsm_reg(double* A, int n, int k, int kb) {
+  __shared__ double Ls[KB][KB];
+  for (int i = threadIdx.x; i < KB * KB; i += blockDim.x) {
+    const int r = i / KB, t = i - r * KB;
+    Ls[r][t] = (r < kb && t < kb) ? A[(int64_t)(k + r) * n + k + t] : 0.0;
+  }
+  __syncthreads();
+  for (int c = k + kb + blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    double v[KB];
+#pragma unroll
+    for (int r = 0; r < KB; ++r) v[r] = r < kb ? A[(int64_t)(k + r) * n + c] : 0.0;
+#pragma unroll
+    for (int r = 1; r < KB; ++r)
+#pragma unroll
+      for (int t = 0; t < r; ++t) v[r] -= Ls[r][t] * v[t];
+#pragma unroll
+    for (int r = 0; r < KB; ++r)
+      if (r < kb) A[(int64_t)(k + r) * n + c] = v[r];
+  }
 }
 
 // Swaps on b, then L y = b (unit diagonal) and U x = y, one CTA, by blocks
@@ -951,18 +1167,39 @@ bool lu_solve(tnfa_ctx* ctx, double* A, double* b, int n) {
   DBuf piv(ctx, (size_t)n * sizeof(int)), sing(ctx, sizeof(int));
   TNFA_CUDA(cudaMemsetAsync(sing.p, 0, sizeof(int), ctx->stream));
   KernelScope ks(ctx, "lu_f64", 2.0 / 3.0 * (double)n * n * n, 0.0);
-  for (int k = 0; k < n; k += LU_NB) {
-    const int kb = std::min(LU_NB, n - k);
-    k_lu_panel<<<1, 256, 0, ctx->stream>>>(A, n, k, kb, piv.as<int>(), sing.as<int>());
+  TNFA_CUDA(cudaFuncSetAttribute(k_lu_panel_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)LU_SMEM_PANEL));
+  for (int k = 0; k < n;) {
+    // panel width: 32 columns, or 16 when only that lets the panel sit in
+    // shared memory; the global-memory panel beyond that
+    // the panel in registers (at most 1024 rows left, 16 columns), in shared
+    // memory (at most 1600 rows, 16 columns), else in global memory (32)
+    const int rows = n - k;
+    int kb;
+    if (rows <= 1024) {
+      kb = std::min(LU_RB, rows);
+      k_lu_panel_reg<<<1, 512, 0, ctx->stream>>>(A, n, k, kb, piv.as<int>(), sing.as<int>());
+    } else if ((size_t)rows * 17 * 8 <= LU_SMEM_PANEL) {
+      kb = 16;
+      k_lu_panel_smem<<<1, 1024, (size_t)rows * (kb + 1) * 8, ctx->stream>>>(A, n, k, kb, piv.as<int>(),
+                                                                           sing.as<int>());
+    } else {
+      kb = LU_NB;
+      k_lu_panel<<<1, 256, 0, ctx->stream>>>(A, n, k, kb, piv.as<int>(), sing.as<int>());
+    }
     k_lu_swap<<<grid_for(n, 256, 1024), 256, 0, ctx->stream>>>(A, n, k, kb, piv.as<int>());
     if (k + kb < n) {
-      k_lu_trsm<<<grid_for(n - k - kb, 128, 1024), 128, 0, ctx->stream>>>(A, n, k, kb);
+      if (kb <= 16)
+        k_lu_trsm_reg<16><<<grid_for(n - k - kb, 128, 1024), 128, 0, ctx->stream>>>(A, n, k, kb);
+      else
+        k_lu_trsm_reg<32><<<grid_for(n - k - kb, 128, 1024), 128, 0, ctx->stream>>>(A, n, k, kb);
       const int m2 = n - k - kb;
       GemmJob g{A + (int64_t)(k + kb) * n + k, A + (int64_t)k * n + k + kb,
                 A + (int64_t)(k + kb) * n + k + kb, m2, m2, kb, n, n, n, 0, 0, -1.0, 1.0};
       gemm<double>(ctx, {g});
     }
     TNFA_LAUNCH_CHECK();
+    k += kb;
   }
   k_lu_subst<<<1, 512, 0, ctx->stream>>>(A, n, piv.as<int>(), b);
   TNFA_LAUNCH_CHECK();

@@ -52,6 +52,26 @@ def test_second_derivative_path(ina):
     assert abs(x.rel_residual - res) < 1e-11 + 1e-3 * res
 
 
+def test_large_local_systems(ina):
+    """A 12-bit path with a random right-hand side of full rank: the middle
+    two-site systems reach 32 x 2 x 2 x 32 = 4096 unknowns, so the dense LU
+    runs its global-memory panels (more than 1600 rows left), its 16-column
+    shared-memory panels (801-1600) and its 32-column ones (800 or fewer)."""
+    L = 12
+    s = ina.continuous_siteinds(ina.named_path_graph(L))
+    b = ina.truncate(ina.rand_itn(s, link_space=64, rng=78), cutoff=0.0)  # bonds at full rank
+    A = ina.second_derivative_operator(s)
+    a0, a1 = 1.0, -1e-6  # (1 - 1e-6 d2/dx2): condition number ~ 70
+    x = ina.linsolve(A, b, b, a0=a0, a1=a1, nsweeps=2, maxdim=64, cutoff=0.0, tol=0.0)
+    assert x.maxlinkdim() == 64
+    M = _dense_operator(O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2), L,
+                        {(1, k): k - 1 for k in range(1, L + 1)})
+    xs = _grid_1d(L)
+    err, res = _check(M, a0, a1, b.evaluate_batch(xs), x.evaluate_batch(xs), x.rel_residual)
+    assert res < 1e-11, res
+    assert err < 1e-10, err
+
+
 @pytest.mark.parametrize("a0,a1", [(0.0, 1.0), (1.0, -1e-3), (2.0, 0.5)])
 def test_laplacian_comb(ina, a0, a1):
     """(a0 + a1 Laplacian) u = b on a 2 x 5 comb (a 10-site path whose layout
