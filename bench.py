@@ -252,129 +252,138 @@ def secondary_measurements(ctx, ws, rank, args) -> dict:
     import itensornumericalanalysis as ina
     from itensornumericalanalysis.workloads import uneven_mps_batch, upload_batch
 
+    only = set(args.only.split(",")) if args.only else None
+
+    def want(name):
+        return only is None or name in only
+
     out = {}
-    # --- config 5: MPO apply + truncate of an uneven batch -------------------
-    batch = uneven_mps_batch(n=args.mps, seed=3)
-    fs = upload_batch(batch, ctx=ctx)
-    ops = {}
-    for s, _ in batch:
-        if s.nv() not in ops:
-            ops[s.nv()] = ina.first_derivative_operator(s)
-    oplist = [ops[s.nv()] for s, _ in batch]
-    Xc5 = np.random.default_rng(0).random(256)
-    c5 = {}
-    for prec in ("f64", "mixed"):
-        ina.operate_batched(oplist[:8], fs[:8], cutoff=1e-10, precision=prec)  # warm-up
-        ctx.kernel_stats(reset=True)
-        ctx.set_timing(True)
-        t, res = _timed(lambda: ina.operate_batched(oplist, fs, cutoff=1e-10, precision=prec))
-        ctx.set_timing(False)
-        st = ctx.kernel_stats(reset=True)
-        t = max_over_ranks(t, ws)
-        c5[prec] = {
-            "value": ws * len(fs) / t, "unit": "MPS/s", "s_per_batch": t,
-            "max_bond_after": max(r.maxlinkdim() for r in res),
-            "kernel_ms": {k: round(v["ms"], 2) for k, v in sorted(st.items(), key=lambda kv: -kv[1]["ms"])[:6]},
-            "vals": [r.evaluate_batch(Xc5) for r in res[:64]],
+    if want("apply_truncate"):
+        # --- config 5: MPO apply + truncate of an uneven batch -------------------
+        batch = uneven_mps_batch(n=args.mps, seed=3)
+        fs = upload_batch(batch, ctx=ctx)
+        ops = {}
+        for s, _ in batch:
+            if s.nv() not in ops:
+                ops[s.nv()] = ina.first_derivative_operator(s)
+        oplist = [ops[s.nv()] for s, _ in batch]
+        Xc5 = np.random.default_rng(0).random(256)
+        c5 = {}
+        for prec in ("f64", "mixed"):
+            ina.operate_batched(oplist[:8], fs[:8], cutoff=1e-10, precision=prec)  # warm-up
+            ctx.kernel_stats(reset=True)
+            ctx.set_timing(True)
+            t, res = _timed(lambda: ina.operate_batched(oplist, fs, cutoff=1e-10, precision=prec))
+            ctx.set_timing(False)
+            st = ctx.kernel_stats(reset=True)
+            t = max_over_ranks(t, ws)
+            c5[prec] = {
+                "value": ws * len(fs) / t, "unit": "MPS/s", "s_per_batch": t,
+                "max_bond_after": max(r.maxlinkdim() for r in res),
+                "kernel_ms": {k: round(v["ms"], 2) for k, v in sorted(st.items(), key=lambda kv: -kv[1]["ms"])[:6]},
+                "vals": [r.evaluate_batch(Xc5) for r in res[:64]],
+            }
+            del res
+        va, vb = c5["f64"].pop("vals"), c5["mixed"].pop("vals")
+        err = max(float(np.max(np.abs(a - b)) / max(np.max(np.abs(a)), 1e-300)) for a, b in zip(va, vb))
+        out["mpo_apply_truncate"] = {
+            "value": c5["mixed"]["value"], "unit": "MPS/s", "batch": len(fs),
+            "precision": "mixed (FP32-preconditioned Jacobi, FP64 polish and QR)",
+            "mixed": c5["mixed"], "fp64_plain": c5["f64"],
+            "mixed_over_fp64": c5["mixed"]["value"] / c5["f64"]["value"],
+            "rel_err_mixed_vs_fp64": err,
+            "rel_err_what": "max over 64 MPS of max|g_mixed - g_f64| / max|g_f64| at 256 points",
         }
-        del res
-    va, vb = c5["f64"].pop("vals"), c5["mixed"].pop("vals")
-    err = max(float(np.max(np.abs(a - b)) / max(np.max(np.abs(a)), 1e-300)) for a, b in zip(va, vb))
-    out["mpo_apply_truncate"] = {
-        "value": c5["mixed"]["value"], "unit": "MPS/s", "batch": len(fs),
-        "precision": "mixed (FP32-preconditioned Jacobi, FP64 polish and QR)",
-        "mixed": c5["mixed"], "fp64_plain": c5["f64"],
-        "mixed_over_fp64": c5["mixed"]["value"] / c5["f64"]["value"],
-        "rel_err_mixed_vs_fp64": err,
-        "rel_err_what": "max over 64 MPS of max|g_mixed - g_f64| / max|g_f64| at 256 points",
-    }
-    del fs
-    # --- config 2: 2-D Laplace solve on a comb, 2 x 16 bits ---------------------
-    L2 = 16
-    s2 = ina.continuous_siteinds(ina.named_comb_tree((2, L2)),
-                                 [[(1, j) for j in range(L2, 0, -1)], [(2, j) for j in range(1, L2 + 1)]])
-    b2 = ina.sin_itn(s2, k=np.pi, dim=1) * ina.sin_itn(s2, k=np.pi, dim=2)
-    A2 = ina.laplacian_operator(s2)
+        del fs
+    if want("laplace"):
+        # --- config 2: 2-D Laplace solve on a comb, 2 x 16 bits ---------------------
+        L2 = 16
+        s2 = ina.continuous_siteinds(ina.named_comb_tree((2, L2)),
+                                     [[(1, j) for j in range(L2, 0, -1)], [(2, j) for j in range(1, L2 + 1)]])
+        b2 = ina.sin_itn(s2, k=np.pi, dim=1) * ina.sin_itn(s2, k=np.pi, dim=2)
+        A2 = ina.laplacian_operator(s2)
 
-    def solve2():
-        return ina.linsolve(A2, b2, nsweeps=2, maxdim=40, cutoff=1e-20, tol=1e-8, refinements=2)
+        def solve2():
+            return ina.linsolve(A2, b2, nsweeps=2, maxdim=40, cutoff=1e-20, tol=1e-8, refinements=2)
 
-    solve2()
-    t2, x2 = _timed(solve2)
-    X2 = np.random.default_rng(2).random((4096, 2))
-    exact2 = -np.sin(np.pi * X2[:, 0]) * np.sin(np.pi * X2[:, 1]) / (2 * np.pi**2)
-    got2 = x2.evaluate_batch(X2, [1, 2])
-    out["laplace_linsolve"] = {
-        "value": t2, "unit": "s", "what": "linsolve(laplacian, sin(pi x) sin(pi y)), 2 sweeps, maxdim 40, cutoff 1e-20, 2 refinement steps",
-        "rel_residual": x2.rel_residual, "maxlinkdim": x2.maxlinkdim(),
-        "max_err_vs_continuum": float(np.max(np.abs(got2 - exact2)) / np.max(np.abs(exact2))),
-    }
-    # --- config 1: the reference's CPU case on the GPU ---------------------------
-    L = 20
-    s = ina.continuous_siteinds(ina.named_grid((L, 1)))
-    X = np.random.default_rng(0).random((4096, 1))
+        solve2()
+        t2, x2 = _timed(solve2)
+        X2 = np.random.default_rng(2).random((4096, 2))
+        exact2 = -np.sin(np.pi * X2[:, 0]) * np.sin(np.pi * X2[:, 1]) / (2 * np.pi**2)
+        got2 = x2.evaluate_batch(X2, [1, 2])
+        out["laplace_linsolve"] = {
+            "value": t2, "unit": "s", "what": "linsolve(laplacian, sin(pi x) sin(pi y)), 2 sweeps, maxdim 40, cutoff 1e-20, 2 refinement steps",
+            "rel_residual": x2.rel_residual, "maxlinkdim": x2.maxlinkdim(),
+            "max_err_vs_continuum": float(np.max(np.abs(got2 - exact2)) / np.max(np.abs(exact2))),
+        }
+    if want("config1"):
+        # --- config 1: the reference's CPU case on the GPU ---------------------------
+        L = 20
+        s = ina.continuous_siteinds(ina.named_grid((L, 1)))
+        X = np.random.default_rng(0).random((4096, 1))
 
-    def cfg1():
-        f = ina.exp_itn(s, k=-1.0) + ina.sin_itn(s, k=2 * np.pi)
-        g = ina.operate(ina.second_derivative_operator(s), f, cutoff=1e-12, maxdim=32)
-        return g.evaluate_batch(X), g.integrate()
+        def cfg1():
+            f = ina.exp_itn(s, k=-1.0) + ina.sin_itn(s, k=2 * np.pi)
+            g = ina.operate(ina.second_derivative_operator(s), f, cutoff=1e-12, maxdim=32)
+            return g.evaluate_batch(X), g.integrate()
 
-    cfg1()
-    t1, _ = _timed(cfg1)
-    out["config1_latency"] = {"value": t1, "unit": "s",
-                              "what": "build f, build d2/dx2, apply+truncate (1e-12, 32), 4096 evals, integrate"}
-    # small-batch evaluation latency: eager calls vs the captured plan (CUDA graph)
-    import ctypes
-    import torch
+        cfg1()
+        t1, _ = _timed(cfg1)
+        out["config1_latency"] = {"value": t1, "unit": "s",
+                                  "what": "build f, build d2/dx2, apply+truncate (1e-12, 32), 4096 evals, integrate"}
+        # small-batch evaluation latency: eager calls vs the captured plan (CUDA graph)
+        import ctypes
+        import torch
 
-    g1 = ina.operate(ina.second_derivative_operator(s), ina.exp_itn(s, k=-1.0) + ina.sin_itn(s, k=2 * np.pi),
-                     cutoff=1e-12, maxdim=32)
-    Xd1 = torch.tensor(X, dtype=torch.float64, device="cuda")
-    o1 = torch.empty(len(X), dtype=torch.complex128, device="cuda")
-    d1 = (ctypes.c_int32 * 1)(1)
+        g1 = ina.operate(ina.second_derivative_operator(s), ina.exp_itn(s, k=-1.0) + ina.sin_itn(s, k=2 * np.pi),
+                         cutoff=1e-12, maxdim=32)
+        Xd1 = torch.tensor(X, dtype=torch.float64, device="cuda")
+        o1 = torch.empty(len(X), dtype=torch.complex128, device="cuda")
+        d1 = (ctypes.c_int32 * 1)(1)
 
-    def eager():
-        g1.ctx.call("tnfa_evaluate", g1.handle, Xd1.data_ptr(), len(X), 1, d1, ina._lib.MEM_DEVICE,
-                    o1.data_ptr(), ina._lib.OUT_C128, ina._lib.MEM_DEVICE, ina._lib.PREC_F64)
+        def eager():
+            g1.ctx.call("tnfa_evaluate", g1.handle, Xd1.data_ptr(), len(X), 1, d1, ina._lib.MEM_DEVICE,
+                        o1.data_ptr(), ina._lib.OUT_C128, ina._lib.MEM_DEVICE, ina._lib.PREC_F64)
 
-    plan = g1.evaluation_plan(Xd1, o1)
-    eager()
-    te, _ = _timed(eager, 200)
-    plan.launch()
-    tg, _ = _timed(plan.launch, 200)
-    plan.check()
-    plan.close()
-    out["small_batch_eval_latency"] = {
-        "value": tg * 1e6, "unit": "us per call", "eager_us": te * 1e6, "points": len(X),
-        "what": "config-1 network (path 20, complex, bond <= 32) at 4096 device points: "
-                "captured plan replay (one graph launch) vs eager tnfa_evaluate"}
-    # --- config 4: gradient of batched evaluation --------------------------------
-    import torch
+        plan = g1.evaluation_plan(Xd1, o1)
+        eager()
+        te, _ = _timed(eager, 200)
+        plan.launch()
+        tg, _ = _timed(plan.launch, 200)
+        plan.check()
+        plan.close()
+        out["small_batch_eval_latency"] = {
+            "value": tg * 1e6, "unit": "us per call", "eager_us": te * 1e6, "points": len(X),
+            "what": "config-1 network (path 20, complex, bond <= 32) at 4096 device points: "
+                    "captured plan replay (one graph launch) vs eager tnfa_evaluate"}
+    if want("gradient"):
+        # --- config 4: gradient of batched evaluation --------------------------------
+        import torch
 
-    L4 = 12
-    s4 = ina.continuous_siteinds(ina.named_comb_tree((2, L4)),
-                                 [[(1, j) for j in range(1, L4 + 1)], [(2, j) for j in range(1, L4 + 1)]])
-    rng = np.random.default_rng(2)
-    lay = s4.layout
-    ts = {}
-    for i, v in enumerate(lay.order):
-        shape = (2, 32 if lay.parent[i] >= 0 else 1) + (32,) * len(lay.children[i])
-        ts[v] = 0.1 * rng.standard_normal(shape)
-    f4 = ina.ITensorNetworkFunction.from_tensors(s4, ts, ctx=ctx, dtype=ina._lib.F32)
-    P4 = 1 << 20
-    X4 = torch.tensor(rng.random((P4, 2)), device="cuda")
-    dout = torch.tensor(rng.standard_normal(P4), device="cuda")
-    g4 = torch.zeros(f4.info()[2], dtype=torch.float32, device="cuda")
-    dims = (ctypes.c_int32 * 2)(1, 2)
+        L4 = 12
+        s4 = ina.continuous_siteinds(ina.named_comb_tree((2, L4)),
+                                     [[(1, j) for j in range(1, L4 + 1)], [(2, j) for j in range(1, L4 + 1)]])
+        rng = np.random.default_rng(2)
+        lay = s4.layout
+        ts = {}
+        for i, v in enumerate(lay.order):
+            shape = (2, 32 if lay.parent[i] >= 0 else 1) + (32,) * len(lay.children[i])
+            ts[v] = 0.1 * rng.standard_normal(shape)
+        f4 = ina.ITensorNetworkFunction.from_tensors(s4, ts, ctx=ctx, dtype=ina._lib.F32)
+        P4 = 1 << 20
+        X4 = torch.tensor(rng.random((P4, 2)), device="cuda")
+        dout = torch.tensor(rng.standard_normal(P4), device="cuda")
+        g4 = torch.zeros(f4.info()[2], dtype=torch.float32, device="cuda")
+        dims = (ctypes.c_int32 * 2)(1, 2)
 
-    def grad():
-        ctx.call("tnfa_evaluate_vjp", f4.handle, X4.data_ptr(), P4, 2, dims, 1, dout.data_ptr(), 1,
-                 g4.data_ptr(), 1)
+        def grad():
+            ctx.call("tnfa_evaluate_vjp", f4.handle, X4.data_ptr(), P4, 2, dims, 1, dout.data_ptr(), 1,
+                     g4.data_ptr(), 1)
 
-    grad()
-    t4, _ = _timed(grad, 3)
-    out["gradient"] = {"value": P4 / t4, "unit": "points/s", "points": P4,
-                       "what": "tnfa_evaluate_vjp, comb 2x12 chi 32 FP32 (forward + outside messages + accumulation)"}
+        grad()
+        t4, _ = _timed(grad, 3)
+        out["gradient"] = {"value": P4 / t4, "unit": "points/s", "points": P4,
+                           "what": "tnfa_evaluate_vjp, comb 2x12 chi 32 FP32 (forward + outside messages + accumulation)"}
     return out
 
 
@@ -391,6 +400,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--mps", type=int, default=512, help="config-5 batch size")
+    ap.add_argument("--only", default="",
+                    help="run only these secondary measurements (comma list of apply_truncate, "
+                         "laplace, config1, gradient) and print them; no headline step")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_init()
@@ -408,6 +420,11 @@ def main():
     torch.cuda.set_device(local)
     stream = torch.cuda.current_stream()
     ctx = _lib.Context(local, stream.cuda_stream)
+    if args.only:
+        sec = secondary_measurements(ctx, ws, rank, args)
+        if rank == 0:
+            print(json.dumps({"secondary": sec}))
+        return
     ina.set_default_context(ctx)
 
     s, ts = config3_tensors(1)
