@@ -332,18 +332,19 @@ def secondary_measurements(ctx, ws, rank, args) -> dict:
         out["config1_latency"] = {"value": t1, "unit": "s",
                                   "what": "build f, build d2/dx2, apply+truncate (1e-12, 32), 4096 evals, integrate"}
         # small-batch evaluation latency: eager calls vs the captured plan (CUDA graph)
-        import ctypes
         import torch
 
         g1 = ina.operate(ina.second_derivative_operator(s), ina.exp_itn(s, k=-1.0) + ina.sin_itn(s, k=2 * np.pi),
                          cutoff=1e-12, maxdim=32)
         Xd1 = torch.tensor(X, dtype=torch.float64, device="cuda")
-        o1 = torch.empty(len(X), dtype=torch.complex128, device="cuda")
+        cplx1 = g1.is_complex
+        o1 = torch.empty(len(X), dtype=torch.complex128 if cplx1 else torch.float64, device="cuda")
+        kind1 = ina._lib.OUT_C128 if cplx1 else ina._lib.OUT_F64
         d1 = (ctypes.c_int32 * 1)(1)
 
         def eager():
             g1.ctx.call("tnfa_evaluate", g1.handle, Xd1.data_ptr(), len(X), 1, d1, ina._lib.MEM_DEVICE,
-                        o1.data_ptr(), ina._lib.OUT_C128, ina._lib.MEM_DEVICE, ina._lib.PREC_F64)
+                        o1.data_ptr(), kind1, ina._lib.MEM_DEVICE, ina._lib.PREC_F64)
 
         plan = g1.evaluation_plan(Xd1, o1)
         eager()
@@ -354,7 +355,7 @@ def secondary_measurements(ctx, ws, rank, args) -> dict:
         plan.close()
         out["small_batch_eval_latency"] = {
             "value": tg * 1e6, "unit": "us per call", "eager_us": te * 1e6, "points": len(X),
-            "what": "config-1 network (path 20, complex, bond <= 32) at 4096 device points: "
+            "what": "config-1 network (path 20, FP64, bond <= 32) at 4096 device points: "
                     "captured plan replay (one graph launch) vs eager tnfa_evaluate"}
     if want("gradient"):
         # --- config 4: gradient of batched evaluation --------------------------------

@@ -273,3 +273,20 @@ def test_tensor_core_path(ina, graph_name, chi):
     assert np.median(np.abs(got - ref) / np.abs(ref)) < 3e-4
     if graph_name != "path6":
         assert st.get("contract_f32", {}).get("launches", 0) == 0, st
+
+
+@pytest.mark.parametrize("chi", [3, 5, 12])
+def test_batch_composition_invariance(ina, chi):
+    """A point's value must not depend on which other points share its batch
+    (tiles of the narrow and SIMT contractions mix points of one site value):
+    the full 2^12 grid in one call equals the same points in calls of 1, 7 and
+    333 points."""
+    s = ina.continuous_siteinds(ina.named_path_graph(12))
+    f = ina.rand_itn(s, link_space=chi, rng=110 + chi)
+    xs = np.arange(2**12) / 2**12
+    whole = f.evaluate_batch(xs)
+    scale = np.max(np.abs(whole))
+    for step in (1, 7, 333):
+        idx = np.arange(0, len(xs), 97 if step == 1 else 1)
+        parts = np.concatenate([f.evaluate_batch(xs[idx[i:i + step]]) for i in range(0, len(idx), step)])
+        assert np.max(np.abs(parts - whole[idx])) <= 1e-13 * scale, step
