@@ -119,6 +119,172 @@ def tci_path(sample, d: list, tol: float = 1e-10, maxbonddim: int = 64, nsweeps:
                                         "ranks": [len(I[l]) for l in range(1, L)]}
 
 
+# ------------------------------------------------------------------ trees --
+class _TreeCross:
+    """Nested pivot sets of a tree.  Vertices are 0..n-1 with adjacency nbrs;
+    for a directed edge (u, v), side[(u, v)] holds the vertices on u's side and
+    P[(u, v)] the pivots there: rows of digit values over all n vertices, zero
+    off the side, so that pivots of disjoint sides combine by addition."""
+
+    def __init__(self, nbrs, d):
+        self.nbrs, self.d, self.n = nbrs, d, len(d)
+        self.side = {}
+        for u in range(self.n):
+            for v in nbrs[u]:
+                seen, stack = {u}, [u]
+                while stack:
+                    x = stack.pop()
+                    for y in nbrs[x]:
+                        if y not in seen and not (x == u and y == v):
+                            seen.add(y)
+                            stack.append(y)
+                self.side[(u, v)] = np.array(sorted(seen), dtype=np.int64)
+        self.P = {}
+
+    def restrict(self, pts, u, v):
+        out = np.zeros_like(pts)
+        cols = self.side[(u, v)]
+        out[:, cols] = pts[:, cols]
+        return out
+
+    def block(self, u, exclude):
+        """Assignments over side(u, exclude): pivots of u's other neighbours
+        combined, then u's own digit (fastest)."""
+        rows = np.zeros((1, self.n), dtype=np.int64)
+        for w in self.nbrs[u]:
+            if w == exclude:
+                continue
+            A = self.P[(w, u)]
+            rows = (rows[:, None, :] + A[None, :, :]).reshape(-1, self.n)
+        e = np.zeros(self.n, dtype=np.int64)
+        e[u] = 1
+        s = np.arange(self.d[u])
+        return (rows[:, None, :] + s[None, :, None] * e[None, None, :]).reshape(-1, self.n)
+
+    def add_unique(self, key, new_rows, cap):
+        cur = self.P[key]
+        have = {tuple(r) for r in cur}
+        keep = [r for r in new_rows if tuple(r) not in have]
+        if keep:
+            self.P[key] = np.concatenate([cur, np.array(keep[: max(0, cap - len(cur))],
+                                                        dtype=np.int64).reshape(-1, self.n)])
+
+
+def _tree_order(nbrs, root):
+    parent = {root: -1}
+    order = [root]
+    for x in order:
+        for y in nbrs[x]:
+            if y not in parent:
+                parent[y] = x
+                order.append(y)
+    return order, parent
+
+
+def _tree_assemble(sample, tc: _TreeCross, root: int):
+    """Cross form -> one tensor per vertex, axes (digit, neighbours in nbrs
+    order).  The bond of edge (child c, parent p) is indexed by P[(c, p)] on
+    both ends: the parent's tensor is sampled on it directly and the child's
+    absorbs the pivot matrix M[(c, p)]^-1 (least squares)."""
+    order, parent = _tree_order(tc.nbrs, root)
+    cores = {}
+    for v in order:
+        parts = [tc.P[(w, v)] for w in tc.nbrs[v]]
+        idx = np.zeros((1, tc.n), dtype=np.int64)
+        for A in parts:
+            idx = (idx[:, None, :] + A[None, :, :]).reshape(-1, tc.n)
+        e = np.zeros(tc.n, dtype=np.int64)
+        e[v] = 1
+        idx = (idx[:, None, :] + np.arange(tc.d[v])[None, :, None] * e[None, None, :]).reshape(-1, tc.n)
+        T = np.asarray(sample(idx)).reshape([len(A) for A in parts] + [tc.d[v]])
+        T = np.moveaxis(T, -1, 0)  # (digit, neighbours...)
+        p = parent[v]
+        if p >= 0:
+            k = 1 + tc.nbrs[v].index(p)
+            Pc, Pp = tc.P[(v, p)], tc.P[(p, v)]
+            M = np.asarray(sample((Pc[:, None, :] + Pp[None, :, :]).reshape(-1, tc.n))).reshape(len(Pc), len(Pp))
+            Tm = np.moveaxis(T, k, -1)
+            sh = Tm.shape
+            X = np.linalg.lstsq(M.T, Tm.reshape(-1, sh[-1]).T, rcond=None)[0].T
+            T = np.moveaxis(X.reshape(sh[:-1] + (len(Pc),)), -1, k)
+        cores[v] = T
+    return cores
+
+
+def _tree_values(cores, nbrs, root, idx):
+    """Contract the assembled tree at the rows of idx (N, n)."""
+    order, parent = _tree_order(nbrs, root)
+    N = idx.shape[0]
+    msg = {}
+    for v in reversed(order):
+        S = cores[v][idx[:, v]]  # (N, neighbours...)
+        S = S.astype(np.result_type(S, float))
+        # contract the children's messages, last neighbour axis first
+        for k in reversed(range(len(nbrs[v]))):
+            w = nbrs[v][k]
+            if w == parent[v]:
+                continue
+            S = np.moveaxis(S, 1 + k, -1)
+            S = np.einsum("p...k,pk->p...", S, msg[w])
+        msg[v] = S.reshape(N, -1)
+    return msg[root][:, 0]
+
+
+def tci_tree(sample, nbrs, d, tol: float = 1e-10, maxbonddim: int = 64, nsweeps: int = 20,
+             initial_pivot=None, root: int = 0):
+    """Two-site TCI on a tree (the generalisation of tci_path: every edge
+    carries nested pivot sets for its two sides; an update samples the block
+    [u's side x v's side] built from the neighbours' pivots and re-selects both
+    by ACA).  sample(idx) evaluates f at an (N, n) array of digit values,
+    column v = vertex v.  Returns (cores, info) with cores[v] of axes (digit,
+    neighbours in nbrs[v] order), ready for _tree_values / layout reordering."""
+    n = len(d)
+    tc = _TreeCross(nbrs, d)
+    if initial_pivot is None:
+        rng = np.random.default_rng(0)
+        cand = np.stack([rng.integers(0, dv, 256) for dv in d], axis=1)
+        piv = cand[int(np.argmax(np.abs(sample(cand))))]
+    else:
+        piv = np.asarray(initial_pivot, dtype=np.int64)
+    piv = piv.reshape(1, n)
+    for (u, v) in tc.side:
+        tc.P[(u, v)] = tc.restrict(piv, u, v)
+    fmax = abs(float(np.asarray(sample(piv))[0]))
+    order, parent = _tree_order(nbrs, root)
+    edges = [(parent[v], v) for v in order if parent[v] >= 0]
+    rng = np.random.default_rng(1)
+    errs, ranks_prev = [], None
+    for sweep in range(nsweeps):
+        bond_err = []
+        for (u, v) in (edges if sweep % 2 == 0 else edges[::-1]):
+            rows, cols = tc.block(u, v), tc.block(v, u)
+            Pi = np.asarray(sample((rows[:, None, :] + cols[None, :, :]).reshape(-1, n))).reshape(len(rows), len(cols))
+            fmax = max(fmax, float(np.max(np.abs(Pi))))
+            pr, pc, err, _ = _aca_full(Pi, tol * fmax / max(np.max(np.abs(Pi)), 1e-300), maxbonddim)
+            if not pr:
+                continue
+            tc.P[(u, v)] = rows[pr]
+            tc.P[(v, u)] = cols[pc]
+            bond_err.append(err / max(fmax, 1e-300))
+        cores = _tree_assemble(sample, tc, root)
+        test = np.stack([rng.integers(0, dv, 512) for dv in d], axis=1)
+        miss = np.abs(_tree_values(cores, nbrs, root, test) - np.asarray(sample(test)))
+        bad = [int(i) for i in np.argsort(miss)[::-1][:4] if miss[i] > tol * fmax]
+        for i in bad:
+            pt = test[i:i + 1]
+            for (u, v) in tc.side:
+                tc.add_unique((u, v), tc.restrict(pt, u, v), maxbonddim)
+        e = max(bond_err + [float(np.max(miss)) / max(fmax, 1e-300)])
+        errs.append(e)
+        ranks = [len(tc.P[(v, u)]) for (u, v) in edges]
+        if sweep >= 1 and e <= tol and not bad and ranks == ranks_prev:
+            break
+        ranks_prev = ranks
+    cores = _tree_assemble(sample, tc, root)
+    return cores, {"sweeps": len(errs), "errors": errs,
+                   "ranks": [len(tc.P[(v, u)]) for (u, v) in edges]}
+
+
 def _mps_values(cores, idx):
     out = np.ones((idx.shape[0], 1))
     for l, A in enumerate(cores):
@@ -149,20 +315,24 @@ def _assemble(sample, d, I, J):
 def interpolate(f, s, tol: float = 1e-10, maxbonddim: int = 64, nsweeps: int = 20,
                 initial_pivot=None, dtype=None):
     """Interpolate f (vectorised: (N, n_dims) points -> N values, or an
-    ITensorNetworkFunction) into an ITensorNetworkFunction on the map s, which
-    must be path-shaped with one digit leg per vertex (ITensorTCI.interpolate
-    through tci_util.jl:21-55 accepts trees; this restatement covers paths,
-    which include the 2-D combs)."""
+    ITensorNetworkFunction) into an ITensorNetworkFunction on the map s, a
+    tree with one digit leg per vertex (ITensorTCI.interpolate through
+    tci_util.jl:21-55, which asserts is_tree(s) and maps each vertex to one
+    (dimension, digit)).  Paths (2-D combs included) use tci_path, other trees
+    tci_tree."""
     from .network import ITensorNetworkFunction
 
     lay = s.layout
     g = s.graph
     verts = s.vertices()
-    ends = [v for v in verts if len(g.neighbors(v)) <= 1]
-    if len(lay.order) < 2 or any(len(g.neighbors(v)) > 2 for v in verts) or len(g.components()) != 1:
-        raise ValueError("interpolate needs a connected path-shaped map")
+    nedges = sum(len(g.neighbors(v)) for v in verts) // 2
+    if len(lay.order) < 2 or len(g.components()) != 1 or nedges != len(verts) - 1:
+        raise ValueError("interpolate needs a connected tree")
     if any(len(s.legs[v]) != 1 for v in verts):
         raise ValueError("interpolate needs one digit leg per vertex")
+    if any(len(g.neighbors(v)) > 2 for v in verts):
+        return _interpolate_tree(f, s, tol, maxbonddim, nsweeps, initial_pivot, dtype)
+    ends = [v for v in verts if len(g.neighbors(v)) <= 1]
     # walk the path from its first end in vertex order
     path, prev, v = [], None, ends[0]
     while v is not None:
@@ -206,6 +376,43 @@ def interpolate(f, s, tol: float = 1e-10, maxbonddim: int = 64, nsweeps: int = 2
         B = A.reshape([A.shape[a] for a in sorted(keep)])
         perm = [sorted(keep).index(a) for a in order]
         B = np.transpose(B, perm)
+        if p < 0:
+            B = B.reshape(B.shape[:1] + (1,) + B.shape[1:])
+        ts[v] = B
+    out = ITensorNetworkFunction.from_tensors(s, ts, dtype=dtype)
+    out.tci_info = info
+    return out
+
+
+def _interpolate_tree(f, s, tol, maxbonddim, nsweeps, initial_pivot, dtype):
+    """interpolate() on a tree that is not a path: tci_tree over the layout's
+    vertex order (position i = lay.order[i], root 0), then each tensor's axes
+    reordered to the layout [site, parent, children...]."""
+    from .network import ITensorNetworkFunction
+
+    lay = s.layout
+    g = s.graph
+    pos = {v: i for i, v in enumerate(lay.order)}
+    nbrs = [[pos[w] for w in g.neighbors(v)] for v in lay.order]
+    legs = [s.legs[v][0] for v in lay.order]
+    ndims = max(s.dimensions())
+    if isinstance(f, ITensorNetworkFunction):
+        fn = f
+        f = lambda X: fn.evaluate_batch(X, list(range(1, ndims + 1)))
+    sampler = _PathSampler(f, legs, ndims)
+    d = [l.base for l in legs]
+    pivot = None
+    if initial_pivot is not None:
+        iv = s.calculate_ind_values(initial_pivot, list(range(1, ndims + 1)))
+        pivot = [iv[l] for l in legs]
+    cores, info = tci_tree(sampler, nbrs, d, tol=tol, maxbonddim=maxbonddim, nsweeps=nsweeps,
+                           initial_pivot=pivot, root=0)
+    ts = {}
+    for i, v in enumerate(lay.order):
+        A = cores[i]
+        p = lay.parent[i]
+        perm = [0] + ([1 + nbrs[i].index(p)] if p >= 0 else []) + [1 + nbrs[i].index(c) for c in lay.children[i]]
+        B = np.transpose(A, perm)
         if p < 0:
             B = B.reshape(B.shape[:1] + (1,) + B.shape[1:])
         ts[v] = B

@@ -35,3 +35,14 @@ def test_interpolate_a_network(ina):
     X = np.random.default_rng(2).random((2000, 1))
     assert np.max(np.abs(g.evaluate_batch(X) - h.evaluate_batch(X))) < 1e-10
     assert g.maxlinkdim() <= 3
+
+
+def test_interpolate_binary_tree_3d(ina):
+    """A 3-variable function on a 45-vertex binary tree (15 digits per
+    variable) through the tree form of TCI; checked on grid points."""
+    s = ina.continuous_siteinds(ina.named_binary_tree(45), map_dimension=3)
+    f = lambda X: np.cos(X[:, 0] + 2 * X[:, 1]) * np.exp(-X[:, 2]) + X[:, 0] * X[:, 2] ** 2
+    g = ina.interpolate(f, s, tol=1e-12, maxbonddim=32)
+    X = np.floor(np.random.default_rng(3).random((4000, 3)) * 2**15) / 2**15
+    assert np.max(np.abs(g.evaluate_batch(X, [1, 2, 3]) - f(X))) < 1e-9
+    assert g.maxlinkdim() <= 16

@@ -94,3 +94,92 @@ def test_interpolate_layout_through_the_oracle(monkeypatch):
 
     got = np.array([value(x) for x in X])
     assert np.max(np.abs(got - f(X))) < 1e-11
+
+
+def _heap_tree(n):
+    nbrs = [[] for _ in range(n)]
+    for v in range(1, n):
+        p = (v - 1) // 2
+        nbrs[p].append(v)
+        nbrs[v].append(p)
+    return nbrs
+
+
+def test_tci_tree_on_a_binary_tree():
+    """tci_tree on a 31-vertex binary tree, 3 variables with round-robin
+    digits: the assembled cross form matches f at random digit strings."""
+    from itensornumericalanalysis.tci import _tree_values, tci_tree
+
+    n = 31
+    nbrs = _heap_tree(n)
+    var = [v % 3 for v in range(n)]
+    dig = [v // 3 + 1 for v in range(n)]
+
+    def sample(idx):
+        X = np.zeros((idx.shape[0], 3))
+        for v in range(n):
+            X[:, var[v]] += idx[:, v] * 2.0 ** (-dig[v])
+        return np.cos(X[:, 0] + 2 * X[:, 1]) * np.exp(-X[:, 2]) + X[:, 0] * X[:, 2] ** 2
+
+    cores, info = tci_tree(sample, nbrs, [2] * n, tol=1e-12, maxbonddim=32)
+    idx = np.random.default_rng(5).integers(0, 2, (4000, n))
+    err = np.max(np.abs(_tree_values(cores, nbrs, 0, idx) - sample(idx)))
+    assert err < 1e-10, (err, info)
+    assert max(info["ranks"]) <= 12, info
+
+
+def test_tci_tree_agrees_with_path_version():
+    """On a path both formulations interpolate to the tolerance."""
+    from itensornumericalanalysis.tci import _tree_values, tci_tree
+
+    L = 20
+    nbrs = [[j for j in (i - 1, i + 1) if 0 <= j < L] for i in range(L)]
+    f = lambda x: np.exp(-x) * np.sin(20 * x) + x**2
+    sample = lambda idx: f(_bits_to_x(idx))
+    cores, info = tci_tree(sample, nbrs, [2] * L, tol=1e-12, maxbonddim=32)
+    pcores, pinfo = tci_path(sample, [2] * L, tol=1e-12, maxbonddim=32)
+    idx = np.random.default_rng(6).integers(0, 2, (2000, L))
+    assert np.max(np.abs(_tree_values(cores, nbrs, 0, idx) - sample(idx))) < 1e-9
+    assert np.max(np.abs(_mps_values(pcores, idx) - sample(idx))) < 1e-9
+    assert max(info["ranks"]) <= max(pinfo["ranks"]) + 2
+
+
+def test_interpolate_tree_layout_through_the_oracle(monkeypatch):
+    """interpolate() on a non-path tree (a comb with three teeth): the layout
+    tensors [site, parent, children] handed to the library contract to f on
+    grid points."""
+    import itensornumericalanalysis as ina
+    from itensornumericalanalysis.network import ITensorNetworkFunction
+
+    captured = {}
+
+    def fake_from_tensors(cls, s, ts, ctx=None, legs=None, dtype=None):
+        captured["ts"] = ts
+
+        class Dummy:
+            pass
+        return Dummy()
+
+    monkeypatch.setattr(ITensorNetworkFunction, "from_tensors", classmethod(fake_from_tensors))
+    L = 5
+    g = ina.named_comb_tree((3, L))
+    s = ina.continuous_siteinds(g, [[(i, j) for j in range(1, L + 1)] for i in range(1, 4)])
+    f = lambda X: np.exp(X[:, 0] - X[:, 1]) * np.cos(2 * X[:, 2]) + X[:, 1] * X[:, 2]
+    ina.interpolate(f, s, tol=1e-13)
+    ts = captured["ts"]
+    lay = s.layout
+    X = np.floor(np.random.default_rng(7).random((60, 3)) * 2**L) / 2**L
+
+    def value(x):
+        iv = s.calculate_ind_values(list(x), [1, 2, 3])
+
+        def up(i):
+            v = lay.order[i]
+            T = ts[v][iv[s.legs[v][0]]]
+            for c in reversed(lay.children[i]):
+                T = T @ up(c)
+            return T
+        return float(up(0)[0])
+
+    got = np.array([value(x) for x in X])
+    assert np.max(np.abs(got - f(X))) < 1e-11
