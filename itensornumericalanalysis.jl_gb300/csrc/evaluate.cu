@@ -421,6 +421,226 @@ __global__ void k_combine(const T* __restrict__ rootv, const int* __restrict__ r
   }
 }
 
+// --------------------------------------------- fused small-bond path ----
+// For networks whose bonds are all small (chi <= 8, or chi <= 16 on paths),
+// one thread walks its point through the whole tree: digits from the digit
+// program, then the vertices in post-order, each a chain of small
+// matrix-vector products against the network's tensors held in shared
+// memory, the messages in shared memory ([slot][entry][thread], conflict
+// free), each message rescaled by a power of two with the exponent carried.
+// One launch per chunk instead of about four per vertex, and no message
+// traffic through HBM.
+struct FusedStep {
+  int off;       // element offset of the vertex tensor in the shared copy
+  int vertex;
+  int chi_a;     // parent bond (1 at a root)
+  int nchild;    // 0, 1 or 2
+  int d1, d2;    // child bonds (1 when absent)
+  int in1, in2;  // message slots of the children
+  int out;       // message slot of this vertex; -1 at a root
+};
+constexpr int FUSED_MAXV = 128;
+
+template <class T, int CHI>
+__global__ void __launch_bounds__(128) k_eval_fused(
+    const double* __restrict__ X, int ncols, int Pc, const DigitEntry* __restrict__ prog, int nprog,
+    const FusedStep* __restrict__ steps, int nsteps, const T* __restrict__ tensors, int n_elem,
+    int V, int nslots, size_t off_msg, size_t off_prog, size_t off_steps, void* out, int kind,
+    int64_t P, int64_t p0, int* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // the tensors in shared memory when they fit (off_msg > 0), else read in
+  // place (a few hundred KB at most: they stay in L1 / L2)
+  const T* ts = off_msg ? (const T*)smem_raw : tensors;
+  T* msg = (T*)(smem_raw + off_msg);
+  DigitEntry* pg = (DigitEntry*)(smem_raw + off_prog);
+  FusedStep* st = (FusedStep*)(smem_raw + off_steps);
+  if (off_msg)
+    for (int i = threadIdx.x; i < n_elem; i += blockDim.x) ((T*)smem_raw)[i] = tensors[i];
+  for (int i = threadIdx.x; i < nprog; i += blockDim.x) pg[i] = prog[i];
+  for (int i = threadIdx.x; i < nsteps; i += blockDim.x) st[i] = steps[i];
+  __syncthreads();
+  const int tpb = blockDim.x, tid = threadIdx.x;
+  auto M = [&](int slot, int k) -> T& { return msg[((size_t)slot * CHI + k) * tpb + tid]; };
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < Pc; p += gridDim.x * blockDim.x) {
+    uint8_t dg[FUSED_MAXV];
+    for (int v = 0; v < V; ++v) dg[v] = 0;
+    double xr = 0.0;
+    for (int e = 0; e < nprog; ++e) {
+      const DigitEntry d = pg[e];
+      if (d.start) {
+        xr = X[(int64_t)p * ncols + d.col];
+        if (!(xr >= 0.0) || !isfinite(xr)) {
+          atomicOr(err, 1);
+          xr = 0.0;
+        }
+      }
+      int dig = 0;
+      for (int v = d.base - 1; v >= 1; --v) {
+        const double t = (double)v * d.invb;
+        if (xr >= t) {
+          dig = v;
+          xr -= t;
+          break;
+        }
+      }
+      dg[d.vertex] = (uint8_t)(dg[d.vertex] + dig * d.stride);
+    }
+    T val = Sc<T>::one();
+    int ex_acc = 0;
+    for (int i = 0; i < nsteps; ++i) {
+      const FusedStep s = st[i];
+      const int K = s.d1 * s.d2;
+      const T* Tv = ts + s.off + (int64_t)dg[s.vertex] * s.chi_a * K;
+      T o[CHI];
+      if (s.nchild == 0) {
+#pragma unroll
+        for (int a = 0; a < CHI; ++a) o[a] = a < s.chi_a ? Tv[a] : Sc<T>::zero();
+      } else {
+        T m1[CHI], m2[CHI];
+#pragma unroll
+        for (int b = 0; b < CHI; ++b) m1[b] = b < s.d1 ? M(s.in1, b) : Sc<T>::zero();
+        if (s.nchild == 2) {
+#pragma unroll
+          for (int c = 0; c < CHI; ++c) m2[c] = c < s.d2 ? M(s.in2, c) : Sc<T>::zero();
+        }
+#pragma unroll
+        for (int a = 0; a < CHI; ++a) {
+          T acc = Sc<T>::zero();
+          if (a < s.chi_a) {
+            const T* Ta = Tv + (int64_t)a * K;
+            if (s.nchild == 1) {
+#pragma unroll
+              for (int b = 0; b < CHI; ++b)
+                if (b < s.d1) acc = Sc<T>::fma(Ta[b], m1[b], acc);
+            } else {
+#pragma unroll
+              for (int b = 0; b < CHI; ++b) {
+                if (b < s.d1) {
+                  T in = Sc<T>::zero();
+#pragma unroll
+                  for (int c = 0; c < CHI; ++c)
+                    if (c < s.d2) in = Sc<T>::fma(Ta[b * s.d2 + c], m2[c], in);
+                  acc = Sc<T>::fma(m1[b], in, acc);
+                }
+              }
+            }
+          }
+          o[a] = acc;
+        }
+      }
+      if (s.out < 0) {  // a root: its parent bond is 1
+        val = val * o[0];
+        continue;
+      }
+      decltype(Sc<T>::absmax(Sc<T>::zero())) mx = 0;
+#pragma unroll
+      for (int a = 0; a < CHI; ++a) mx = max(mx, Sc<T>::absmax(o[a]));
+      const int ex = mx > 0 ? Frexp<decltype(mx)>::e(mx) : 0;
+      ex_acc += ex;
+#pragma unroll
+      for (int a = 0; a < CHI; ++a)
+        if (a < s.chi_a) M(s.out, a) = Sc<T>::scale2(o[a], -ex);
+    }
+    write_out<T>(out, kind, p0 + p, P, val, ex_acc);
+  }
+}
+
+struct FusedPlan {
+  bool ok = false;
+  int chi = 0;  // CHI of the kernel
+  int nslots = 0, tpb = 0;
+  std::vector<FusedStep> steps;
+  size_t off_msg = 0, off_prog = 0, off_steps = 0, smem = 0;
+};
+
+// Whether the fused kernel takes this network, and its schedule (post-order,
+// message slots recycled as children are consumed) and shared-memory layout.
+static FusedPlan make_fused_plan(const Topo& T, size_t tsize, size_t nprog) {
+  FusedPlan F;
+  const char* env = getenv("TNFA_EVAL_FUSED");
+  if (env && *env == '0') return F;
+  if (T.V > FUSED_MAXV) return F;
+  int chimax = 1, maxch = 0;
+  for (int v = 0; v < T.V; ++v) {
+    chimax = std::max(chimax, T.link[v]);
+    maxch = std::max(maxch, (int)T.children[v].size());
+    if (T.site_dim[v] > 256) return F;
+  }
+  if (maxch > 2 || chimax > 16 || (chimax > 8 && maxch > 1)) return F;
+  if (T.n_elem * (int64_t)tsize > 4 * 1024 * 1024) return F;
+  F.chi = chimax <= 2 ? 2 : chimax <= 4 ? 4 : chimax <= 8 ? 8 : 16;
+  std::vector<int> slot(T.V, -1), free_slots;
+  int n = 0;
+  for (int r : T.roots()) {
+    std::vector<std::pair<int, int>> stack{{r, 0}};
+    while (!stack.empty()) {
+      auto& [v, i] = stack.back();
+      if (i < (int)T.children[v].size()) {
+        const int c = T.children[v][i++];
+        stack.push_back({c, 0});
+        continue;
+      }
+      FusedStep s{};
+      s.off = (int)T.off[v];
+      s.vertex = v;
+      s.chi_a = T.link[v];
+      s.nchild = (int)T.children[v].size();
+      s.d1 = s.nchild >= 1 ? T.link[T.children[v][0]] : 1;
+      s.d2 = s.nchild >= 2 ? T.link[T.children[v][1]] : 1;
+      s.in1 = s.nchild >= 1 ? slot[T.children[v][0]] : 0;
+      s.in2 = s.nchild >= 2 ? slot[T.children[v][1]] : 0;
+      for (int c : T.children[v]) free_slots.push_back(slot[c]);
+      if (T.parent[v] >= 0) {
+        if (free_slots.empty()) free_slots.push_back(n++);
+        s.out = slot[v] = free_slots.back();
+        free_slots.pop_back();
+      } else {
+        s.out = -1;
+      }
+      F.steps.push_back(s);
+      stack.pop_back();
+    }
+  }
+  F.nslots = std::max(n, 1);
+  auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  // threads per block: as many as keep the messages within 64 KB, 32..128
+  const size_t per_thread = (size_t)F.nslots * F.chi * tsize;
+  F.tpb = (int)std::min<size_t>(128, std::max<size_t>(32, (64 * 1024 / per_thread) / 32 * 32));
+  if ((size_t)F.tpb * per_thread > 64 * 1024) return F;
+  const bool ts_smem = (size_t)T.n_elem * tsize <= 96 * 1024;
+  F.off_msg = ts_smem ? al((size_t)T.n_elem * tsize) : 0;
+  F.off_prog = al(F.off_msg + (size_t)F.tpb * per_thread);
+  F.off_steps = al(F.off_prog + nprog * sizeof(DigitEntry));
+  F.smem = F.off_steps + F.steps.size() * sizeof(FusedStep);
+  F.ok = F.smem <= 200 * 1024;
+  return F;
+}
+
+template <class T>
+static void launch_fused(tnfa_ctx* ctx, const FusedPlan& F, const FusedStep* dsteps, const T* tensors,
+                         const Topo& Tp, const double* Xc, int ncols, int Pc,
+                         const DigitEntry* dprog, int nprog, void* o, int kind, int64_t Pout,
+                         int64_t pofs, int* derr) {
+  const int tpb = F.tpb;
+  const unsigned grid = grid_for(Pc, tpb, ctx->sm_count * (2048 / tpb));
+  double fl = 0;
+  for (const auto& s : F.steps) fl += 2.0 * s.chi_a * s.d1 * s.d2;
+  KernelScope ks(ctx, "eval_fused", fl * Pc, (double)Pc * (ncols * 8.0 + 8.0));
+  auto go = [&](auto kern) {
+    TNFA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)F.smem));
+    kern<<<grid, tpb, F.smem, ctx->stream>>>(Xc, ncols, Pc, dprog, nprog, dsteps, (int)F.steps.size(),
+                                             tensors, (int)Tp.n_elem, Tp.V, F.nslots, F.off_msg,
+                                             F.off_prog, F.off_steps, o, kind, Pout, pofs, derr);
+  };
+  switch (F.chi) {
+    case 2: go(k_eval_fused<T, 2>); break;
+    case 4: go(k_eval_fused<T, 4>); break;
+    case 8: go(k_eval_fused<T, 8>); break;
+    default: go(k_eval_fused<T, 16>); break;
+  }
+  TNFA_LAUNCH_CHECK();
+}
+
 // -------------------------------------------------------------- driver ----
 struct EvalPlan {
   std::vector<int> order;        // vertices computed, children before parents
@@ -584,6 +804,14 @@ static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, 
   DBuf dout(ctx, out_mem == TNFA_MEM_HOST ? (size_t)Pcap * out_elem : 0);
   std::vector<int> root_index(V, -1);
   for (int r = 0; r < nroots; ++r) root_index[plan.roots[r]] = r;
+  // small bonds everywhere: the whole tree per thread in one launch
+  const FusedPlan F = make_fused_plan(Tp, sizeof(T), prog.size());
+  DBuf dsteps;
+  if (F.ok) {
+    dsteps = DBuf(ctx, F.steps.size() * sizeof(FusedStep));
+    TNFA_CUDA(cudaMemcpyAsync(dsteps.p, F.steps.data(), F.steps.size() * sizeof(FusedStep),
+                              cudaMemcpyHostToDevice, ctx->stream));
+  }
 
   for (int64_t p0 = 0; p0 < P; p0 += Pcap) {
     const int Pc = (int)std::min<int64_t>(Pcap, P - p0);
@@ -595,6 +823,13 @@ static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, 
     } else {
       Xc = X + p0 * ncols;
     }
+    if (F.ok) {
+      void* o = out_mem == TNFA_MEM_HOST ? dout.p : out;
+      launch_fused<T>(ctx, F, dsteps.as<FusedStep>(), tensors, Tp, Xc, ncols, Pc,
+                      dprog.as<DigitEntry>(), (int)prog.size(), o, out_kind,
+                      out_mem == TNFA_MEM_HOST ? Pc : P, out_mem == TNFA_MEM_HOST ? 0 : p0,
+                      derr.as<int>());
+    } else {
     TNFA_CUDA(cudaMemsetAsync(dS.p, 0, (size_t)V * Pcap, ctx->stream));
     if (!prog.empty()) {
       KernelScope ks(ctx, "digitize", 0.0, (double)Pc * (ncols * 8.0 + V));
@@ -704,6 +939,7 @@ static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, 
     k_combine<T><<<grid_for(Pc, 256, 8192), 256, 0, ctx->stream>>>(
         (const T*)droot.p, droote.as<int>(), nroots, Pc, o, out_kind, Pout, pofs);
     TNFA_LAUNCH_CHECK();
+    }
     if (out_mem == TNFA_MEM_HOST) {
       if (out_kind == TNFA_OUT_F32_SCALED) {
         TNFA_CUDA(cudaMemcpyAsync((float*)out + p0, dout.p, (size_t)Pc * 4, cudaMemcpyDeviceToHost,

@@ -290,3 +290,38 @@ def test_batch_composition_invariance(ina, chi):
         idx = np.arange(0, len(xs), 97 if step == 1 else 1)
         parts = np.concatenate([f.evaluate_batch(xs[idx[i:i + step]]) for i in range(0, len(idx), step)])
         assert np.max(np.abs(parts - whole[idx])) <= 1e-13 * scale, step
+
+
+@pytest.mark.parametrize("graph_name,chi", [("path20", 16), ("binary31", 8), ("comb3x5", 5), ("binary7", 2)])
+@pytest.mark.parametrize("dtype", ["f64", "f32", "c128"])
+def test_fused_small_bond_path_matches_per_vertex(ina, monkeypatch, graph_name, chi, dtype):
+    """The one-launch small-bond evaluation (k_eval_fused) against the
+    per-vertex kernels on the same network and points."""
+    L = ina._lib
+    graph = {"path20": O.path_graph(20), "binary31": O.binary_tree_graph(31),
+             "comb3x5": O.comb_tree_graph((3, 5)), "binary7": O.binary_tree_graph(7)}[graph_name]
+    nd = 1 if graph_name == "path20" else 3
+    rng = np.random.default_rng(120 + chi)
+    s_or = O.siteinds(graph, map_dimension=nd)
+    net = O.random_net(s_or, chi, rng, normalize=True)
+    f, _ = upload_oracle(ina, graph, net, dtype=L.F32 if dtype == "f32" else L.F64)
+    if dtype == "c128":
+        f = f.astype(L.C128)
+        f.scale_vertex(f.s.layout.order[0], 0.6 - 0.8j)
+    X = rng.random((5000, nd))
+    dims = list(range(1, nd + 1))
+    prec = "f32" if dtype == "f32" else "f64"
+    ctx = f.ctx
+    ctx.kernel_stats(reset=True)
+    fused = f.evaluate_batch(X, dims, precision=prec)
+    st = ctx.kernel_stats(reset=True)
+    assert st.get("eval_fused", {}).get("launches", 0) >= 1, st
+    monkeypatch.setenv("TNFA_EVAL_FUSED", "0")
+    plain = f.evaluate_batch(X, dims, precision=prec)
+    st = ctx.kernel_stats(reset=True)
+    assert st.get("eval_fused", {}).get("launches", 0) == 0, st
+    tol = 2e-5 if dtype == "f32" else 1e-12
+    assert rel_err(fused, plain) < tol
+    if dtype == "f64":  # and the oracle on a few points
+        ref = np.array([O.evaluate(net, list(x), dims) for x in X[:20]])
+        assert rel_err(fused[:20], ref) < 1e-12
