@@ -1138,18 +1138,23 @@ struct Carve {
 };
 
 // The pieces evaluate_noalloc_impl carves for P points, in order: digit
-// program, digits, permutation, group tables, error flag, message slots,
-// slot exponents, root values, root exponents.
+// program, fused schedule, digits, permutation, group tables, error flag,
+// message slots, slot exponents, root values, root exponents.  The fused
+// small-bond path needs only the program, its schedule and the error flag.
 template <class T>
-std::array<size_t, 9> noalloc_sizes(const tnfa_net* net, const EvalPlan& plan, int64_t P,
-                                    size_t prog_entries) {
+std::array<size_t, 10> noalloc_sizes(const tnfa_net* net, const EvalPlan& plan, int64_t P,
+                                     size_t prog_entries, const FusedPlan& F) {
   const Topo& Tp = net->topo;
   const int V = Tp.V;
   const int nroots = (int)plan.roots.size();
   int maxsd = 1;
   for (int v = 0; v < V; ++v) maxsd = std::max(maxsd, Tp.site_dim[v]);
   const size_t slot_vals = (size_t)P * plan.chimax;
+  if (F.ok)
+    return {prog_entries * sizeof(DigitEntry), F.steps.size() * sizeof(FusedStep), 0, 0, 0, 4,
+            0, 0, 0, 0};
   return {prog_entries * sizeof(DigitEntry),
+          0,
           (size_t)V * P,
           (size_t)P * 4,
           group_meta_ints(maxsd) * 4,
@@ -1164,7 +1169,8 @@ std::array<size_t, 9> noalloc_sizes(const tnfa_net* net, const EvalPlan& plan, i
 template <class T>
 size_t noalloc_bytes(const tnfa_net* net, int64_t P, size_t prog_entries) {
   Carve dry{nullptr, ~(size_t)0};
-  for (size_t s : noalloc_sizes<T>(net, make_plan(net->topo), P, prog_entries)) dry.take_off(s);
+  const FusedPlan F = make_fused_plan(net->topo, sizeof(T), prog_entries);
+  for (size_t s : noalloc_sizes<T>(net, make_plan(net->topo), P, prog_entries, F)) dry.take_off(s);
   return dry.used;
 }
 
@@ -1185,7 +1191,8 @@ void evaluate_noalloc_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors,
   // Dry run of the carving to size the request before touching the device.
   const int64_t P = P64;
   const size_t slot_vals = (size_t)P * plan.chimax;
-  const std::array<size_t, 9> sizes = noalloc_sizes<T>(net, plan, P, prog.size());
+  const FusedPlan F = make_fused_plan(Tp, sizeof(T), prog.size());
+  const std::array<size_t, 10> sizes = noalloc_sizes<T>(net, plan, P, prog.size(), F);
   Carve dry{nullptr, cap};
   for (size_t s : sizes) dry.take_off(s);
   if (dry.used > cap) {
@@ -1198,18 +1205,28 @@ void evaluate_noalloc_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors,
   }
   Carve cv{base, cap};
   DigitEntry* dprog = (DigitEntry*)cv.take(sizes[0]);
-  uint8_t* dS = (uint8_t*)cv.take(sizes[1]);
-  int* dperm = (int*)cv.take(sizes[2]);
-  int* meta = (int*)cv.take(sizes[3]);
-  int* derr = (int*)cv.take(sizes[4]);
-  T* slots = (T*)cv.take(sizes[5]);
-  int* slote = (int*)cv.take(sizes[6]);
-  T* rootv = (T*)cv.take(sizes[7]);
-  int* roote = (int*)cv.take(sizes[8]);
+  FusedStep* dsteps = (FusedStep*)cv.take(sizes[1]);
+  uint8_t* dS = (uint8_t*)cv.take(sizes[2]);
+  int* dperm = (int*)cv.take(sizes[3]);
+  int* meta = (int*)cv.take(sizes[4]);
+  int* derr = (int*)cv.take(sizes[5]);
+  T* slots = (T*)cv.take(sizes[6]);
+  int* slote = (int*)cv.take(sizes[7]);
+  T* rootv = (T*)cv.take(sizes[8]);
+  int* roote = (int*)cv.take(sizes[9]);
   const int Pc = (int)P;
   // the array keeps the previous call's contents: clear what must start at 0
   if (err_flag) *err_flag = derr;
   TNFA_CUDA(cudaMemsetAsync(derr, 0, 4, ctx->stream));
+  if (F.ok) {
+    if (check) {
+      if (!prog.empty())
+        TNFA_CUDA(cudaMemcpyAsync(dprog, prog.data(), sizes[0], cudaMemcpyHostToDevice, ctx->stream));
+      TNFA_CUDA(cudaMemcpyAsync(dsteps, F.steps.data(), sizes[1], cudaMemcpyHostToDevice, ctx->stream));
+    }
+    launch_fused<T>(ctx, F, dsteps, tensors, Tp, X, ncols, Pc, dprog, (int)prog.size(), out, out_kind,
+                    P, 0, derr);
+  } else {
   TNFA_CUDA(cudaMemsetAsync(dS, 0, (size_t)V * P, ctx->stream));
   if (!prog.empty()) {
     if (check)
@@ -1281,6 +1298,7 @@ void evaluate_noalloc_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors,
   k_combine<T><<<grid_for(Pc, 256, 8192), 256, 0, ctx->stream>>>(rootv, roote, nroots, Pc, out,
                                                                    out_kind, P, 0);
   TNFA_LAUNCH_CHECK();
+  }
   if (!check) return;
   int herr = 0;
   TNFA_CUDA(cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, ctx->stream));
