@@ -357,6 +357,26 @@ def secondary_measurements(ctx, ws, rank, args) -> dict:
             "value": tg * 1e6, "unit": "us per call", "eager_us": te * 1e6, "points": len(X),
             "what": "config-1 network (path 20, FP64, bond <= 32) at 4096 device points: "
                     "captured plan replay (one graph launch) vs eager tnfa_evaluate"}
+        # the same low-rank network at 10^7 device points: the fused small-bond
+        # kernel (one launch, the tree walked per point on chip) in FP64 and FP32
+        nbig = 10_000_000
+        Xbig = torch.tensor(np.random.default_rng(5).random((nbig, 1)), dtype=torch.float64, device="cuda")
+        obig = torch.empty(nbig, dtype=torch.float64, device="cuda")
+        low = {}
+        for name, net, pr in (("f64", g1, ina._lib.PREC_F64),
+                              ("f32", g1.astype(ina._lib.F32), ina._lib.PREC_F32)):
+            def big(net=net, pr=pr):
+                net.ctx.call("tnfa_evaluate", net.handle, Xbig.data_ptr(), nbig, 1, d1, ina._lib.MEM_DEVICE,
+                             obig.data_ptr(), ina._lib.OUT_F64, ina._lib.MEM_DEVICE, pr)
+            big()
+            tb, _ = _timed(big, 5)
+            low[name] = {"value": nbig / tb, "unit": "points/s", "ms": tb * 1e3,
+                         "compulsory_GBps": nbig * 16 / tb / 1e9}
+        out["lowrank_eval"] = {
+            "value": low["f64"]["value"], "unit": "points/s", "points": nbig, "f64": low["f64"],
+            "f32": low["f32"], "maxlinkdim": g1.maxlinkdim(),
+            "what": "config-1 network at 10^7 device points through the fused small-bond kernel; "
+                    "compulsory traffic 16 B/point (x in, value out)"}
     if want("gradient"):
         # --- config 4: gradient of batched evaluation --------------------------------
         import torch
