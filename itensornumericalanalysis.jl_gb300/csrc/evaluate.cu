@@ -422,7 +422,7 @@ __global__ void k_combine(const T* __restrict__ rootv, const int* __restrict__ r
 }
 
 // --------------------------------------------- fused small-bond path ----
-// For networks whose bonds are all small (chi <= 8, or chi <= 16 on paths),
+// For networks whose bonds are all small (chi <= 16, or chi <= 32 on paths),
 // one thread walks its point through the whole tree: digits from the digit
 // program, then the vertices in post-order, each a chain of small
 // matrix-vector products against the network's tensors held in shared
@@ -491,55 +491,50 @@ __global__ void __launch_bounds__(128) k_eval_fused(
       const FusedStep s = st[i];
       const int K = s.d1 * s.d2;
       const T* Tv = ts + s.off + (int64_t)dg[s.vertex] * s.chi_a * K;
-      T o[CHI];
-      if (s.nchild == 0) {
+      // the last child's message in registers; the first child's (two
+      // children) read from its slot inside the loop, which the output slot
+      // never aliases (it is taken before the children's slots are freed)
+      const int dl = s.nchild == 2 ? s.d2 : s.d1;
+      const int il = s.nchild == 2 ? s.in2 : s.in1;
+      T ml[CHI];
 #pragma unroll
-        for (int a = 0; a < CHI; ++a) o[a] = a < s.chi_a ? Tv[a] : Sc<T>::zero();
-      } else {
-        T m1[CHI], m2[CHI];
+      for (int c = 0; c < CHI; ++c) ml[c] = (s.nchild > 0 && c < dl) ? M(il, c) : Sc<T>::zero();
+      decltype(Sc<T>::absmax(Sc<T>::zero())) mx = 0;
+      T rv = Sc<T>::zero();
+      for (int a = 0; a < s.chi_a; ++a) {
+        const T* Ta = Tv + (int64_t)a * K;
+        T acc = Sc<T>::zero();
+        if (s.nchild == 0) {
+          acc = Ta[0];
+        } else if (s.nchild == 1) {
 #pragma unroll
-        for (int b = 0; b < CHI; ++b) m1[b] = b < s.d1 ? M(s.in1, b) : Sc<T>::zero();
-        if (s.nchild == 2) {
+          for (int c = 0; c < CHI; ++c)
+            if (c < dl) acc = Sc<T>::fma(Ta[c], ml[c], acc);
+        } else {
+          for (int b = 0; b < s.d1; ++b) {
+            const T* Tb = Ta + b * dl;
+            T in = Sc<T>::zero();
 #pragma unroll
-          for (int c = 0; c < CHI; ++c) m2[c] = c < s.d2 ? M(s.in2, c) : Sc<T>::zero();
-        }
-#pragma unroll
-        for (int a = 0; a < CHI; ++a) {
-          T acc = Sc<T>::zero();
-          if (a < s.chi_a) {
-            const T* Ta = Tv + (int64_t)a * K;
-            if (s.nchild == 1) {
-#pragma unroll
-              for (int b = 0; b < CHI; ++b)
-                if (b < s.d1) acc = Sc<T>::fma(Ta[b], m1[b], acc);
-            } else {
-#pragma unroll
-              for (int b = 0; b < CHI; ++b) {
-                if (b < s.d1) {
-                  T in = Sc<T>::zero();
-#pragma unroll
-                  for (int c = 0; c < CHI; ++c)
-                    if (c < s.d2) in = Sc<T>::fma(Ta[b * s.d2 + c], m2[c], in);
-                  acc = Sc<T>::fma(m1[b], in, acc);
-                }
-              }
-            }
+            for (int c = 0; c < CHI; ++c)
+              if (c < dl) in = Sc<T>::fma(Tb[c], ml[c], in);
+            acc = Sc<T>::fma(M(s.in1, b), in, acc);
           }
-          o[a] = acc;
+        }
+        if (s.out < 0) {
+          rv = acc;  // a root: its parent bond is 1
+        } else {
+          M(s.out, a) = acc;
+          mx = max(mx, Sc<T>::absmax(acc));
         }
       }
-      if (s.out < 0) {  // a root: its parent bond is 1
-        val = val * o[0];
+      if (s.out < 0) {
+        val = val * rv;
         continue;
       }
-      decltype(Sc<T>::absmax(Sc<T>::zero())) mx = 0;
-#pragma unroll
-      for (int a = 0; a < CHI; ++a) mx = max(mx, Sc<T>::absmax(o[a]));
       const int ex = mx > 0 ? Frexp<decltype(mx)>::e(mx) : 0;
       ex_acc += ex;
-#pragma unroll
-      for (int a = 0; a < CHI; ++a)
-        if (a < s.chi_a) M(s.out, a) = Sc<T>::scale2(o[a], -ex);
+      if (ex != 0)
+        for (int a = 0; a < s.chi_a; ++a) M(s.out, a) = Sc<T>::scale2(M(s.out, a), -ex);
     }
     write_out<T>(out, kind, p0 + p, P, val, ex_acc);
   }
@@ -555,7 +550,7 @@ struct FusedPlan {
 
 // Whether the fused kernel takes this network, and its schedule (post-order,
 // message slots recycled as children are consumed) and shared-memory layout.
-static FusedPlan make_fused_plan(const Topo& T, size_t tsize, size_t nprog) {
+static FusedPlan make_fused_plan(const Topo& T, size_t tsize, size_t nprog, int64_t npoints) {
   FusedPlan F;
   const char* env = getenv("TNFA_EVAL_FUSED");
   if (env && *env == '0') return F;
@@ -566,9 +561,12 @@ static FusedPlan make_fused_plan(const Topo& T, size_t tsize, size_t nprog) {
     maxch = std::max(maxch, (int)T.children[v].size());
     if (T.site_dim[v] > 256) return F;
   }
-  if (maxch > 2 || chimax > 16 || (chimax > 8 && maxch > 1)) return F;
+  if (maxch > 2 || chimax > 32 || (chimax > 16 && maxch > 1)) return F;
+  // a thread per point: above chi 8 a few thousand points leave the GPU
+  // mostly idle, where the per-vertex kernels spread a point over a warp
+  if (chimax > 8 && npoints < 32768) return F;
   if (T.n_elem * (int64_t)tsize > 4 * 1024 * 1024) return F;
-  F.chi = chimax <= 2 ? 2 : chimax <= 4 ? 4 : chimax <= 8 ? 8 : 16;
+  F.chi = chimax <= 2 ? 2 : chimax <= 4 ? 4 : chimax <= 8 ? 8 : chimax <= 16 ? 16 : 32;
   std::vector<int> slot(T.V, -1), free_slots;
   int n = 0;
   for (int r : T.roots()) {
@@ -589,7 +587,8 @@ static FusedPlan make_fused_plan(const Topo& T, size_t tsize, size_t nprog) {
       s.d2 = s.nchild >= 2 ? T.link[T.children[v][1]] : 1;
       s.in1 = s.nchild >= 1 ? slot[T.children[v][0]] : 0;
       s.in2 = s.nchild >= 2 ? slot[T.children[v][1]] : 0;
-      for (int c : T.children[v]) free_slots.push_back(slot[c]);
+      // the output slot is taken before the children's are released, so it
+      // never aliases a message the step still reads
       if (T.parent[v] >= 0) {
         if (free_slots.empty()) free_slots.push_back(n++);
         s.out = slot[v] = free_slots.back();
@@ -597,6 +596,7 @@ static FusedPlan make_fused_plan(const Topo& T, size_t tsize, size_t nprog) {
       } else {
         s.out = -1;
       }
+      for (int c : T.children[v]) free_slots.push_back(slot[c]);
       F.steps.push_back(s);
       stack.pop_back();
     }
@@ -636,7 +636,8 @@ static void launch_fused(tnfa_ctx* ctx, const FusedPlan& F, const FusedStep* dst
     case 2: go(k_eval_fused<T, 2>); break;
     case 4: go(k_eval_fused<T, 4>); break;
     case 8: go(k_eval_fused<T, 8>); break;
-    default: go(k_eval_fused<T, 16>); break;
+    case 16: go(k_eval_fused<T, 16>); break;
+    default: go(k_eval_fused<T, 32>); break;
   }
   TNFA_LAUNCH_CHECK();
 }
@@ -805,7 +806,7 @@ static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, 
   std::vector<int> root_index(V, -1);
   for (int r = 0; r < nroots; ++r) root_index[plan.roots[r]] = r;
   // small bonds everywhere: the whole tree per thread in one launch
-  const FusedPlan F = make_fused_plan(Tp, sizeof(T), prog.size());
+  const FusedPlan F = make_fused_plan(Tp, sizeof(T), prog.size(), std::min<int64_t>(P, Pcap));
   DBuf dsteps;
   if (F.ok) {
     dsteps = DBuf(ctx, F.steps.size() * sizeof(FusedStep));
@@ -1169,7 +1170,7 @@ std::array<size_t, 10> noalloc_sizes(const tnfa_net* net, const EvalPlan& plan, 
 template <class T>
 size_t noalloc_bytes(const tnfa_net* net, int64_t P, size_t prog_entries) {
   Carve dry{nullptr, ~(size_t)0};
-  const FusedPlan F = make_fused_plan(net->topo, sizeof(T), prog_entries);
+  const FusedPlan F = make_fused_plan(net->topo, sizeof(T), prog_entries, P);
   for (size_t s : noalloc_sizes<T>(net, make_plan(net->topo), P, prog_entries, F)) dry.take_off(s);
   return dry.used;
 }
@@ -1191,7 +1192,7 @@ void evaluate_noalloc_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors,
   // Dry run of the carving to size the request before touching the device.
   const int64_t P = P64;
   const size_t slot_vals = (size_t)P * plan.chimax;
-  const FusedPlan F = make_fused_plan(Tp, sizeof(T), prog.size());
+  const FusedPlan F = make_fused_plan(Tp, sizeof(T), prog.size(), P);
   const std::array<size_t, 10> sizes = noalloc_sizes<T>(net, plan, P, prog.size(), F);
   Carve dry{nullptr, cap};
   for (size_t s : sizes) dry.take_off(s);

@@ -292,14 +292,16 @@ def test_batch_composition_invariance(ina, chi):
         assert np.max(np.abs(parts - whole[idx])) <= 1e-13 * scale, step
 
 
-@pytest.mark.parametrize("graph_name,chi", [("path20", 16), ("binary31", 8), ("comb3x5", 5), ("binary7", 2)])
+@pytest.mark.parametrize("graph_name,chi", [("path20", 16), ("path20", 32), ("binary31", 8),
+                                            ("binary15", 16), ("comb3x5", 5), ("binary7", 2)])
 @pytest.mark.parametrize("dtype", ["f64", "f32", "c128"])
 def test_fused_small_bond_path_matches_per_vertex(ina, monkeypatch, graph_name, chi, dtype):
     """The one-launch small-bond evaluation (k_eval_fused) against the
     per-vertex kernels on the same network and points."""
     L = ina._lib
     graph = {"path20": O.path_graph(20), "binary31": O.binary_tree_graph(31),
-             "comb3x5": O.comb_tree_graph((3, 5)), "binary7": O.binary_tree_graph(7)}[graph_name]
+             "binary15": O.binary_tree_graph(15), "comb3x5": O.comb_tree_graph((3, 5)),
+             "binary7": O.binary_tree_graph(7)}[graph_name]
     nd = 1 if graph_name == "path20" else 3
     rng = np.random.default_rng(120 + chi)
     s_or = O.siteinds(graph, map_dimension=nd)
@@ -308,7 +310,7 @@ def test_fused_small_bond_path_matches_per_vertex(ina, monkeypatch, graph_name, 
     if dtype == "c128":
         f = f.astype(L.C128)
         f.scale_vertex(f.s.layout.order[0], 0.6 - 0.8j)
-    X = rng.random((5000, nd))
+    X = rng.random((40000 if chi > 8 else 5000, nd))  # above chi 8 the fused path wants >= 32768 points
     dims = list(range(1, nd + 1))
     prec = "f32" if dtype == "f32" else "f64"
     ctx = f.ctx
