@@ -533,6 +533,24 @@ def main():
     step_f64()
     torch.cuda.synchronize()
     f64_rate = nf / (time.perf_counter() - t0)
+
+    # integrate over [0,1)^3: the HBM-bound member of the path (every tensor
+    # byte read once by k_integrate_vertex), on the same networks
+    integ = {}
+    for name, nt in (("f32", f32net), ("f64", f64net)):
+        nt.integrate()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record()
+        reps = 5
+        for _ in range(reps):
+            nt.integrate()
+        ev1.record()
+        torch.cuda.synchronize()
+        ti = ev0.elapsed_time(ev1) / 1e3 / reps
+        nbytes = nt.info()[2] * (4 if name == "f32" else 8)
+        integ[name] = {"ms": ti * 1e3, "tensor_bytes": nbytes, "GBps": nbytes / ti / 1e9,
+                       "frac_of_hbm": nbytes / ti / 1e9 / peaks["hbm_gbs"]}
     ref64 = o64.cpu().numpy()
     o = out.cpu().numpy()
     got = np.ldexp(o[:nf].astype(np.float64), o[P:P + nf].view(np.int32))
@@ -559,6 +577,9 @@ def main():
                             "points": nf},
         "kernels": {k: {"launches_per_step": v["launches"] // args.steps,
                         "ms_per_step": v["ms"] / args.steps} for k, v in stats.items()},
+        "integrate": dict(integ, what="integrate() of the benchmark network; bytes = tensor bytes "
+                                      "(read once), time per call incl. the final readback",
+                          peak_source="MEASURED_PEAKS.json hbm_gbs"),
     }
     if not args.no_secondary:
         result["secondary"] = secondary_measurements(ctx, ws, rank, args)
