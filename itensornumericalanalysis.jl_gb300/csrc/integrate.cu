@@ -2,13 +2,13 @@
 //
 // Reference: integrate (src/integration.jl:6-17) multiplies every vertex by
 // ITensor(c, site_inds...) with c = 1/base (1 with take_sum) and contracts the
-// network with belief propagation.  Here (tnfa_integrate): the vertices in
-// post-order, one HBM-streaming launch each over all SMs that reads the
-// tensor once and contracts it at the same time with the site weights and the
-// children's messages (k_integrate_vertex); messages are kept in FP64 (or
-// complex FP64) with a power-of-two exponent per vertex.  site_reduced_net
-// (the site-reduced network as a network) serves the operator and partial
-// integrals.
+// network with belief propagation.  Here (tnfa_integrate): the vertices by
+// height, leaves first, one HBM-streaming launch per level over all SMs that
+// reads each tensor once and contracts it at the same time with the site
+// weights and the children's messages (k_integrate_level); messages are kept
+// in FP64 (or complex FP64) with a power-of-two exponent per vertex.
+// site_reduced_net (the site-reduced network as a network) serves the
+// operator and partial integrals.
 #include <cmath>
 
 #include "evaluate.cuh"
