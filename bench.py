@@ -243,6 +243,30 @@ def _timed(fn, reps=1):
     return (time.perf_counter() - t0) / reps, out
 
 
+def integrate_rates(f32net, f64net, peaks) -> dict:
+    """integrate() over [0,1)^3 of the benchmark network: the HBM-bound member
+    of the path (k_integrate_level reads every tensor byte once), FP32 and
+    FP64 copies, CUDA events on the current stream around 5 calls."""
+    import torch
+
+    out = {}
+    for name, nt in (("f32", f32net), ("f64", f64net)):
+        nt.integrate()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record()
+        reps = 5
+        for _ in range(reps):
+            nt.integrate()
+        ev1.record()
+        torch.cuda.synchronize()
+        ti = ev0.elapsed_time(ev1) / 1e3 / reps
+        nbytes = nt.info()[2] * (4 if name == "f32" else 8)
+        out[name] = {"ms": ti * 1e3, "tensor_bytes": nbytes, "GBps": nbytes / ti / 1e9,
+                     "frac_of_hbm": nbytes / ti / 1e9 / peaks["hbm_gbs"]}
+    return out
+
+
 def secondary_measurements(ctx, ws, rank, args) -> dict:
     """The other configurations of the metric, one timed repetition each after
     a warm-up: batched MPO apply + truncate (512 uneven MPS, first derivative,
@@ -258,6 +282,11 @@ def secondary_measurements(ctx, ws, rank, args) -> dict:
         return only is None or name in only
 
     out = {}
+    if only is not None and "integrate" in only:
+        s3, ts3 = config3_tensors(1)
+        n32 = ina.ITensorNetworkFunction.from_tensors(s3, ts3, ctx=ctx, dtype=ina._lib.F32)
+        out["integrate"] = integrate_rates(n32, n32.astype(ina._lib.F64), measured_peaks())
+        del n32
     if want("apply_truncate"):
         # --- config 5: MPO apply + truncate of an uneven batch -------------------
         batch = uneven_mps_batch(n=args.mps, seed=3)
@@ -423,7 +452,7 @@ def main():
     ap.add_argument("--mps", type=int, default=512, help="config-5 batch size")
     ap.add_argument("--only", default="",
                     help="run only these secondary measurements (comma list of apply_truncate, "
-                         "laplace, config1, gradient) and print them; no headline step")
+                         "laplace, config1, gradient, integrate) and print them; no headline step")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_init()
@@ -534,23 +563,7 @@ def main():
     torch.cuda.synchronize()
     f64_rate = nf / (time.perf_counter() - t0)
 
-    # integrate over [0,1)^3: the HBM-bound member of the path (every tensor
-    # byte read once by k_integrate_vertex), on the same networks
-    integ = {}
-    for name, nt in (("f32", f32net), ("f64", f64net)):
-        nt.integrate()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        ev0.record()
-        reps = 5
-        for _ in range(reps):
-            nt.integrate()
-        ev1.record()
-        torch.cuda.synchronize()
-        ti = ev0.elapsed_time(ev1) / 1e3 / reps
-        nbytes = nt.info()[2] * (4 if name == "f32" else 8)
-        integ[name] = {"ms": ti * 1e3, "tensor_bytes": nbytes, "GBps": nbytes / ti / 1e9,
-                       "frac_of_hbm": nbytes / ti / 1e9 / peaks["hbm_gbs"]}
+    integ = integrate_rates(f32net, f64net, peaks)
     ref64 = o64.cpu().numpy()
     o = out.cpu().numpy()
     got = np.ldexp(o[:nf].astype(np.float64), o[P:P + nf].view(np.int32))
