@@ -1020,23 +1020,6 @@ static std::vector<DigitEntry> make_digit_program(const Topo& T, int n_dims, con
   return prog;
 }
 
-void contract_scalar(tnfa_ctx* ctx, const tnfa_net* net, double* out_host) {
-  for (int v = 0; v < net->topo.V; ++v)
-    TNFA_CHECK(net->topo.site_dim[v] == 1, TNFA_ERR_INVALID_ARGUMENT,
-               "contract_scalar needs a network without site legs");
-  double dummy = 0.0;
-  std::vector<DigitEntry> prog;
-  if (net->dtype == TNFA_C128)
-    evaluate_impl<cplx>(ctx, net, (const cplx*)net->d, &dummy, 1, 0, prog, TNFA_MEM_HOST, out_host,
-                        TNFA_OUT_C128, TNFA_MEM_HOST, false);
-  else if (net->dtype == TNFA_F64)
-    evaluate_impl<double>(ctx, net, (const double*)net->d, &dummy, 1, 0, prog, TNFA_MEM_HOST,
-                          out_host, TNFA_OUT_F64, TNFA_MEM_HOST, false);
-  else
-    evaluate_impl<float>(ctx, net, (const float*)net->d, &dummy, 1, 0, prog, TNFA_MEM_HOST,
-                         out_host, TNFA_OUT_F64, TNFA_MEM_HOST, false);
-}
-
 }  // namespace tnfa
 
 using namespace tnfa;

@@ -54,8 +54,3 @@ int tc_tile_rows();
 
 }  // namespace tnfa
 
-namespace tnfa {
-// Scalar of a network without site legs (product over the roots of the
-// forest of the full contraction).  out: 1 double (real) or 2 (complex).
-void contract_scalar(tnfa_ctx* ctx, const tnfa_net* net, double* out_host);
-}  // namespace tnfa
