@@ -183,3 +183,40 @@ def test_interpolate_tree_layout_through_the_oracle(monkeypatch):
 
     got = np.array([value(x) for x in X])
     assert np.max(np.abs(got - f(X))) < 1e-11
+
+
+def test_tci_tree_on_random_trees():
+    """Prüfer-random trees (vertices of degree up to 5) with one digit per
+    vertex: the cross form reproduces f at random digit strings."""
+    from itensornumericalanalysis.tci import _tree_values, tci_tree
+
+    for seed, n in ((11, 18), (12, 25)):
+        rng = np.random.default_rng(seed)
+        prufer = rng.integers(0, n, n - 2)
+        degree = np.ones(n, dtype=int)
+        for x in prufer:
+            degree[x] += 1
+        nbrs = [[] for _ in range(n)]
+        for x in prufer:
+            leaf = int(np.flatnonzero(degree == 1)[0])
+            nbrs[leaf].append(int(x))
+            nbrs[int(x)].append(leaf)
+            degree[leaf] -= 1
+            degree[x] -= 1
+        u, w = (int(i) for i in np.flatnonzero(degree == 1))
+        nbrs[u].append(w)
+        nbrs[w].append(u)
+        var = [v % 2 for v in range(n)]
+        dig = [v // 2 + 1 for v in range(n)]
+
+        def sample(idx):
+            X = np.zeros((idx.shape[0], 2))
+            for v in range(n):
+                X[:, var[v]] += idx[:, v] * 2.0 ** (-dig[v])
+            return np.exp(-X[:, 0]) * np.cos(3 * X[:, 1]) + X[:, 0] * X[:, 1]
+
+        cores, info = tci_tree(sample, nbrs, [2] * n, tol=1e-12, maxbonddim=32)
+        idx = rng.integers(0, 2, (3000, n))
+        err = np.max(np.abs(_tree_values(cores, nbrs, 0, idx) - sample(idx)))
+        assert err < 1e-10, (seed, err, info)
+        assert max(len(x) for x in nbrs) >= 3
