@@ -21,7 +21,7 @@ from typing import Sequence
 import numpy as np
 
 from . import _lib
-from .indexmap import IMAG, IndsNetworkMap
+from .indexmap import IndsNetworkMap
 from .network import ITensorNetworkFunction
 
 default_c_value = 1.0

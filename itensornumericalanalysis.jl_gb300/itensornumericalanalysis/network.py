@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import TnfaError
-from .indexmap import IMAG, IndsNetworkMap, TreeLayout
+from .indexmap import IndsNetworkMap
 
 PRECISIONS = {"f64": _lib.PREC_F64, "f32": _lib.PREC_F32, "mixed": _lib.PREC_MIXED}
 
