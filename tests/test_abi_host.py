@@ -122,3 +122,32 @@ def test_reduced_maps():
     assert s2.dimensions() == [2]
     assert s2.vertices() == [(2, j) for j in range(1, 6)]
     assert s2.is_tree()
+
+
+def test_plan_and_autotune_entry_points_reject_null_handles(lib):
+    from itensornumericalanalysis import _lib
+
+    L = _lib.load()
+    assert L.tnfa_eval_plan_destroy(None) == _lib.OK  # like free(NULL)
+    assert L.tnfa_eval_plan_launch(None, None) == _lib.ERR_INVALID_ARGUMENT
+    assert L.tnfa_eval_plan_check(None, None) == _lib.ERR_INVALID_ARGUMENT
+    assert L.tnfa_eval_plan_create(None, None, None, 1, 0, None, None, 0, 0, None) == _lib.ERR_INVALID_ARGUMENT
+    assert L.tnfa_ctx_set_autotune(None, 1, -1.0, 0) == _lib.ERR_INVALID_ARGUMENT
+    need = C.c_int64()
+    assert L.tnfa_ctx_tuning_report(None, None, 0, C.byref(need)) == _lib.ERR_INVALID_ARGUMENT
+
+
+def test_opsum_site_operators_are_validated():
+    """OpSum terms name a digit operator or give a base x base matrix."""
+    from itensornumericalanalysis.elementary_operators import _op_matrix
+
+    assert np.array_equal(_op_matrix("D+", 2), np.array([[0.0, 1.0], [0.0, 0.0]]))
+    assert np.array_equal(_op_matrix("I", 3), np.eye(3))
+    m = np.arange(4.0).reshape(2, 2)
+    assert np.array_equal(_op_matrix(m, 2), m)
+    with pytest.raises(ValueError, match="2x2"):
+        _op_matrix(np.eye(3), 2)
+    with pytest.raises(ValueError, match="unknown"):
+        _op_matrix("Dx", 2)
+    with pytest.raises(ValueError, match="base 2"):
+        _op_matrix("D+", 3)
