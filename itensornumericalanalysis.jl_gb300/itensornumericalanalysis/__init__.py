@@ -61,13 +61,26 @@ from .graphs import (
 from .indexmap import (
     IndsNetworkMap,
     SiteLeg,
+    calculate_ind_values,
+    calculate_p,
     complex_continuous_siteinds,
     continuous_siteinds,
     default_dimension_vertices,
     digit_siteinds,
+    dimension,
+    dimension_inds,
+    dimension_vertices,
+    dimensions,
     grid_points,
+    indexmap,
+    indexmaptype,
+    indsnetwork,
     real_continuous_siteinds,
     reduced_indsnetworkmap,
+    vertex_digit,
+    vertex_dimension,
+    vertices_digits,
+    vertices_dimensions,
 )
 from .grad import TTNEvaluate, evaluate_vjp
 from .integration import integrate, partial_integrate

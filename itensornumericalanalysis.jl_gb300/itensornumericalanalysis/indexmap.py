@@ -316,3 +316,76 @@ def reduced_indsnetworkmap(s: IndsNetworkMap, dims) -> IndsNetworkMap:
 
 def grid_points(s: IndsNetworkMap, N: int, d: int) -> list:
     return s.grid_points(N, d)
+
+
+# ---------------------------------------------------------------------------
+# Free functions with the reference's exported names.  Each takes an
+# IndsNetworkMap or anything holding one in `.s` (an ITensorNetworkFunction),
+# as the reference forwards them from the function to its map
+# (src/itensornetworkfunction.jl:60-76).
+def _map(x) -> IndsNetworkMap:
+    return x if isinstance(x, IndsNetworkMap) else x.s
+
+
+def dimension(x, leg: SiteLeg | None = None) -> int:
+    """Number of variables, or the variable of one leg (abstractindexmap.jl)."""
+    return _map(x).dimension(leg)
+
+
+def dimensions(x) -> list[int]:
+    return _map(x).dimensions()
+
+
+def dimension_inds(x, dims) -> list[SiteLeg]:
+    """The legs of one or several variables (abstractindexmap.jl:83-89)."""
+    return _map(x).dimension_inds(dims)
+
+
+def dimension_vertices(x, dims) -> list:
+    """Vertices carrying digits of the given variable(s) (indsnetworkmap.jl:139-145)."""
+    return _map(x).dimension_vertices(dims)
+
+
+def vertex_dimension(x, v) -> int:
+    """The variable of the one leg of v (indsnetworkmap.jl:123-125)."""
+    return _map(x).vertex_dimension(v)
+
+
+def vertex_digit(x, v) -> int:
+    """The digit of the one leg of v (indsnetworkmap.jl:135-137)."""
+    return _map(x).vertex_digit(v)
+
+
+def vertices_dimensions(x, verts) -> list[int]:
+    return _map(x).vertices_dimensions(verts)
+
+
+def vertices_digits(x, verts) -> list[int]:
+    return _map(x).vertices_digits(verts)
+
+
+def calculate_ind_values(x, xs, dims=None) -> dict:
+    """Digits of a point: leg -> value (abstractindexmap.jl:121-160)."""
+    return _map(x).calculate_ind_values(xs, dims)
+
+
+def calculate_p(x, ind_values: dict, dims=None) -> list:
+    """The point a digit assignment stands for (abstractindexmap.jl:103-119)."""
+    return _map(x).calculate_p(ind_values, dims)
+
+
+def indsnetwork(x):
+    """The graph and its site legs (indsnetworkmap.jl:15): (graph, {v: [legs]})."""
+    m = _map(x)
+    return m.graph, {v: list(m.legs[v]) for v in m.vertices()}
+
+
+def indexmap(x) -> dict:
+    """The index map (indsnetworkmap.jl:16): leg -> (variable, digit)."""
+    m = _map(x)
+    return {l: (l.dim, l.digit) for v in m.vertices() for l in m.legs[v]}
+
+
+def indexmaptype(x) -> str:
+    """'complex' for a ComplexIndexMap, else 'real' (indsnetworkmap.jl:20)."""
+    return "complex" if _map(x).is_complex else "real"

@@ -151,3 +151,35 @@ def test_opsum_site_operators_are_validated():
         _op_matrix("Dx", 2)
     with pytest.raises(ValueError, match="base 2"):
         _op_matrix("D+", 3)
+
+
+def test_reference_named_free_functions():
+    """The reference's exported helpers (src/ITensorNumericalAnalysis.jl:20-66)
+    as free functions on a map or a function's map: digit round trip through
+    calculate_ind_values / calculate_p on grid points, vertex <-> (dimension,
+    digit) bookkeeping, the index map and its type."""
+    import itensornumericalanalysis as ina
+
+    L = 5
+    g = ina.named_comb_tree((2, L))
+    s = ina.continuous_siteinds(g, [[(1, j) for j in range(L, 0, -1)], [(2, j) for j in range(1, L + 1)]])
+    assert ina.dimensions(s) == [1, 2] and ina.dimension(s) == 2
+    assert sorted(ina.dimension_vertices(s, 2)) == sorted((2, j) for j in range(1, L + 1))
+    for v in s.vertices():
+        d, k = ina.vertex_dimension(s, v), ina.vertex_digit(s, v)
+        assert s.vertex(d, k) == v
+    vs = s.vertices()
+    assert ina.vertices_dimensions(s, vs) == [ina.vertex_dimension(s, v) for v in vs]
+    assert ina.vertices_digits(s, vs) == [ina.vertex_digit(s, v) for v in vs]
+    assert len(ina.dimension_inds(s, 1)) == L
+    rng = np.random.default_rng(130)
+    for _ in range(20):
+        x = np.floor(rng.random(2) * 2**L) / 2**L
+        iv = ina.calculate_ind_values(s, list(x), [1, 2])
+        assert np.allclose(ina.calculate_p(s, iv, [1, 2]), x)
+    graph, legs = ina.indsnetwork(s)
+    assert graph is s.graph and set(legs) == set(s.vertices())
+    im = ina.indexmap(s)
+    assert sorted(im.values()) == sorted((d, k) for d in (1, 2) for k in range(1, L + 1))
+    assert ina.indexmaptype(s) == "real"
+    assert ina.indexmaptype(ina.complex_continuous_siteinds(ina.named_path_graph(4))) == "complex"
