@@ -385,6 +385,12 @@ def inner(f: ITensorNetworkFunction, g: ITensorNetworkFunction):
     return f.inner(g)
 
 
+def itensornetwork(f: ITensorNetworkFunction) -> dict:
+    """The network inside the function (src/itensornetworkfunction.jl:24), as
+    host arrays: vertex name -> tensor [site legs..., parent bond, child bonds]."""
+    return f.tensors()
+
+
 def calculate_fx(f: ITensorNetworkFunction, X, dims=None, **kw) -> np.ndarray:
     """Batched evaluation (the name the GB300 API uses for evaluate over many points)."""
     return f.evaluate_batch(X, dims, **kw)
