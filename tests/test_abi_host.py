@@ -183,3 +183,22 @@ def test_reference_named_free_functions():
     assert sorted(im.values()) == sorted((d, k) for d in (1, 2) for k in range(1, L + 1))
     assert ina.indexmaptype(s) == "real"
     assert ina.indexmaptype(ina.complex_continuous_siteinds(ina.named_path_graph(4))) == "complex"
+
+
+@pytest.mark.parametrize("boundary", ["Dirichlet", "Periodic", "Neumann"])
+@pytest.mark.parametrize("n", [0, 1])
+def test_shift_opsums_match_oracle_terms(boundary, n):
+    """The product's OpSum term lists for the shift operators
+    (src/elementary_operators.jl:32-103) equal the oracle's, term for term."""
+    import itensornumericalanalysis as ina
+
+    L = 7
+    s = ina.continuous_siteinds(ina.named_path_graph(L))
+
+    def canon(terms):
+        return sorted((complex(c).real, complex(c).imag, tuple(sorted(o.items()))) for c, o in terms)
+
+    for fwd in (True, False):
+        mine = (ina.forward_shift_opsum if fwd else ina.backward_shift_opsum)(s, 1, boundary, n)
+        ref = (O.forward_shift_terms if fwd else O.backward_shift_terms)(L, 1, boundary, n)
+        assert canon(mine.terms) == canon(ref), (fwd, boundary, n)
