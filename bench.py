@@ -32,6 +32,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = "MPO-apply+truncate/s & point evals/s, mixed vs FP64 plain, rel.err<=1e-8"
 WORKLOAD = "batched_evaluate: binary tree 60 vertices, 3 vars x 20 bits, chi=128, fp32 tensors"
 N_VERT, CHI, NDIM = 60, 128, 3
+# k_contract_tc2 DRAM traffic per point (read 2.108 GB + write 1.000 GB for
+# 2e6 points in an ncu capture of this workload's two-child vertices)
+TC2_DRAM_BYTES_PER_POINT = (2.108e9 + 1.000e9) / 2.0e6
 
 
 # ------------------------------------------------------------- workload --
@@ -526,8 +529,19 @@ def main():
         # the kernel runs back to back for the whole ~2 s step, under the power
         # cap: the sustained cuBLAS figure is the denominator; burst beside it
         peak = peaks["bf16_tflops_sustained"]
+        # DRAM bytes per launch: read + write per point of a two-child chi-128
+        # vertex from an ncu capture of 2e6 points (2.108 GB + 1.000 GB),
+        # scaled to this run's average points per launch of the family
+        # (traffic grows with the points: it is their messages)
+        traffic = None
+        if tc and st["launches"]:
+            pts_per_launch = st["flops"] / st["launches"] / (2.0 * CHI ** 3)
+            traffic = TC2_DRAM_BYTES_PER_POINT * pts_per_launch
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "kernel": fam,
+                "frac": achieved / peak, "traffic": traffic,
+                "traffic_source": "ncu dram__bytes_read+write of a 2e6-point capture, "
+                                  "scaled by points per launch" if traffic else None,
+                "kernel": fam,
                 "kernel_share": st["ms"] / sum(v["ms"] for v in stats.values()),
                 "peak_source": ("MEASURED_PEAKS.json bf16 sustained (kernel timed inside a long step)"
                                 if "fallback" not in peaks else "fallback"),
