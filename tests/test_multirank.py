@@ -72,3 +72,22 @@ def test_reference_arm_under_torchrun():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2
     assert d["cpu_baseline"]["kind"] == "port" and d["value"] > 0
+
+
+def test_config5_lpt_shards_partition_the_batch():
+    """Config 5 on N GPUs splits the 512 MPS by longest-processing-time-first
+    on their apply+truncate flop estimates: every MPS exactly once, loads
+    within 4/3 of the ideal split."""
+    sys.path.insert(0, str(ROOT / "itensornumericalanalysis.jl_gb300"))
+    from itensornumericalanalysis.workloads import lpt_shards, mps_apply_truncate_cost, uneven_mps_batch
+
+    batch = uneven_mps_batch(n=512, seed=3)
+    costs = [mps_apply_truncate_cost(s, ts) for s, ts in batch]
+    assert min(costs) > 0
+    for n in (1, 2, 4, 8):
+        shards = lpt_shards(costs, n)
+        flat = sorted(i for sh in shards for i in sh)
+        assert flat == list(range(len(batch)))
+        loads = [sum(costs[i] for i in sh) for sh in shards]
+        assert max(loads) <= 4.0 / 3.0 * max(sum(costs) / n, max(costs)) + 1e-6
+    assert lpt_shards(costs, 1) == [list(range(len(batch)))]
