@@ -320,6 +320,42 @@ def delta_p(s: IndsNetworkMap, xs, dims=None):
     return _product_network(s, site)
 
 
+def _delta_overlaps(points, points_dims):
+    """The intersections delta_kernel subtracts once (src/elementary_functions.jl
+    :264-324): for every pair of (point, dims) sets that are not two distinct
+    points on the same dims, the union of their coordinates, unless the two
+    fix one dimension at different values (no intersection).  Returns
+    (points, dims) lists."""
+    over_p, over_d = [], []
+    for i in range(len(points)):
+        p1, d1 = list(points[i]), list(points_dims[i])
+        for j in range(i + 1, len(points)):
+            p2, d2 = list(points[j]), list(points_dims[j])
+            if len(d1) == len(d2) and np.allclose(d1, d2) and not (
+                len(p1) == len(p2) and np.allclose(p1, p2)
+            ):
+                continue
+            ps_, ds_ = p1 + p2, d1 + d2
+            order = sorted(range(len(ds_)), key=lambda q: ds_[q])
+            ps, ds = [ps_[order[0]]], [ds_[order[0]]]
+            for q in range(1, len(ds_)):
+                if ds_[order[q]] != ds_[order[q - 1]]:
+                    ps.append(ps_[order[q]])
+                    ds.append(ds_[order[q]])
+                    continue
+                # same dimension twice: the reference compares ps_[q] and
+                # ps_[q-1] (unsorted positions) here
+                if np.isclose(ps_[q], ps_[q - 1]):
+                    continue
+                ps, ds = [], []
+                break
+            if not ds:
+                continue
+            over_p.append(ps)
+            over_d.append(ds)
+    return over_p, over_d
+
+
 def delta_kernel(s: IndsNetworkMap, points, points_dims=None, remove_overlap: bool = True,
                  coeff=-1.0, include_identity: bool = True):
     """const + coeff * sum of delta_p over points, minus the double-counted
@@ -330,33 +366,7 @@ def delta_kernel(s: IndsNetworkMap, points, points_dims=None, remove_overlap: bo
     if include_identity:
         psi = const_itensornetwork(s) + psi
     if remove_overlap and len(points) > 1:
-        over_p, over_d = [], []
-        for i in range(len(points)):
-            p1, d1 = list(points[i]), list(points_dims[i])
-            for j in range(i + 1, len(points)):
-                p2, d2 = list(points[j]), list(points_dims[j])
-                if len(d1) == len(d2) and np.allclose(d1, d2) and not (
-                    len(p1) == len(p2) and np.allclose(p1, p2)
-                ):
-                    continue
-                ps_, ds_ = p1 + p2, d1 + d2
-                order = sorted(range(len(ds_)), key=lambda q: ds_[q])
-                ps, ds = [ps_[order[0]]], [ds_[order[0]]]
-                for q in range(1, len(ds_)):
-                    if ds_[order[q]] != ds_[order[q - 1]]:
-                        ps.append(ps_[order[q]])
-                        ds.append(ds_[order[q]])
-                        continue
-                    # same dimension twice: the reference compares ps_[q] and
-                    # ps_[q-1] (unsorted positions) here
-                    if np.isclose(ps_[q], ps_[q - 1]):
-                        continue
-                    ps, ds = [], []
-                    break
-                if not ds:
-                    continue
-                over_p.append(ps)
-                over_d.append(ds)
+        over_p, over_d = _delta_overlaps(points, points_dims)
         if over_p:
             psi = psi + (-coeff) * delta_p(s, over_p, over_d)
     return psi

@@ -202,3 +202,72 @@ def test_shift_opsums_match_oracle_terms(boundary, n):
         mine = (ina.forward_shift_opsum if fwd else ina.backward_shift_opsum)(s, 1, boundary, n)
         ref = (O.forward_shift_terms if fwd else O.backward_shift_terms)(L, 1, boundary, n)
         assert canon(mine.terms) == canon(ref), (fwd, boundary, n)
+
+
+def _on(s, x, p, d):
+    """1 when the digits of point x agree with those of p on dims d."""
+    full = s.calculate_ind_values(list(x), list(range(1, len(x) + 1)))
+    part = s.calculate_ind_values(list(p), list(d))
+    return float(all(full[l] == v for l, v in part.items()))
+
+
+def _kernel_value(s, x, points, dims, coeff=-1.0):
+    from itensornumericalanalysis.elementary_functions import _delta_overlaps
+
+    over_p, over_d = _delta_overlaps(points, dims)
+    val = 1.0 + coeff * sum(_on(s, x, p, d) for p, d in zip(points, dims))
+    return val - coeff * sum(_on(s, x, p, d) for p, d in zip(over_p, over_d))
+
+
+def test_delta_kernel_overlaps_match_reference_cases():
+    """test/test_operators.jl:415-515 restated through the indicator the
+    kernel stands for (1 + coeff sum of point/plane deltas - coeff sum of the
+    overlaps that _delta_overlaps lists), at the reference's points."""
+    import itensornumericalanalysis as ina
+
+    # 1D: one point
+    g = ina.named_comb_tree((2, 3))
+    s = ina.continuous_siteinds(g)
+    delta = 2.0 ** -g.nv()
+    assert _kernel_value(s, [0.5], [[0.5]], [[1]]) == 0
+    for x in [0.0, delta, 0.25, 0.625, 0.875, 1 - delta]:
+        assert _kernel_value(s, [x], [[0.5]], [[1]]) == 1
+    # 2D, intersecting lines and line + point
+    g = ina.named_comb_tree((2, 3))
+    s = ina.continuous_siteinds(g, map_dimension=2)
+    delta = 2.0 ** -(g.nv() // 2)
+    xs = [0.0, delta, 0.25, 0.625, 0.875, 1 - delta]
+    P, D = [[0.5], [0.5]], [[1], [2]]
+    assert _kernel_value(s, [0.5, 0.5], P, D) == 0
+    for x in xs:
+        assert _kernel_value(s, [x, 0.5], P, D) == 0
+        assert _kernel_value(s, [0.5, x], P, D) == 0
+        assert _kernel_value(s, [x, delta], P, D) == 1
+        assert _kernel_value(s, [delta, x], P, D) == 1
+    P, D = [[0.5], [0.5, 0.1]], [[1], [1, 2]]
+    assert _kernel_value(s, [0.5, 0.5], P, D) == 0
+    assert _kernel_value(s, [0.5, 0.1], P, D) == 0
+    for x in xs:
+        assert _kernel_value(s, [0.5, x], P, D) == 0
+        assert _kernel_value(s, [x, delta], P, D) == 1
+        assert _kernel_value(s, [delta, x], P, D) == 1
+    # 3D, intersecting planes, plane + line, two lines meeting at an endpoint
+    g = ina.named_comb_tree((3, 2))
+    s = ina.continuous_siteinds(g, map_dimension=3)
+    delta = 2.0 ** -(g.nv() // 3)
+    xs, zs = [0.0, delta, 1 - delta], [0, delta, 0.5, 1 - delta]
+    for P, D in (([[0.5], [0.5]], [[1], [2]]), ([[0.5], [0.5, 0]], [[1], [1, 2]])):
+        for z in zs:
+            assert _kernel_value(s, [0.5, 0.5, z], P, D) == 0
+            for x in xs:
+                if len(P[1]) == 1:  # two planes: the second one too
+                    assert _kernel_value(s, [x, 0.5, z], P, D) == 0
+                assert _kernel_value(s, [0.5, x, z], P, D) == 0
+                assert _kernel_value(s, [x, delta, z], P, D) == 1
+                assert _kernel_value(s, [delta, x, z], P, D) == 1
+    P, D = [[0.5, 0], [0, 0.5]], [[2, 3], [1, 2]]
+    assert _kernel_value(s, [0.0, 0.5, 0.5], P, D) == 0
+    for x in xs:
+        assert _kernel_value(s, [x, 0.5, 0], P, D) == 0
+        assert _kernel_value(s, [x, delta, 0], P, D) == 1
+        assert _kernel_value(s, [delta, x, 0], P, D) == 1
