@@ -1,6 +1,6 @@
 """Gradients of batched evaluation (the rrule of evaluate).
 
-The reference has no automatic differentiation; the benchmark spec asks for a
+The reference has no automatic differentiation; a Julia caller binds a
 hand-written backward pass behind a ChainRulesCore.rrule.  Here
 `tnfa_evaluate_vjp` is that backward pass; `evaluate_vjp` returns it per
 vertex, and `TTNEvaluate` wraps forward + backward as a torch.autograd.Function
