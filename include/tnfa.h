@@ -55,9 +55,14 @@ typedef enum { TNFA_MEM_HOST = 0, TNFA_MEM_DEVICE = 1 } tnfa_memory;
 
 /* Arithmetic used by tnfa_evaluate. */
 typedef enum {
-  TNFA_PREC_F64 = 0,   /* plain FP64 on the CUDA cores                                */
-  TNFA_PREC_F32 = 1,   /* FP32 on the CUDA cores                                      */
-  TNFA_PREC_MIXED = 2  /* tcgen05 tensor cores, split-BF16 (hi/lo) operands, FP32 acc */
+  TNFA_PREC_F64 = 0,       /* plain FP64 on the CUDA cores                                 */
+  TNFA_PREC_F32 = 1,       /* FP32 on the CUDA cores                                       */
+  TNFA_PREC_MIXED = 2,     /* FP64 messages; two-child vertices (bonds 64/128) as exact
+                              products of 8-bit integer slices on the tcgen05 tensor cores
+                              (26 BF16 passes, FP32 accumulation exact), FP64-class result.
+                              In truncation: FP32-preconditioned Jacobi with FP64 polish.  */
+  TNFA_PREC_MIXED_FAST = 3 /* FP32 messages, tcgen05 split-BF16 (hi/lo, 3 passes) products:
+                              about 1e-5 relative (norm-wise) on random bond-128 trees     */
 } tnfa_precision;
 
 /* Leg kinds (tnfa_topology.leg_kind). */
@@ -136,6 +141,16 @@ int tnfa_ctx_set_autotune(tnfa_ctx* ctx, int enable, double min_work, int forget
 int tnfa_ctx_tuning_report(tnfa_ctx* ctx, char* buf, int64_t size, int64_t* needed);
 int tnfa_ctx_kernel_stats(tnfa_ctx* ctx, int32_t max, char* names, int64_t* launches, double* ms,
                           double* flops, double* bytes, int32_t* n_families, int reset);
+
+/* Wait budget of the tensor-core pipelines: every mbarrier wait in a tcgen05
+ * kernel gives up after `polls` try_wait polls (0 keeps the current budget;
+ * the default is 2^26), the kernel stops, releases its tensor memory and the
+ * call returns TNFA_ERR_TIMEOUT.  drop_arrive != 0 is a test switch: the
+ * sliced tensor-core evaluation then withholds the arrive that releases its
+ * MMA issuer, so that a wait runs out (with a small budget) and the timeout
+ * path can be exercised; 0 restores normal operation.  No counterpart in the
+ * reference (it has no device pipelines). */
+int tnfa_ctx_set_wait_budget(tnfa_ctx* ctx, uint32_t polls, int drop_arrive);
 
 /* ---- networks ----------------------------------------------------------- */
 

@@ -156,6 +156,10 @@ struct tnfa_ctx {
   std::map<std::string, std::vector<float>> tuned_ms;
   std::vector<tnfa::KernelFamily> families;
   std::vector<cudaEvent_t> event_pool;
+  // tensor-core pipelines: try_wait polls before an mbarrier wait gives up,
+  // and a test switch that withholds one arrive so that a wait runs out
+  uint32_t tc_wait_limit = 1u << 26;
+  int tc_drop_arrive = 0;
 };
 
 struct tnfa_net {
@@ -167,6 +171,9 @@ struct tnfa_net {
   mutable void* d_f32 = nullptr;   // FP32 copy of a real network
   mutable void* d_bhi = nullptr;   // BF16 hi part (tensor-core evaluation)
   mutable void* d_blo = nullptr;   // BF16 lo part
+  mutable void* d_f64 = nullptr;   // FP64 copy of an FP32 network (accurate mixed path)
+  mutable void* d_oz = nullptr;    // BF16 digit planes of two-child vertices (evaluate_oz.cu)
+  mutable int* d_ozexp = nullptr;  // their per-(site value, parent index) exponents
   void invalidate_caches() const;
 };
 

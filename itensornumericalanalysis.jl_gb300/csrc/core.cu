@@ -280,7 +280,11 @@ void tnfa_net::invalidate_caches() const {
   if (d_f32) tnfa::dfree(ctx, d_f32);
   if (d_bhi) tnfa::dfree(ctx, d_bhi);
   if (d_blo) tnfa::dfree(ctx, d_blo);
-  d_f32 = d_bhi = d_blo = nullptr;
+  if (d_f64) tnfa::dfree(ctx, d_f64);
+  if (d_oz) tnfa::dfree(ctx, d_oz);
+  if (d_ozexp) tnfa::dfree(ctx, d_ozexp);
+  d_f32 = d_bhi = d_blo = d_f64 = d_oz = nullptr;
+  d_ozexp = nullptr;
 }
 
 using namespace tnfa;
@@ -392,6 +396,13 @@ int tnfa_ctx_kernel_stats(tnfa_ctx* ctx, int32_t max, char* names, int64_t* laun
   }
   if (reset) ctx->families.clear();
   TNFA_API_END
+}
+
+int tnfa_ctx_set_wait_budget(tnfa_ctx* ctx, uint32_t polls, int drop_arrive) {
+  if (!ctx) return TNFA_ERR_INVALID_ARGUMENT;
+  if (polls) ctx->tc_wait_limit = polls;
+  ctx->tc_drop_arrive = drop_arrive ? 1 : 0;
+  return TNFA_OK;
 }
 
 int tnfa_ctx_destroy(tnfa_ctx* ctx) {

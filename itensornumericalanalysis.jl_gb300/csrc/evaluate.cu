@@ -652,6 +652,11 @@ struct EvalPlan {
   int chimax = 1;
 };
 
+// A vertex's output slot is taken while its children still hold theirs, so
+// that it never shares memory with the messages it reads: the contraction
+// kernels write their output as they go (tiles split over columns, the
+// sliced kernel's two phases) and the autotuner runs one contraction several
+// times over the same inputs.
 static EvalPlan make_plan(const Topo& T) {
   EvalPlan P;
   P.fused_leaf.assign(T.V, 0);
@@ -676,14 +681,14 @@ static EvalPlan make_plan(const Topo& T) {
   std::vector<int> free_slots;
   int n = 0;
   for (int v : P.order) {
-    for (int c : T.children[v])
-      if (!P.fused_leaf[c]) free_slots.push_back(P.slot[c]);
     if (T.parent[v] >= 0) {
       if (free_slots.empty()) free_slots.push_back(n++);
       P.slot[v] = free_slots.back();
       free_slots.pop_back();
       P.chimax = std::max(P.chimax, T.link[v]);
     }
+    for (int c : T.children[v])
+      if (!P.fused_leaf[c]) free_slots.push_back(P.slot[c]);
   }
   P.nslots = n;
   return P;
@@ -769,7 +774,8 @@ static int contract_tile_rows(int chi_a, int sumdim, size_t tsize) {
 template <class T>
 static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, const double* X,
                           int64_t P, int ncols, const std::vector<DigitEntry>& prog, int xmem,
-                          void* out, int out_kind, int out_mem, bool use_tc) {
+                          void* out, int out_kind, int out_mem, bool use_tc,
+                          bool use_oz = false) {
   const Topo& Tp = net->topo;
   const int V = Tp.V;
   EvalPlan plan = make_plan(Tp);
@@ -878,11 +884,14 @@ static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, 
         j.out_exp = dslote.as<int>() + (size_t)plan.slot[v] * Pcap;
       }
       const bool tc = use_tc && j.site_dim <= 256 && tc_vertex_eligible(j.nchild, cdims, j.chi_a);
+      const bool oz = use_oz && oz_vertex_eligible(j.nchild, cdims, j.chi_a);
       // SIMT shapes: the tile kept by the autotuner for this shape, else the rule's
       std::vector<GemmTile> cand;
       std::string key;
-      int tp = tc ? tc_tile_rows() : contract_tile_rows(j.chi_a, sumdim, sizeof(T));
-      if (!tc && j.chi_a > 16) {
+      int tp = tc   ? tc_tile_rows()
+               : oz ? oz_tile_rows()
+                    : contract_tile_rows(j.chi_a, sumdim, sizeof(T));
+      if (!tc && !oz && j.chi_a > 16) {
         cand = gemm_tile_candidates(j.chi_a, sumdim, sizeof(T));
         key = std::string("simt:") + FamilyName<T>::v + ":" + std::to_string(j.chi_a) + ":";
         for (int i = 0; i < j.nchild; ++i) key += std::to_string(cdims[i]) + (i + 1 < j.nchild ? "x" : "");
@@ -915,6 +924,12 @@ static void evaluate_impl(tnfa_ctx* ctx, const tnfa_net* net, const T* tensors, 
       if constexpr (std::is_same<T, float>::value) {
         if (tc) {
           tc_contract_vertex(ctx, net, v, j, tp, derr.as<int>());
+          continue;
+        }
+      }
+      if constexpr (std::is_same<T, double>::value) {
+        if (oz) {
+          oz_contract_vertex(ctx, net, v, j, tp, derr.as<int>());
           continue;
         }
       }
@@ -1056,7 +1071,15 @@ extern "C" int tnfa_evaluate(tnfa_ctx* ctx, const tnfa_net* net, const double* X
       TNFA_CHECK(net->dtype == TNFA_F64, TNFA_ERR_DTYPE, "TNFA_PREC_F64 needs an FP64 network");
       evaluate_impl<double>(ctx, net, (const double*)net->d, X, n_points, ncols, prog, x_memory,
                             out, out_kind, out_memory, false);
-    } else if (precision == TNFA_PREC_F32 || precision == TNFA_PREC_MIXED) {
+    } else if (precision == TNFA_PREC_MIXED) {
+      // FP64 messages; two-child vertices of tensor-core shape take the
+      // error-free sliced products, the rest the FP64 kernels
+      oz_prepare_net(ctx, net);
+      const double* t64 =
+          net->dtype == TNFA_F64 ? (const double*)net->d : (const double*)net->d_f64;
+      evaluate_impl<double>(ctx, net, t64, X, n_points, ncols, prog, x_memory, out, out_kind,
+                            out_memory, false, true);
+    } else if (precision == TNFA_PREC_F32 || precision == TNFA_PREC_MIXED_FAST) {
       const float* t32;
       if (net->dtype == TNFA_F32) {
         t32 = (const float*)net->d;
@@ -1067,9 +1090,9 @@ extern "C" int tnfa_evaluate(tnfa_ctx* ctx, const tnfa_net* net, const double* X
         }
         t32 = (const float*)net->d_f32;
       }
-      if (precision == TNFA_PREC_MIXED) tc_prepare_net(ctx, net);
+      if (precision == TNFA_PREC_MIXED_FAST) tc_prepare_net(ctx, net);
       evaluate_impl<float>(ctx, net, t32, X, n_points, ncols, prog, x_memory, out, out_kind,
-                           out_memory, precision == TNFA_PREC_MIXED);
+                           out_memory, precision == TNFA_PREC_MIXED_FAST);
     } else {
       fail(TNFA_ERR_INVALID_ARGUMENT, "unknown precision");
     }

@@ -1,6 +1,8 @@
 // Internal interface of the batched evaluation engine (shared by the SIMT
 // kernels in evaluate.cu and the tensor-core kernels in evaluate_tc.cu).
 #pragma once
+#include <cuda.h>
+
 #include "common.cuh"
 
 namespace tnfa {
@@ -51,6 +53,18 @@ void tc_prepare_net(tnfa_ctx* ctx, const tnfa_net* net);  // BF16 hi/lo copies
 void tc_contract_vertex(tnfa_ctx* ctx, const tnfa_net* net, int v, const VertexJob<float>& job,
                         int tile_rows, int* err);
 int tc_tile_rows();
+// 3-D BF16 tensor map {x_dim, y_dim, z_dim} (x contiguous) with a box of
+// {64, box_y, box_z} elements and 128-byte swizzle.
+CUtensorMap tc_make_map3(const void* base, int x_dim, int y_dim, int64_t z_dim, int box_y,
+                         int box_z);
+
+// Error-free sliced tensor-core contraction (evaluate_oz.cu): a vertex of two
+// children evaluated from FP64 messages to FP64 messages on tcgen05.
+bool oz_vertex_eligible(int nchild, const int* child_dims, int chi_a);
+void oz_prepare_net(tnfa_ctx* ctx, const tnfa_net* net);  // digit planes of the tensors
+void oz_contract_vertex(tnfa_ctx* ctx, const tnfa_net* net, int v, const VertexJob<double>& job,
+                        int tile_rows, int* err);
+int oz_tile_rows();
 
 }  // namespace tnfa
 

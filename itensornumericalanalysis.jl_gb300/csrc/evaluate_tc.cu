@@ -26,6 +26,7 @@
 #include <mutex>
 
 #include "evaluate.cuh"
+#include "tc_ptx.cuh"
 
 namespace tnfa {
 
@@ -35,120 +36,8 @@ constexpr int TC_M = 128;         // rows per tile (points)
 constexpr int TC_KC = 64;         // K elements per chunk (128 bytes of BF16)
 constexpr int TC_PRODUCERS = 256; // warps 0-7
 constexpr int TC_THREADS = 320;
-constexpr uint32_t TC_WAIT_LIMIT = 1u << 26;  // try_wait iterations before giving up
-constexpr int TC_ERR_TIMEOUT = 2;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-
-// Bounded wait for the phase with the given parity; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t addr = smem_u32(bar);
-  for (uint32_t it = 0; it < TC_WAIT_LIMIT; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                            int x, int y) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
-      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
-      : "memory");
-}
-
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                            int x, int y, int z) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
-      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
-// 1024 bytes (SBO), version 1.
-__device__ __forceinline__ uint64_t sw128_desc(const void* base) {
-  uint64_t a = smem_u32(base);
-  uint64_t d = (a & 0x3FFFFull) >> 4;
-  d |= (uint64_t)1 << 16;            // leading byte offset (unused for this layout)
-  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
-  d |= (uint64_t)1 << 46;            // descriptor version
-  d |= (uint64_t)2 << 61;            // SWIZZLE_128B
-  return d;
-}
-
-// Instruction descriptor, kind::f16: BF16 x BF16 -> FP32, both K-major.
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
-         ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-  return *reinterpret_cast<uint32_t*>(&h);
-}
+using namespace ptx;
+constexpr int TC_ERR_TIMEOUT = ptx::ERR_TIMEOUT;
 
 struct TcParams {
   const float* m1_ptr;   // child 1 rows (message or leaf tensor); null: chi1 = 1
@@ -166,6 +55,7 @@ struct TcParams {
   const int* tile_start;
   int ngroups;
   int* err;
+  uint32_t wait_limit;  // try_wait polls before a wait gives up
 };
 
 // BILIN = false: Kronecker mode above (output N = chi_a columns).
@@ -265,7 +155,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for (int cblk = 0; cblk < CPB; ++cblk) {
         const int kc = bb * CPB + cblk;
         const int s = kc % STAGES, use = kc / STAGES;
-        if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+        if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1, P.wait_limit)) {
           ok = false;
           break;
         }
@@ -297,7 +187,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       sh_abort = 1;
     }
     // ------------------------------------------------------- epilogue ----
-    const bool acc_ok = mbar_wait(&acc_bar, 0);
+    const bool acc_ok = mbar_wait(&acc_bar, 0, P.wait_limit);
     if (!acc_ok) {
       atomicOr(P.err, TC_ERR_TIMEOUT);
       sh_abort = 1;
@@ -350,7 +240,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       bool ok = true;
       for (int kc = 0; kc < nk; ++kc) {
         const int s = kc % STAGES, use = kc / STAGES;
-        if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+        if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1, P.wait_limit)) {
           ok = false;
           break;
         }
@@ -369,7 +259,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       bool ok = true;
       for (int kc = 0; kc < nk; ++kc) {
         const int s = kc % STAGES, use = kc / STAGES;
-        if (!mbar_wait(&full_bar[s], use & 1)) {
+        if (!mbar_wait(&full_bar[s], use & 1, P.wait_limit)) {
           ok = false;
           break;
         }
@@ -542,7 +432,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int i = 0; i < NBT; ++i) mbn[i] = valid ? m1row[(t + 1) * NBT + i] : 0.f;
       }
       const int buf = t & 1;
-      if (!mbar_wait(&tfull[buf], (t >> 1) & 1)) {
+      if (!mbar_wait(&tfull[buf], (t >> 1) & 1, P.wait_limit)) {
         ok = false;
         break;
       }
@@ -588,7 +478,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int nst = ntiles * KCH;
       for (int si = 0; si < nst; ++si) {
         const int s = si % STAGES, use = si / STAGES;
-        if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+        if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1, P.wait_limit)) {
           ok = false;
           break;
         }
@@ -605,11 +495,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // ------------------------------------------------------------ MMA ----
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16(TC_M, T2_N);
-      bool ok = mbar_wait(&a_ready, 0);
+      bool ok = mbar_wait(&a_ready, 0, P.wait_limit);
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       for (int t = 0; t < ntiles && ok; ++t) {
         const int buf = t & 1;
-        if (t >= 2 && !mbar_wait(&tempty[buf], ((t >> 1) - 1) & 1)) {
+        if (t >= 2 && !mbar_wait(&tempty[buf], ((t >> 1) - 1) & 1, P.wait_limit)) {
           ok = false;
           break;
         }
@@ -618,7 +508,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int kc = 0; kc < KCH; ++kc) {
           const int si = t * KCH + kc;
           const int s = si % STAGES, use = si / STAGES;
-          if (!mbar_wait(&full_bar[s], use & 1)) {
+          if (!mbar_wait(&full_bar[s], use & 1, P.wait_limit)) {
             ok = false;
             break;
           }
@@ -745,6 +635,11 @@ struct TcCache {
 
 }  // namespace
 
+CUtensorMap tc_make_map3(const void* base, int x_dim, int y_dim, int64_t z_dim, int box_y,
+                         int box_z) {
+  return make_map3(base, x_dim, y_dim, z_dim, box_y, box_z);
+}
+
 bool tc_vertex_eligible(int nchild, const int* child_dims, int chi_a) {
   if (nchild < 1 || nchild > 2) return false;
   const int chi2 = child_dims[nchild - 1];
@@ -822,6 +717,7 @@ void tc_contract_vertex(tnfa_ctx* ctx, const tnfa_net* net, int v, const VertexJ
   p.tile_start = j.tile_start;
   p.ngroups = j.ngroups;
   p.err = err;
+  p.wait_limit = ctx->tc_wait_limit;
   const unsigned grid = (unsigned)((j.Pc + TC_M - 1) / TC_M + j.ngroups);
   KernelScope ks(ctx, "contract_tc", 2.0 * j.Pc * (double)j.K * j.chi_a,
                  4.0 * ((double)j.Pc * (p.chi1 + p.chi2 + j.chi_a)) +

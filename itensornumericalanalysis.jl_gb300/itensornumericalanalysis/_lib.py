@@ -43,7 +43,7 @@ F64, F32, C128 = 0, 1, 2
 # tnfa_memory
 MEM_HOST, MEM_DEVICE = 0, 1
 # tnfa_precision
-PREC_F64, PREC_F32, PREC_MIXED = 0, 1, 2
+PREC_F64, PREC_F32, PREC_MIXED, PREC_MIXED_FAST = 0, 1, 2, 3
 # tnfa_leg_kind
 LEG_REAL, LEG_IMAG, LEG_OPERATOR = 0, 1, 2
 # tnfa_out
@@ -118,6 +118,7 @@ SIGNATURES = {
     "tnfa_ctx_create": (C.c_int, [C.c_int, _P, _PP]),
     "tnfa_ctx_destroy": (C.c_int, [_P]),
     "tnfa_ctx_synchronize": (C.c_int, [_P]),
+    "tnfa_ctx_set_wait_budget": (C.c_int, [_P, C.c_uint32, C.c_int]),
     "tnfa_last_error_string": (C.c_char_p, [_P]),
     "tnfa_ctx_set_timing": (C.c_int, [_P, C.c_int]),
     "tnfa_ctx_set_autotune": (C.c_int, [_P, C.c_int, C.c_double, C.c_int]),
@@ -253,6 +254,12 @@ class Context:
             nm = names.raw[32 * i : 32 * i + 32].split(b"\0")[0].decode()
             out[nm] = {"launches": la[i], "ms": ms[i], "flops": fl[i], "bytes": by[i]}
         return out
+
+    def set_wait_budget(self, polls: int = 0, drop_arrive: bool = False) -> None:
+        """tnfa_ctx_set_wait_budget: try_wait polls before a tensor-core
+        pipeline wait gives up (0 keeps the budget), and the test switch that
+        withholds one arrive so that a wait runs out."""
+        self.check(self.lib.tnfa_ctx_set_wait_budget(self.handle, int(polls), int(drop_arrive)))
 
     def synchronize(self) -> None:
         self.call("tnfa_ctx_synchronize")

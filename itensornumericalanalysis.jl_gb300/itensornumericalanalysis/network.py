@@ -16,7 +16,8 @@ from . import _lib
 from ._lib import TnfaError
 from .indexmap import IndsNetworkMap
 
-PRECISIONS = {"f64": _lib.PREC_F64, "f32": _lib.PREC_F32, "mixed": _lib.PREC_MIXED}
+PRECISIONS = {"f64": _lib.PREC_F64, "f32": _lib.PREC_F32, "mixed": _lib.PREC_MIXED,
+              "mixed_fast": _lib.PREC_MIXED_FAST}
 
 
 def _i32(a) -> C.Array:
@@ -216,8 +217,11 @@ class ITensorNetworkFunction:
                        device_out=None) -> np.ndarray:
         """f at every row of X (n_points x len(dims)); complex maps take complex X.
 
-        precision: "f64" (plain FP64), "f32" (FP32 CUDA cores) or "mixed"
-        (tcgen05 tensor cores, split-BF16, FP32 accumulation)."""
+        precision: "f64" (plain FP64), "f32" (FP32 CUDA cores), "mixed"
+        (FP64 messages; bond-64/128 vertices as exact products of 8-bit
+        integer slices on the tcgen05 tensor cores, FP64-class accuracy) or
+        "mixed_fast" (FP32 messages, split-BF16 tensor-core products, about
+        1e-5 relative on random bond-128 trees)."""
         dims = self.s.dimensions() if dims is None else ([dims] if isinstance(dims, int) else list(dims))
         X = np.asarray(X)
         if X.ndim == 1:

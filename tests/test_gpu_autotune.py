@@ -48,7 +48,7 @@ def test_tensor_core_formulation_tuned(ina):
     ctx.set_autotune(True, min_work=0.0, forget=True)
 
     def mixed():
-        m, e = f.evaluate_batch(X, precision="mixed", out="f32_scaled")
+        m, e = f.evaluate_batch(X, precision="mixed_fast", out="f32_scaled")
         return np.ldexp(m, e)
 
     a = mixed()

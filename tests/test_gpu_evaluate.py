@@ -40,7 +40,7 @@ def test_random_network_f64(ina, gname, chi):
         assert abs(f.evaluate(list(X[p]), [1, 2]) - got[p]) <= 1e-14 * max(1.0, abs(got[p]))
 
 
-@pytest.mark.parametrize("precision", ["f32", "mixed"])
+@pytest.mark.parametrize("precision", ["f32", "mixed_fast", "mixed"])
 def test_random_network_f32_paths(ina, precision):
     graph = O.binary_tree_graph(31)
     rng = np.random.default_rng(5)
@@ -248,8 +248,9 @@ def test_deep_tree_underflow_is_scaled(ina):
 
 @pytest.mark.parametrize("graph_name,chi", [("binary7", 128), ("binary15", 64), ("path6", 128)])
 def test_tensor_core_path(ina, graph_name, chi):
-    """The tcgen05 split-BF16 contraction (chi in {64, 128}; the binary trees'
-    roots use the bilinear mode) against the FP64 path on the same tensors.
+    """The tcgen05 split-BF16 contraction (precision "mixed_fast", chi in
+    {64, 128}; the binary trees' roots use the bilinear mode) against the FP64
+    path on the same tensors.
     Split BF16 x3 leaves ~2^-17 per product; random trees amplify it by their
     depth, so the norm-wise bound is 3e-4."""
     graph = {"binary7": O.binary_tree_graph(7), "binary15": O.binary_tree_graph(15),
@@ -263,7 +264,7 @@ def test_tensor_core_path(ina, graph_name, chi):
     dims = list(range(1, nd + 1))
     ctx = f.ctx
     ctx.kernel_stats(reset=True)
-    m, e = f.evaluate_batch(X, dims, precision="mixed", out="f32_scaled")
+    m, e = f.evaluate_batch(X, dims, precision="mixed_fast", out="f32_scaled")
     st = ctx.kernel_stats(reset=True)
     assert st.get("contract_tc", {}).get("launches", 0) > 0, st
     got = np.ldexp(m, e)
@@ -327,3 +328,35 @@ def test_fused_small_bond_path_matches_per_vertex(ina, monkeypatch, graph_name, 
     if dtype == "f64":  # and the oracle on a few points
         ref = np.array([O.evaluate(net, list(x), dims) for x in X[:20]])
         assert rel_err(fused[:20], ref) < 1e-12
+
+
+@pytest.mark.parametrize("graph_name,chi", [("one_child_pair", 128), ("binary15", 128), ("binary15", 64)])
+def test_output_never_overwrites_inputs(ina, graph_name, chi):
+    """A vertex's output message never shares memory with its children's
+    messages.  Two ways it used to go wrong: the autotuner runs one
+    contraction several times over the same inputs (the first run had
+    overwritten them), and a SIMT tile split over output columns lets one CTA
+    overwrite the rows another CTA of the same points has not read yet (more
+    CTAs than fit at once).  Autotuning is forced here (threshold 0) and the
+    batch spans several waves; the first call must match the oracle and a
+    repeat."""
+    L = ina._lib
+    graph = {"one_child_pair": (list(range(1, 7)), [(1, 2), (2, 3), (2, 4), (3, 5), (4, 6)]),
+             "binary15": O.binary_tree_graph(15)}[graph_name]
+    rng = np.random.default_rng(77 + chi)
+    nd = 2
+    s_or = O.siteinds(graph, map_dimension=nd)
+    net = O.random_net(s_or, chi, rng, normalize=True)
+    ctx = L.Context(0)
+    ctx.set_autotune(True, min_work=0.0, forget=True)
+    s = product_map(ina, graph, net.s)
+    from _helpers import oracle_to_tensors
+    f = ina.ITensorNetworkFunction.from_tensors(s, oracle_to_tensors(net, s), ctx=ctx)
+    X = rng.random((40000, nd))
+    first = f.evaluate_batch(X, [1, 2], precision="f64")
+    again = f.evaluate_batch(X, [1, 2], precision="f64")
+    assert rel_err(first, again) < 1e-13
+    idx = np.linspace(0, len(X) - 1, 96).astype(int)
+    ref = O.evaluate_batch(net, X[idx], [1, 2])
+    assert rel_err(first[idx], ref) < TOL_F64
+    assert np.max(np.abs(first[idx] - ref) / np.abs(ref)) < 1e-9
