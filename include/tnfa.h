@@ -152,6 +152,15 @@ int tnfa_ctx_kernel_stats(tnfa_ctx* ctx, int32_t max, char* names, int64_t* laun
  * reference (it has no device pipelines). */
 int tnfa_ctx_set_wait_budget(tnfa_ctx* ctx, uint32_t polls, int drop_arrive);
 
+/* Fault injection for tests of the error paths.  fail_alloc_after >= 0: the
+ * next fail_alloc_after device allocations of this context succeed and the
+ * one after fails as if the device were out of memory (the call returns
+ * TNFA_ERR_OUT_OF_MEMORY and releases what it held); -1 turns it off.
+ * jacobi_sweep_cap > 0 caps every one-sided Jacobi SVD at that many sweeps,
+ * so that a truncation that needs more returns TNFA_ERR_NOT_CONVERGED; 0
+ * restores the built-in caps.  No counterpart in the reference. */
+int tnfa_ctx_inject_faults(tnfa_ctx* ctx, int64_t fail_alloc_after, int32_t jacobi_sweep_cap);
+
 /* ---- networks ----------------------------------------------------------- */
 
 /* Build a network from the canonical layout.  Replaces the construction of an
@@ -304,6 +313,20 @@ int tnfa_net_convert(tnfa_ctx* ctx, const tnfa_net* f, int dtype, tnfa_net** out
  * ITensorNetworks.contract(O, f; alg="fit", cutoff, maxdim, normalize). */
 int tnfa_apply(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f,
                const tnfa_trunc_params* params, tnfa_net** out);
+/* y = O f contracted exactly site by site, without truncation (every bond
+ * of y is the operator's bond times f's).  The exact part of operate
+ * (src/elementary_operators.jl:294-299) before ITensorNetworks' fit
+ * compresses it; the forward map of tnfa_apply_vjp.  FP64 / complex128. */
+int tnfa_apply_exact(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f, tnfa_net** out);
+/* Vector-Jacobian product of tnfa_apply_exact with respect to f's tensors:
+ * df += J^T dy, i.e. df_v[s_in][..] += sum O_v[(s_out, s_in)][..] dy_v[s_out][..]
+ * with dy in the canonical layout of y = tnfa_apply_exact(op, f) and df in
+ * f's (both n_elements scalars of f's type, host or device memory; complex
+ * networks get the holomorphic derivative, not conjugated).  No reference
+ * counterpart (the reference has no AD); it backs the rrule of operate,
+ * differentiating through the exact contraction (not the truncation). */
+int tnfa_apply_vjp(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f, const void* dy,
+                   int dy_memory, void* df, int df_memory);
 /* Batched form: n independent (op[i], f[i]) pairs of uneven shapes in one
  * scheduled pass. */
 int tnfa_apply_batched(tnfa_ctx* ctx, int32_t n, const tnfa_net* const* ops,

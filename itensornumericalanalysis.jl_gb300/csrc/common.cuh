@@ -160,6 +160,10 @@ struct tnfa_ctx {
   // and a test switch that withholds one arrive so that a wait runs out
   uint32_t tc_wait_limit = 1u << 26;
   int tc_drop_arrive = 0;
+  // fault injection for tests: device allocations left before one fails
+  // (-1: never), and a cap on Jacobi sweeps (0: the built-in caps)
+  int64_t alloc_countdown = -1;
+  int jacobi_sweep_cap = 0;
 };
 
 struct tnfa_net {

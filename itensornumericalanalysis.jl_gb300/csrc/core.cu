@@ -41,6 +41,10 @@ void Topo::validate() const {
 void* dalloc(tnfa_ctx* ctx, size_t bytes) {
   void* p = nullptr;
   if (bytes == 0) return nullptr;
+  if (ctx->alloc_countdown == 0)
+    fail(TNFA_ERR_OUT_OF_MEMORY, "device allocation of " + std::to_string(bytes) +
+                                     " bytes failed: injected failure (tnfa_ctx_inject_faults)");
+  if (ctx->alloc_countdown > 0) --ctx->alloc_countdown;
   cudaError_t e = cudaMallocAsync(&p, bytes, ctx->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -396,6 +400,13 @@ int tnfa_ctx_kernel_stats(tnfa_ctx* ctx, int32_t max, char* names, int64_t* laun
   }
   if (reset) ctx->families.clear();
   TNFA_API_END
+}
+
+int tnfa_ctx_inject_faults(tnfa_ctx* ctx, int64_t fail_alloc_after, int32_t jacobi_sweep_cap) {
+  if (!ctx) return TNFA_ERR_INVALID_ARGUMENT;
+  ctx->alloc_countdown = fail_alloc_after < 0 ? -1 : fail_alloc_after;
+  ctx->jacobi_sweep_cap = jacobi_sweep_cap > 0 ? jacobi_sweep_cap : 0;
+  return TNFA_OK;
 }
 
 int tnfa_ctx_set_wait_budget(tnfa_ctx* ctx, uint32_t polls, int drop_arrive) {

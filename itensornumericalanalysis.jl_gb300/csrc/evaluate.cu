@@ -1121,9 +1121,15 @@ unsigned char* noalloc_base(int device) {
   std::lock_guard<std::mutex> lock(mu);
   if ((int)addr.size() <= device) addr.resize(device + 1, nullptr);
   if (!addr[device]) {
-    TNFA_CUDA(cudaSetDevice(device));
+    // the look-up needs `device` current; the caller's current device is
+    // put back afterwards
+    int prev = -1;
+    TNFA_CUDA(cudaGetDevice(&prev));
+    if (prev != device) TNFA_CUDA(cudaSetDevice(device));
     void* p = nullptr;
-    TNFA_CUDA(cudaGetSymbolAddress(&p, noalloc_scratch));
+    const cudaError_t e = cudaGetSymbolAddress(&p, noalloc_scratch);
+    if (prev != device) TNFA_CUDA(cudaSetDevice(prev));
+    TNFA_CUDA(e);
     addr[device] = (unsigned char*)p;
   }
   return addr[device];

@@ -17,10 +17,12 @@
 // of M = 128 points x N = 256 columns x K per product.  The epilogue folds
 // each group into
 //   out[p, a] += 2^(-8k) sum_b m1[p, b] acc_k[p, (a, b)]
-// with precision matched to the group's weight: FP64 for the leading group
-// k = 2, double-float (FP32 pairs with error-free products and sums) for
-// k = 3..5, plain FP32 into the low word of that pair for k = 6..8.  The contraction is accurate to a few units of
-// 2^-50 of the result's norm (relative), about what an FP64 evaluation gives.
+// in double-float (FP32 pairs: error-free products and sums) for the groups
+// k <= 5 and plain FP32 into the pair's low word for k >= 6 (below 2^-32 of
+// the result), the pair renormalised after every group; each N-tile's pair
+// sums (8 values of b) go to FP64 once.  The
+// contraction is accurate to a few units of 2^-48 of the result's norm
+// (relative), within a small factor of an FP64 evaluation.
 //
 // Shared memory holds six A plane-chunks of 128 points x 64 K (96 KB): all
 // six digit planes when K = 64, three at a time when K = 128 (two phases over
@@ -110,6 +112,14 @@ __device__ __forceinline__ void oz_digits(double xs, int first, float (&d)[PP]) 
 #pragma unroll
     for (int o = 0; o < PP; ++o) d[o] = (i == first + o) ? di : d[o];
   }
+}
+
+// s + e = a + b exactly (Knuth's two-sum, no ordering assumption).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  const float t = __fadd_rn(a, b);
+  const float bp = __fsub_rn(t, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(t, bp)), __fsub_rn(b, bp));
+  s = t;
 }
 
 template <int KCH>
@@ -231,12 +241,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           sh[i] = sl[i] = 0.f;
         }
         for (int bb = 0; bb < nbb && ok; ++bb) {
-          double m1d[8];
           float m1h[8], m1l[8];
 #pragma unroll
           for (int t = 0; t < 8; ++t) {
             const double x = valid ? m1row[bb * OZ_NB + t] * s1 : 0.0;
-            m1d[t] = x;
             m1h[t] = __double2float_rn(x);
             m1l[t] = __double2float_rn(x - (double)m1h[t]);
           }
@@ -249,48 +257,65 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             }
             tc_fence_after();
             const uint32_t col = tmem + lane_base + (uint32_t)(buf * OZ_N + h * 128);
-            if (k == 2) {
-              // one value of a (8 of b) per load keeps few doubles live
+            // double-float fold of the groups k <= 5; the k >= 6 groups (below
+            // 2^-32 of the result) only need FP32 and ride in the low word
+            const float w = __int_as_float((127 - 8 * (k - 2)) << 23);  // 2^(-8(k-2))
+            const bool pair = k <= 5;
 #pragma unroll
-              for (int ai = 0; ai < 16; ++ai) {
-                float v[8];
-                tmem_ld8(col + ai * 8, v);
+            for (int cc = 0; cc < 4; ++cc) {  // 4 values of a x 8 of b per load
+              float v[32];
+              tmem_ld32(col + cc * 32, v);
 #pragma unroll
-                for (int bl = 0; bl < 8; ++bl) acc64[ai] = fma(m1d[bl], (double)v[bl], acc64[ai]);
-              }
-            } else {
-              // double-float fold; the k >= 6 groups (below 2^-32 of the
-              // result) only need FP32 and ride in the low word
-              const float w = __int_as_float((127 - 8 * (k - 2)) << 23);  // 2^(-8(k-2))
-              const bool pair = k <= 5;
-#pragma unroll
-              for (int ai = 0; ai < 16; ++ai) {
-                float v[8];
-                tmem_ld8(col + ai * 8, v);
+              for (int q = 0; q < 4; ++q) {
+                const int ai = cc * 4 + q;
                 if (pair) {
+                  // error-free products, summed pairwise (a tree of depth 3,
+                  // so that the dependency chains stay short), then into the
+                  // pair; every rounding error goes to the low word
+                  float pr[8], lo = 0.f;
 #pragma unroll
                   for (int bl = 0; bl < 8; ++bl) {
-                    const float x = __fmul_rn(v[bl], w);  // exact: a power of two
-                    const float pr = __fmul_rn(m1h[bl], x);
-                    float pe = __fmaf_rn(m1h[bl], x, -pr);
+                    const float x = __fmul_rn(v[q * 8 + bl], w);  // exact: a power of two
+                    pr[bl] = __fmul_rn(m1h[bl], x);
+                    float pe = __fmaf_rn(m1h[bl], x, -pr[bl]);
                     pe = __fmaf_rn(m1l[bl], x, pe);
-                    const float s = __fadd_rn(sh[ai], pr);
-                    const float bp = __fsub_rn(s, sh[ai]);
-                    const float e =
-                        __fadd_rn(__fsub_rn(sh[ai], __fsub_rn(s, bp)), __fsub_rn(pr, bp));
-                    sh[ai] = s;
-                    sl[ai] = __fadd_rn(sl[ai], __fadd_rn(e, pe));
+                    lo = __fadd_rn(lo, pe);
                   }
+#pragma unroll
+                  for (int st = 1; st < 8; st *= 2)
+#pragma unroll
+                    for (int bl = 0; bl < 8; bl += 2 * st) {
+                      float e;
+                      two_sum(pr[bl], pr[bl + st], pr[bl], e);
+                      lo = __fadd_rn(lo, e);
+                    }
+                  float e;
+                  two_sum(sh[ai], pr[0], sh[ai], e);
+                  sl[ai] = __fadd_rn(sl[ai], __fadd_rn(lo, e));
                 } else {
 #pragma unroll
                   for (int bl = 0; bl < 8; ++bl)
-                    sl[ai] = __fmaf_rn(m1h[bl], __fmul_rn(v[bl], w), sl[ai]);
+                    sl[ai] = __fmaf_rn(m1h[bl], __fmul_rn(v[q * 8 + bl], w), sl[ai]);
                 }
               }
             }
             tc_fence_before();
             mbar_arrive(&tempty[buf]);
             ++u;
+            // renormalise each pair (error free) so that the low word starts
+            // the next group small
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              const float t = __fadd_rn(sh[i], sl[i]);
+              sl[i] = __fsub_rn(sl[i], __fsub_rn(t, sh[i]));
+              sh[i] = t;
+            }
+          }
+          // the N-tile's double-float sums (8 values of b) go to FP64 once
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            acc64[i] += (double)sh[i] + (double)sl[i];
+            sh[i] = sl[i] = 0.f;
           }
         }
         if (ok && valid) {
@@ -298,7 +323,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           const int* be = P.bexp + (int64_t)g * P.chi_a + ab * OZ_NA + h * 16;
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
-            double t = acc64[i] + ((double)sh[i] + (double)sl[i]);
+            double t = acc64[i];
             if (ph > 0) t += dst[i];  // phase 0's partial sum of this entry
             if (ph == NPH - 1) t *= ldexp(1.0, be[i] - 16);  // the rows' 2^(E1+E2) goes to the exponent
             dst[i] = t;

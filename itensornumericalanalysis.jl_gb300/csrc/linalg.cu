@@ -695,6 +695,7 @@ template <class T> constexpr int jacobi_maxr() { return sizeof(T) == 16 ? 8 : 16
 template <class T>
 void jacobi(tnfa_ctx* ctx, const std::vector<SvdJob>& jobs, int max_sweeps, JacobiOpts stop_rel,
             const char* family) {
+  if (ctx->jacobi_sweep_cap > 0) max_sweeps = std::min(max_sweeps, ctx->jacobi_sweep_cap);
   std::vector<SvdJob> big, small;
   for (const auto& j : jobs) (svd_big(j, jobs.size(), ctx->sm_count) ? big : small).push_back(j);
   for (int pass = 0; pass < 2; ++pass) {

@@ -306,6 +306,54 @@ __global__ void k_apply_exact(const T* __restrict__ O, const T* __restrict__ F, 
   }
 }
 
+// Adjoint of k_apply_exact with respect to f:
+//   dF[s_in][fi] += sum_{s_out, oi} O[(s_out, s_in)][oi] dY[s_out][(oi, fi)]
+// (the (oi, fi) pairs fused per bond axis, operator index major, as in Y).
+template <class T>
+__global__ void k_apply_vjp(const T* __restrict__ O, const T* __restrict__ dY, T* __restrict__ dF,
+                            const ApplyJob* __restrict__ jobs) {
+  const ApplyJob& jb = jobs[blockIdx.y];
+  int64_t obond = 1, fbond = 1;
+  for (int a = 1; a < jb.nd; ++a) {
+    obond *= jb.dO[a];
+    fbond *= jb.dF[a];
+  }
+  const int sdim = jb.dF[0];
+  const int64_t nf = (int64_t)sdim * fbond;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int s_in = (int)(i / fbond);
+    const int64_t fi = i % fbond;
+    T acc = Sc<T>::zero();
+    for (int s_out = 0; s_out < sdim; ++s_out) {
+      int so = s_out, si = s_in, osite = 0, mul = 1;
+      for (int l = jb.nlegs - 1; l >= 0; --l) {
+        const int b = jb.base[l];
+        const int o = so % b, in = si % b;
+        so /= b;
+        si /= b;
+        osite += (o * b + in) * mul;
+        mul *= b * b;
+      }
+      const T* orow = O + jb.ooff + (int64_t)osite * obond;
+      const T* yrow = dY + jb.yoff + (int64_t)s_out * obond * fbond;
+      for (int64_t oi = 0; oi < obond; ++oi) {
+        // Y bond index per axis: o_a * dF[a] + f_a, row-major over the axes
+        int64_t yi = 0, ro = oi, rf = fi, ym = 1;
+        for (int a = jb.nd - 1; a >= 1; --a) {
+          const int64_t oa = ro % jb.dO[a], fa = rf % jb.dF[a];
+          ro /= jb.dO[a];
+          rf /= jb.dF[a];
+          yi += (oa * jb.dF[a] + fa) * ym;
+          ym *= (int64_t)jb.dO[a] * jb.dF[a];
+        }
+        acc = Sc<T>::fma(orow[oi], yrow[yi], acc);
+      }
+    }
+    dF[jb.foff + i] += acc;
+  }
+}
+
 // O'[s_in][rest] = w * sum_{s_out} O[(s_out, s_in)][rest]: the out legs of an
 // operator contracted with the uniform integration weights.
 struct RowJob {
@@ -355,10 +403,7 @@ void check_same_tree(const Topo& A, const Topo& B, const char* what) {
              std::string(what) + ": operator and function live on different trees");
 }
 
-template <class T>
-Work<T> apply_exact(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f) {
-  const Topo& A = op->topo;
-  const Topo& B = f->topo;
+void check_apply(const Topo& A, const Topo& B) {
   check_same_tree(A, B, "apply");
   for (int l = 0; l < A.leg_off[A.V]; ++l) {
     TNFA_CHECK(A.leg_kind[l] == TNFA_LEG_OPERATOR, TNFA_ERR_INVALID_ARGUMENT,
@@ -368,13 +413,15 @@ Work<T> apply_exact(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f) {
     TNFA_CHECK(A.leg_dim[l] == B.leg_dim[l] * B.leg_dim[l], TNFA_ERR_SHAPE,
                "apply: operator leg dim must be base^2 of the function's");
   }
-  Topo Y = B;
+}
+
+// One job per vertex of y = O f: offsets and axis dimensions of O, f and Y
+// (Y's topology is f's with every bond multiplied by the operator's).
+std::vector<ApplyJob> apply_jobs(const Topo& A, const Topo& B, Topo& Y) {
+  Y = B;
   for (int v = 0; v < B.V; ++v) Y.link[v] = A.link[v] * B.link[v];
   Y.finalize();
   std::vector<ApplyJob> jobs;
-  int64_t nmax = 1;
-  Work<T> w{ctx, Y, {}};
-  DBuf ybuf(ctx, (size_t)Y.n_elem * sizeof(T));
   for (int v = 0; v < B.V; ++v) {
     ApplyJob j{};
     j.ooff = A.off[v];
@@ -394,8 +441,21 @@ Work<T> apply_exact(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f) {
     j.nlegs = B.nlegs[v];
     for (int l = 0; l < j.nlegs; ++l) j.base[l] = B.leg_dim[B.leg_off[v] + l];
     jobs.push_back(j);
-    nmax = std::max(nmax, j.n);
   }
+  return jobs;
+}
+
+template <class T>
+Work<T> apply_exact(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f) {
+  const Topo& A = op->topo;
+  const Topo& B = f->topo;
+  check_apply(A, B);
+  Topo Y;
+  std::vector<ApplyJob> jobs = apply_jobs(A, B, Y);
+  int64_t nmax = 1;
+  for (auto& j : jobs) nmax = std::max(nmax, j.n);
+  Work<T> w{ctx, Y, {}};
+  DBuf ybuf(ctx, (size_t)Y.n_elem * sizeof(T));
   DBuf dj = upload_jobs(ctx, jobs);
   dim3 grid(grid_for(nmax, 256, 4096), B.V);
   {
@@ -413,6 +473,47 @@ Work<T> apply_exact(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f) {
                               cudaMemcpyDeviceToDevice, ctx->stream));
   }
   return w;
+}
+
+// df += J^T dy for y = apply_exact(op, f) (dy in y's canonical layout).
+template <class T>
+void apply_vjp(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f, const void* dy, int dy_mem,
+               void* df, int df_mem) {
+  const Topo& A = op->topo;
+  const Topo& B = f->topo;
+  check_apply(A, B);
+  Topo Y;
+  std::vector<ApplyJob> jobs = apply_jobs(A, B, Y);
+  int64_t nmax = 1;
+  for (int v = 0; v < B.V; ++v) nmax = std::max<int64_t>(nmax, B.size(v));
+  DBuf dyb, dfb;
+  const T* dyd = (const T*)dy;
+  T* dfd = (T*)df;
+  if (dy_mem == TNFA_MEM_HOST) {
+    dyb = DBuf(ctx, (size_t)Y.n_elem * sizeof(T));
+    TNFA_CUDA(cudaMemcpyAsync(dyb.p, dy, (size_t)Y.n_elem * sizeof(T), cudaMemcpyHostToDevice,
+                              ctx->stream));
+    dyd = dyb.as<T>();
+  }
+  if (df_mem == TNFA_MEM_HOST) {
+    dfb = DBuf(ctx, (size_t)B.n_elem * sizeof(T));
+    TNFA_CUDA(cudaMemcpyAsync(dfb.p, df, (size_t)B.n_elem * sizeof(T), cudaMemcpyHostToDevice,
+                              ctx->stream));
+    dfd = dfb.as<T>();
+  }
+  DBuf dj = upload_jobs(ctx, jobs);
+  dim3 grid(grid_for(nmax, 256, 4096), B.V);
+  {
+    double fl = 0;
+    for (auto& j : jobs) fl += 2.0 * j.n * j.dF[0];
+    KernelScope ks(ctx, "apply_vjp", fl, 0.0);
+    k_apply_vjp<T><<<grid, 256, 0, ctx->stream>>>((const T*)op->d, dyd, dfd, dj.as<ApplyJob>());
+    TNFA_LAUNCH_CHECK();
+  }
+  if (df_mem == TNFA_MEM_HOST)
+    TNFA_CUDA(cudaMemcpyAsync(df, dfd, (size_t)B.n_elem * sizeof(T), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 template <class T>
@@ -1692,6 +1793,45 @@ int tnfa_apply(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f,
   check_params(params);
   TNFA_CHECK(out, TNFA_ERR_INVALID_ARGUMENT, "null out");
   *out = apply_truncate(ctx, op, f, *params);
+  TNFA_API_END
+}
+
+int tnfa_apply_exact(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f, tnfa_net** out) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(op, "apply operator");
+  require_net(f, "apply function");
+  TNFA_CHECK(out, TNFA_ERR_INVALID_ARGUMENT, "null out");
+  TNFA_CHECK(op->dtype == f->dtype, TNFA_ERR_DTYPE, "apply: operator and function types differ");
+  if (f->dtype == TNFA_F64) {
+    Work<double> w = apply_exact<double>(ctx, op, f);
+    *out = store_work(w, TNFA_F64);
+  } else if (f->dtype == TNFA_C128) {
+    Work<cplx> w = apply_exact<cplx>(ctx, op, f);
+    *out = store_work(w, TNFA_C128);
+  } else {
+    fail(TNFA_ERR_DTYPE, "apply: FP64 or complex128 networks");
+  }
+  TNFA_API_END
+}
+
+int tnfa_apply_vjp(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f, const void* dy,
+                   int dy_memory, void* df, int df_memory) {
+  TNFA_API_BEGIN(ctx);
+  require_ctx(ctx);
+  require_net(op, "apply_vjp operator");
+  require_net(f, "apply_vjp function");
+  TNFA_CHECK(dy && df, TNFA_ERR_INVALID_ARGUMENT, "null dy or df");
+  TNFA_CHECK((dy_memory == TNFA_MEM_HOST || dy_memory == TNFA_MEM_DEVICE) &&
+                 (df_memory == TNFA_MEM_HOST || df_memory == TNFA_MEM_DEVICE),
+             TNFA_ERR_INVALID_ARGUMENT, "bad memory kind");
+  TNFA_CHECK(op->dtype == f->dtype, TNFA_ERR_DTYPE, "apply_vjp: operator and function types differ");
+  if (f->dtype == TNFA_F64)
+    apply_vjp<double>(ctx, op, f, dy, dy_memory, df, df_memory);
+  else if (f->dtype == TNFA_C128)
+    apply_vjp<cplx>(ctx, op, f, dy, dy_memory, df, df_memory);
+  else
+    fail(TNFA_ERR_DTYPE, "apply_vjp: FP64 or complex128 networks");
   TNFA_API_END
 }
 

@@ -75,8 +75,10 @@ from .indexmap import (
     indexmap,
     indexmaptype,
     indsnetwork,
+    merge_to_tree_image,
     real_continuous_siteinds,
     reduced_indsnetworkmap,
+    tree_groups,
     vertex_digit,
     vertex_dimension,
     vertices_digits,

@@ -119,6 +119,7 @@ SIGNATURES = {
     "tnfa_ctx_destroy": (C.c_int, [_P]),
     "tnfa_ctx_synchronize": (C.c_int, [_P]),
     "tnfa_ctx_set_wait_budget": (C.c_int, [_P, C.c_uint32, C.c_int]),
+    "tnfa_ctx_inject_faults": (C.c_int, [_P, C.c_int64, C.c_int32]),
     "tnfa_last_error_string": (C.c_char_p, [_P]),
     "tnfa_ctx_set_timing": (C.c_int, [_P, C.c_int]),
     "tnfa_ctx_set_autotune": (C.c_int, [_P, C.c_int, C.c_double, C.c_int]),
@@ -163,6 +164,8 @@ SIGNATURES = {
     "tnfa_operator_proj": (C.c_int, [_P, _P, _PP]),
     "tnfa_apply": (C.c_int, [_P, _P, _P, C.POINTER(TruncParams), _PP]),
     "tnfa_apply_batched": (C.c_int, [_P, _I32, _PP, _PP, C.POINTER(TruncParams), _PP]),
+    "tnfa_apply_exact": (C.c_int, [_P, _P, _P, _PP]),
+    "tnfa_apply_vjp": (C.c_int, [_P, _P, _P, _P, C.c_int, _P, C.c_int]),
     "tnfa_truncate": (C.c_int, [_P, _P, C.POINTER(TruncParams), _PP]),
     "tnfa_truncate_batched": (C.c_int, [_P, _I32, _PP, C.POINTER(TruncParams), _PP]),
     "tnfa_inner": (C.c_int, [_P, _P, _P, _PD]),
@@ -260,6 +263,12 @@ class Context:
         pipeline wait gives up (0 keeps the budget), and the test switch that
         withholds one arrive so that a wait runs out."""
         self.check(self.lib.tnfa_ctx_set_wait_budget(self.handle, int(polls), int(drop_arrive)))
+
+    def inject_faults(self, fail_alloc_after: int = -1, jacobi_sweep_cap: int = 0) -> None:
+        """tnfa_ctx_inject_faults: fail the device allocation after the next
+        `fail_alloc_after` ones (-1: never); cap Jacobi sweeps (0: off)."""
+        self.check(self.lib.tnfa_ctx_inject_faults(self.handle, int(fail_alloc_after),
+                                                   int(jacobi_sweep_cap)))
 
     def synchronize(self) -> None:
         self.call("tnfa_ctx_synchronize")

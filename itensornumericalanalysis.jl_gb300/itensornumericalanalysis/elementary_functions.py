@@ -31,6 +31,18 @@ default_nterms = 20
 default_dim = 1
 
 
+def _on_tree_image(fn):
+    """Build on the map's tree image: on a graph with cycles the function is
+    represented on a tree of vertex groups (IndsNetworkMap.tree_image)."""
+    import functools
+
+    @functools.wraps(fn)
+    def wrapped(s, *args, **kw):
+        return fn(s.tree_image, *args, **kw)
+
+    return wrapped
+
+
 def _is_real(*xs) -> bool:
     return all(np.isreal(x) for x in xs)
 
@@ -64,6 +76,7 @@ def _product_network(s: IndsNetworkMap, site_tensors: dict) -> ITensorNetworkFun
     return ITensorNetworkFunction.from_tensors(s, ts)
 
 
+@_on_tree_image
 def const_itensornetwork(s: IndsNetworkMap, c=default_c_value, linkdim: int = 1):
     """f = c with every bond of dimension `linkdim` (src/elementary_functions.jl:16-26):
     each tensor is c' * delta(bonds) (x) ones(sites), c'^nv * linkdim = c."""
@@ -94,6 +107,7 @@ def const_itensornetwork(s: IndsNetworkMap, c=default_c_value, linkdim: int = 1)
     return ITensorNetworkFunction.from_tensors(s, ts)
 
 
+@_on_tree_image
 def exp_itensornetwork(s: IndsNetworkMap, k=default_k_value, a=default_a_value,
                        c=default_c_value, dim: int = default_dim):
     """exp(k x_dim + a) * c as a bond-1 product network (src/elementary_functions.jl:30-53)."""
@@ -119,16 +133,19 @@ def exp_itensornetwork(s: IndsNetworkMap, k=default_k_value, a=default_a_value,
     return _product_network(s, site)
 
 
+@_on_tree_image
 def cosh_itensornetwork(s, k=default_k_value, a=default_a_value, c=default_c_value, dim=default_dim):
     """cosh(kx+a)*c, bond 2 (src/elementary_functions.jl:57-68)."""
     return exp_itensornetwork(s, k, a, 0.5 * c, dim) + exp_itensornetwork(s, -k, -a, 0.5 * c, dim)
 
 
+@_on_tree_image
 def sinh_itensornetwork(s, k=default_k_value, a=default_a_value, c=default_c_value, dim=default_dim):
     """sinh(kx+a)*c, bond 2 (src/elementary_functions.jl:72-83)."""
     return exp_itensornetwork(s, k, a, 0.5 * c, dim) + exp_itensornetwork(s, -k, -a, -0.5 * c, dim)
 
 
+@_on_tree_image
 def tanh_itensornetwork(s, k=default_k_value, a=default_a_value, c=default_c_value,
                         nterms: int = default_nterms, dim=default_dim):
     """tanh(kx+a)*c ~ 1 + 2 sum_n (-1)^n exp(-2n(kx+a)), bond 1+nterms
@@ -179,6 +196,7 @@ def _rotation_network(s: IndsNetworkMap, k: float, a: float, c: float, dim: int,
     return ITensorNetworkFunction.from_tensors(s, ts)
 
 
+@_on_tree_image
 def cos_itensornetwork(s, k=default_k_value, a=default_a_value, c=default_c_value, dim=default_dim):
     """cos(kx+a)*c, bond 2 (src/elementary_functions.jl:109-120)."""
     if _is_real(k, a, c) and not s.is_complex and s.is_tree():
@@ -187,6 +205,7 @@ def cos_itensornetwork(s, k=default_k_value, a=default_a_value, c=default_c_valu
             + exp_itensornetwork(s, -1j * k, -1j * a, 0.5 * c, dim))
 
 
+@_on_tree_image
 def sin_itensornetwork(s, k=default_k_value, a=default_a_value, c=default_c_value, dim=default_dim):
     """sin(kx+a)*c, bond 2 (src/elementary_functions.jl:124-135)."""
     if _is_real(k, a, c) and not s.is_complex and s.is_tree():
@@ -212,6 +231,7 @@ def _coeff(N: int, alpha: Sequence[int], beta: int) -> int:
     return out
 
 
+@_on_tree_image
 def polynomial_itensornetwork(s: IndsNetworkMap, coeffs: Sequence, dim: int = default_dim,
                               k=default_k_value, c=default_c_value):
     """sum_i coeffs[i] (k x)^i * c as a bond-n tree network (Q_N tensors on the
@@ -272,6 +292,7 @@ def polynomial_itensornetwork(s: IndsNetworkMap, coeffs: Sequence, dim: int = de
     return ITensorNetworkFunction.from_tensors(s, ts)
 
 
+@_on_tree_image
 def random_itensornetwork(s: IndsNetworkMap, link_space: int = 1, rng=None, dtype=float,
                           normalize: bool = False):
     """Gaussian random tensors with bonds of dimension link_space
@@ -290,6 +311,7 @@ def random_itensornetwork(s: IndsNetworkMap, link_space: int = 1, rng=None, dtyp
     return ITensorNetworkFunction.from_tensors(s, ts)
 
 
+@_on_tree_image
 def delta_p(s: IndsNetworkMap, xs, dims=None):
     """Product state that is 1 on the digits of xs (a plane if some dims are
     left out); a list of points gives their sum (src/elementary_functions.jl:224-261)."""
@@ -356,6 +378,7 @@ def _delta_overlaps(points, points_dims):
     return over_p, over_d
 
 
+@_on_tree_image
 def delta_kernel(s: IndsNetworkMap, points, points_dims=None, remove_overlap: bool = True,
                  coeff=-1.0, include_identity: bool = True):
     """const + coeff * sum of delta_p over points, minus the double-counted

@@ -89,6 +89,66 @@ class TreeLayout:
         return ([self.parent[i]] if self.parent[i] >= 0 else []) + self.children[i]
 
 
+def _quotient_is_forest(g: NamedGraph, groups: list[list]) -> tuple[bool, int]:
+    """Whether the groups' quotient graph is a forest, and the most edges
+    that cross between any two groups."""
+    gid = {v: k for k, gr in enumerate(groups) for v in gr}
+    cross: dict = {}
+    for u, w in g.edges():
+        a, b = gid[u], gid[w]
+        if a != b:
+            key = (min(a, b), max(a, b))
+            cross[key] = cross.get(key, 0) + 1
+    q = NamedGraph(range(len(groups)), cross.keys())
+    return q.is_forest(), max(cross.values(), default=0)
+
+
+def tree_groups(g: NamedGraph) -> list[list]:
+    """Vertex groups of a graph whose quotient graph is a forest (each group in
+    graph vertex order, groups ordered by their first vertex).  Candidates:
+    for grid-like names (tuples of one length) the slices of constant
+    coordinate k and the lines along coordinate k; always the breadth-first
+    layers from the first vertex.  The forest candidate crossed by the fewest
+    edges between two groups wins (then the one with the smallest groups)."""
+    verts = g.vertices()
+    pos = {v: i for i, v in enumerate(verts)}
+    cands = []
+    if verts and all(isinstance(v, tuple) for v in verts) and len({len(v) for v in verts}) == 1:
+        for k in range(len(verts[0])):
+            for key in (lambda v, k=k: v[k], lambda v, k=k: v[:k] + v[k + 1:]):
+                grp: dict = {}
+                for v in verts:
+                    grp.setdefault(key(v), []).append(v)
+                cands.append(list(grp.values()))
+    layers, seen = [], set()
+    for r in verts:  # breadth-first layers per component
+        if r in seen:
+            continue
+        frontier = [r]
+        seen.add(r)
+        while frontier:
+            layers.append(frontier)
+            nxt = []
+            for v in frontier:
+                for w in g.neighbors(v):
+                    if w not in seen:
+                        seen.add(w)
+                        nxt.append(w)
+            frontier = nxt
+    cands.append(layers)
+    best = None
+    for groups in cands:
+        groups = [sorted(gr, key=pos.get) for gr in groups]
+        groups.sort(key=lambda gr: pos[gr[0]])
+        ok, cross = _quotient_is_forest(g, groups)
+        if not ok:
+            continue
+        score = (cross, max(len(gr) for gr in groups))
+        if best is None or score < best[0]:
+            best = (score, groups)
+    return best[1]
+
+
 class IndsNetworkMap:
     """A graph whose vertices carry digit legs, plus the digit -> coordinate map."""
 
@@ -101,6 +161,32 @@ class IndsNetworkMap:
     @cached_property
     def layout(self) -> TreeLayout:
         return TreeLayout(self.graph)
+
+    @cached_property
+    def tree_image(self) -> "IndsNetworkMap":
+        """The map itself on a forest.  On a graph with cycles (e.g.
+        named_grid((3, 3)), which the reference evaluates with
+        scalar(alg="bp"/"exact")) the map of a tree of vertex groups: grid
+        rows or columns (the grouping whose tree is crossed by the fewest
+        edges), else breadth-first layers.  A group carries its members' legs
+        in member order; a bond between two groups stands for all the edges
+        between them.  Functions on this map are represented exactly on the
+        image (merge_to_tree_image for given tensors); the constructors build
+        directly on it, where sums keep the bonds of a tree."""
+        if self.graph.is_forest():
+            return self
+        groups = tree_groups(self.graph)
+        names = [tuple(gr) for gr in groups]
+        gid = {v: n for n, gr in zip(names, groups) for v in gr}
+        q = NamedGraph(names)
+        for u, w in self.graph.edges():
+            if gid[u] != gid[w]:
+                q.add_edge(gid[u], gid[w])
+        legs = {n: [l for v in gr for l in self.legs[v]] for n, gr in zip(names, groups)}
+        img = IndsNetworkMap(q, legs, self.is_complex)
+        img.merged_from = self
+        img.groups = dict(zip(names, groups))
+        return img
 
     def vertices(self) -> list:
         return self.graph.vertices()
@@ -264,6 +350,65 @@ class IndsNetworkMap:
 
     def __repr__(self) -> str:
         return f"IndsNetworkMap(nv={self.nv()}, dims={self.dimensions()}, complex={self.is_complex})"
+
+
+def merge_to_tree_image(s: IndsNetworkMap, tensors: dict) -> dict:
+    """Exact tensors of a function on s.tree_image, from per-vertex tensors on
+    the graph of s with axes [site legs..., bonds to the neighbours in graph
+    neighbour order]: the tensors of each group contracted over the group's
+    inner edges; the edges from one group to another (in graph edge order)
+    fused into one bond.  The result is in the image's canonical layout
+    [site legs..., parent bond, child bonds...]."""
+    img = s.tree_image
+    if img is s:
+        raise ValueError("the map's graph is a forest: give canonical-layout tensors")
+    g = s.graph
+    edges = g.edges()
+    eid = {}
+    for k, (u, w) in enumerate(edges):
+        eid[(u, w)] = eid[(w, u)] = k
+    gid = {v: n for n, gr in img.groups.items() for v in gr}
+    lay = img.layout
+    out = {}
+    for i, name in enumerate(lay.order):
+        members = img.groups[name]
+        ops, nsym = [], len(edges)
+        site_syms = []
+        for v in members:
+            t = np.asarray(tensors[v])
+            nl = len(s.legs[v])
+            sub = list(range(nsym, nsym + nl))
+            nsym += nl
+            site_syms += sub
+            sub += [eid[(v, w)] for w in g.neighbors(v)]
+            if t.ndim != len(sub):
+                raise ValueError(f"tensor of vertex {v!r} has {t.ndim} axes, expected {len(sub)}")
+            ops += [t, sub]
+        out_syms, bond_dims = list(site_syms), []
+        for j in lay.neighbours_in_layout_order(i):
+            other = lay.order[j]
+            es = sorted(k for k, (u, w) in enumerate(edges)
+                        if {gid[u], gid[w]} == {name, other})
+            out_syms += es
+            bond_dims.append(es)
+        # compact labels (einsum takes at most 52 distinct ones per call)
+        relabel: dict = {}
+        for k in range(1, len(ops), 2):
+            ops[k] = [relabel.setdefault(x, len(relabel)) for x in ops[k]]
+        out_lab = [relabel[x] for x in out_syms]
+        arr = np.einsum(*ops, out_lab, optimize=True)
+        site_shape = arr.shape[: len(site_syms)]
+        shape, ax = list(site_shape), len(site_syms)
+        for es in bond_dims:
+            d = 1
+            for _ in es:
+                d *= arr.shape[ax]
+                ax += 1
+            shape.append(d)
+        if lay.parent[i] < 0:  # a root's parent bond of dimension 1
+            shape.insert(len(site_shape), 1)
+        out[name] = arr.reshape(shape)
+    return out
 
 
 def digit_siteinds(g: NamedGraph, dimension_vertices=None, base: int = 2, map_dimension: int = 1):

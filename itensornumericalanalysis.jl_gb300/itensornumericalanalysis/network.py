@@ -49,8 +49,16 @@ class ITensorNetworkFunction:
     @classmethod
     def from_tensors(cls, s: IndsNetworkMap, tensors: dict, ctx=None, legs=None, dtype=None):
         """Upload per-vertex tensors given in canonical layout
-        [site legs..., parent bond, child bonds...] (keys are vertex names)."""
+        [site legs..., parent bond, child bonds...] (keys are vertex names).
+        On a map whose graph has cycles the tensors have axes [site legs...,
+        bonds to the neighbours in graph neighbour order]; the function is
+        then held exactly on the map's tree image (merge_to_tree_image)."""
         ctx = ctx or _lib.default_context()
+        if not s.graph.is_forest():
+            from .indexmap import merge_to_tree_image
+
+            return cls.from_tensors(s.tree_image, merge_to_tree_image(s, tensors), ctx=ctx,
+                                    dtype=dtype)
         lay = s.layout
         arrs = [np.asarray(tensors[v]) for v in lay.order]
         is_c = any(np.iscomplexobj(a) for a in arrs)

@@ -44,3 +44,14 @@ def rel_err(a, b) -> float:
     a = np.asarray(a)
     b = np.asarray(b)
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def oracle_to_graph_tensors(net: O.Net, s_prod) -> dict:
+    """Per-vertex arrays [site..., bonds to the neighbours in the product
+    graph's neighbour order] (the input form for graphs with cycles)."""
+    g = s_prod.graph
+    out = {}
+    for v in g.vertices():
+        links = [net.link[frozenset((v, w))] for w in g.neighbors(v)]
+        out[v] = net.T[v].permute(net.s.site[v] + links).arr
+    return out

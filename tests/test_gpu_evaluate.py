@@ -117,8 +117,9 @@ def test_poly_matches_oracle_tensors_values(ina):
 
 
 def test_const_and_sums(ina):
-    """test/test_realitensorfunction.jl:147-189."""
-    s = ina.continuous_siteinds(ina.named_comb_tree((3, 3)), map_dimension=3)
+    """test/test_realitensorfunction.jl:147-189, on the reference's
+    named_grid((3, 3)) (a graph with cycles)."""
+    s = ina.continuous_siteinds(ina.named_grid((3, 3)), map_dimension=3)
     assert abs(ina.const_itn(s, c=1.5).evaluate([0.5, 0.25, 0.0], [1, 2, 3]) - 1.5) < 1e-14
     assert abs(ina.const_itn(s, c=-2.0, linkdim=4).evaluate([0.5, 0.25, 0.0], [1, 2, 3]) + 2.0) < 1e-13
     s = ina.continuous_siteinds(ina.named_grid((10, 1)), map_dimension=2)

@@ -75,6 +75,49 @@ def test_noalloc_matches_evaluate_twice(ina, dtype):
             assert np.max(np.abs(va - vb) / np.abs(vb)) <= TOL_F32
 
 
+@pytest.mark.parametrize("case", ["fused_f64", "fused_f32", "complex"])
+def test_noalloc_other_branches_twice(ina, case):
+    """The small-bond branch (every bond <= 8: the whole tree per thread in
+    one launch, only the digit program and its schedule in the array) in FP64
+    and FP32, and a complex network (complex128 messages, (re, im) output),
+    each against tnfa_evaluate on two calls in a row."""
+    import torch
+
+    L = ina._lib
+    rng = np.random.default_rng(42)
+    if case == "complex":
+        graph = O.binary_tree_graph(15)
+        s_or = O.siteinds(graph, map_dimension=3)
+        net = O.random_net(s_or, 12, rng, normalize=True)
+        f, _ = upload_oracle(ina, graph, net)
+        f = f.astype(L.C128)
+        f.scale_vertex(f.s.layout.order[0], 0.6 - 0.8j)
+        nd, prec, kind = 3, L.PREC_F64, L.OUT_C128
+    else:
+        graph = O.path_graph(12)
+        s_or = O.siteinds(graph)
+        net = O.random_net(s_or, 6, rng, normalize=True)
+        f, _ = upload_oracle(ina, graph, net, dtype=L.F64 if case == "fused_f64" else L.F32)
+        nd = 1
+        prec = L.PREC_F64 if case == "fused_f64" else L.PREC_F32
+        kind = L.OUT_F64
+    dims = list(range(1, nd + 1))
+    for call in range(2):
+        X = rng.random((2500 + 301 * call, nd))
+        Xd = _device(X, torch.float64)
+        n = len(X)
+        odt = torch.complex128 if case == "complex" else torch.float64
+        if case != "complex":
+            f.ctx.kernel_stats(reset=True)
+        a = _evaluate(ina, f, Xd, n, dims, torch.empty(n, dtype=odt, device="cuda"), kind, prec, True)
+        if case != "complex":
+            st = f.ctx.kernel_stats(reset=True)
+            assert st.get("eval_fused", {}).get("launches", 0) >= 1, st
+        b = _evaluate(ina, f, Xd, n, dims, torch.empty(n, dtype=odt, device="cuda"), kind, prec, False)
+        tol = TOL_F32 if case == "fused_f32" else TOL_F64
+        assert np.max(np.abs(a - b)) <= tol * np.max(np.abs(b))
+
+
 def test_noalloc_rejects_oversize_requests(ina):
     import torch
 
