@@ -18,8 +18,8 @@
 // each group into
 //   out[p, a] += 2^(-8k) sum_b m1[p, b] acc_k[p, (a, b)]
 // in double-float (FP32 pairs: error-free products and sums) for the groups
-// k <= 5 and plain FP32 into the pair's low word for k >= 6 (below 2^-32 of
-// the result), the pair renormalised after every group; each N-tile's pair
+// k <= 4 and plain FP32 into the pair's low word for k >= 5 (at most 2^-24
+// of the result), the pair renormalised after every group; each N-tile's pair
 // sums (8 values of b) go to FP64 once.  The
 // contraction is accurate to a few units of 2^-48 of the result's norm
 // (relative), within a small factor of an FP64 evaluation.
@@ -257,10 +257,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             }
             tc_fence_after();
             const uint32_t col = tmem + lane_base + (uint32_t)(buf * OZ_N + h * 128);
-            // double-float fold of the groups k <= 5; the k >= 6 groups (below
-            // 2^-32 of the result) only need FP32 and ride in the low word
+            // double-float fold of the groups k <= 4; the k >= 5 groups (at most
+            // 2^-24 of the result) only need FP32 and ride in the low word
             const float w = __int_as_float((127 - 8 * (k - 2)) << 23);  // 2^(-8(k-2))
-            const bool pair = k <= 5;
+            const bool pair = k <= 4;
+            float mw[8];  // m1 high words times the group's weight (exact)
+#pragma unroll
+            for (int t = 0; t < 8; ++t) mw[t] = __fmul_rn(m1h[t], w);
 #pragma unroll
             for (int cc = 0; cc < 4; ++cc) {  // 4 values of a x 8 of b per load
               float v[32];
@@ -294,8 +297,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                   sl[ai] = __fadd_rn(sl[ai], __fadd_rn(lo, e));
                 } else {
 #pragma unroll
-                  for (int bl = 0; bl < 8; ++bl)
-                    sl[ai] = __fmaf_rn(m1h[bl], __fmul_rn(v[q * 8 + bl], w), sl[ai]);
+                  for (int bl = 0; bl < 8; ++bl) sl[ai] = __fmaf_rn(mw[bl], v[q * 8 + bl], sl[ai]);
                 }
               }
             }

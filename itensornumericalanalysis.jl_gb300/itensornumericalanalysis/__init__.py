@@ -87,7 +87,7 @@ from .indexmap import (
 from .grad import TTNEvaluate, evaluate_vjp
 from .integration import integrate, partial_integrate
 from .network import ITensorNetworkFunction, calculate_fx, evaluate, inner, itensornetwork
-from .operate import operate, operate_batched
+from .operate import operate, operate_batched, operate_exact, operate_vjp
 from .solvers import dmrg, linsolve
 from .tci import interpolate
 from .truncation import truncate, truncate_batched

@@ -107,3 +107,117 @@ def test_fit_decreases_loss(ina):
         losses.append(float(loss.detach()))
     assert losses[-1] < 0.6 * losses[0], losses[::10]
     assert all(np.isfinite(losses))
+
+
+def test_config4_shape_fd_and_oracle(ina):
+    """Config 4 at its stated shape: comb 2 x 12 (a 24-site path), chi 32,
+    FP32 tensors N(0, 0.1^2) (seed 2), MSE loss against
+    sin(3x) cos(5y) exp(-(x^2 + y^2)) at 2^20 points.  The FP32 backward
+    kernels' gradient against central differences (h = 1e-3; the loss is
+    quadratic in each entry, so central differences of an FP64 evaluation of
+    the same FP32 tensors are exact up to rounding) on sampled entries, and
+    against the oracle's gradient on a 48-point subset."""
+    L, chi = 12, 32
+    g = ina.named_comb_tree((2, L))
+    s = ina.continuous_siteinds(g, [[(1, j) for j in range(1, L + 1)], [(2, j) for j in range(1, L + 1)]])
+    rng = np.random.default_rng(2)
+    lay = s.layout
+    ts = {}
+    for i, v in enumerate(lay.order):
+        shape = (2, chi if lay.parent[i] >= 0 else 1) + (chi,) * len(lay.children[i])
+        ts[v] = (0.1 * rng.standard_normal(shape)).astype(np.float32)
+    f32 = ina.ITensorNetworkFunction.from_tensors(s, ts, dtype=ina._lib.F32)
+    P = 1 << 20
+    X = rng.random((P, 2))
+    x, y = X[:, 0], X[:, 1]
+    target = np.sin(3 * x) * np.cos(5 * y) * np.exp(-(x**2 + y**2))
+    pred = f32.evaluate_batch(X, [1, 2], precision="f32", out="f64")
+    dout = 2.0 * (pred - target) / P  # d MSE / d pred
+    grad = ina.evaluate_vjp(f32, X, dout, [1, 2])
+    t64 = {v: a.astype(np.float64) for v, a in ts.items()}
+
+    def loss(tens):
+        fx = ina.ITensorNetworkFunction.from_tensors(s, tens).evaluate_batch(X, [1, 2])
+        return np.mean((fx - target) ** 2)
+
+    h = 1e-3
+    gscale = max(np.max(np.abs(a)) for a in grad.values())
+    for _ in range(6):
+        v = lay.order[rng.integers(len(lay.order))]
+        idx = tuple(rng.integers(d) for d in ts[v].shape)
+        tp = dict(t64)
+        tm = dict(t64)
+        tp[v] = t64[v].copy()
+        tm[v] = t64[v].copy()
+        tp[v][idx] += h
+        tm[v][idx] -= h
+        fd = (loss(tp) - loss(tm)) / (2 * h)
+        assert abs(fd - float(grad[v][idx])) <= 1e-3 * gscale + 1e-3 * abs(fd), (v, idx, fd, grad[v][idx])
+    # the oracle's gradient of sum_p dout_p f(x_p) on a subset of points
+    sub = rng.choice(P, 48, replace=False)
+    gsub = ina.evaluate_vjp(f32.astype(ina._lib.F64), X[sub], dout[sub], [1, 2])
+    so = O.siteinds(O.comb_tree_graph((2, L)), [[(1, j) for j in range(1, L + 1)],
+                                                 [(2, j) for j in range(1, L + 1)]])
+    from _helpers import product_map  # noqa: F401
+    net = O.Net(so, {}, {frozenset(e): O.Index(chi, "L") for e in so.edges})
+    for i, v in enumerate(lay.order):
+        nb = lay.neighbours_in_layout_order(i)
+        arr = t64[v] if lay.parent[i] >= 0 else t64[v][:, 0]
+        inds = so.site[v] + [net.link[frozenset((v, lay.order[j]))] for j in nb]
+        net.T[v] = O.Tensor(arr, inds)
+    ref = _grad_to_layout(net, O.gradient(net, X[sub], [1, 2], dout[sub]), s)
+    sc = max(np.max(np.abs(r)) for r in ref.values())
+    for v in lay.order:
+        assert np.max(np.abs(gsub[v] - ref[v])) <= 1e-10 * sc, v
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_operate_vjp(ina, cplx):
+    """The adjoint of the exact operator contraction: for
+    l(f) = sum_p w_p (O f)(x_p), df = operate_vjp(O, f, evaluate_vjp(O f, ...)).
+    l is multilinear in the V site tensors (degree one in each entry), so
+    <df, f> = V l(f) (Euler), central differences are exact on single entries,
+    and a small step along a random direction matches <df, d>."""
+    L = 8
+    s = ina.continuous_siteinds(ina.named_grid((L, 1)))
+    f = ina.rand_itn(s, link_space=3, rng=70)
+    if cplx:
+        f = f.astype(ina._lib.C128)
+        f.scale_vertex(s.layout.order[2], 0.3 + 0.7j)
+    op = ina.second_derivative_operator(s)
+    if cplx:
+        op = op.astype(ina._lib.C128)
+    rng = np.random.default_rng(71)
+    X = rng.random(200)
+    w = rng.standard_normal(200)
+    y = ina.operate_exact(op, f)
+    dyv = ina.evaluate_vjp(y, X, w, [1])
+    dy = np.concatenate([dyv[v].ravel() for v in s.layout.order])
+    df = ina.operate_vjp(op, f, dy)
+    ts = f.tensors()
+    flat = np.concatenate([ts[v].ravel() for v in s.layout.order])
+
+    def unflat(a):
+        out, off = {}, 0
+        for v in s.layout.order:
+            n = ts[v].size
+            out[v] = a[off:off + n].reshape(ts[v].shape)
+            off += n
+        return out
+
+    def loss(a):
+        g = ina.ITensorNetworkFunction.from_tensors(s, unflat(a))
+        return np.dot(w, ina.operate_exact(op, g).evaluate_batch(X, [1]))
+
+    l0 = loss(flat)
+    assert abs(L * l0 - np.dot(df, flat)) <= 1e-10 * max(1.0, abs(L * l0))
+    d = rng.standard_normal(flat.shape) * (1 + (1j if cplx else 0))
+    eps = 1e-5
+    dd = (loss(flat + eps * d) - loss(flat - eps * d)) / (2 * eps)
+    assert abs(dd - np.dot(df, d)) <= 1e-6 * max(1.0, abs(np.dot(df, d)))
+    h = 1e-3
+    for k in rng.choice(len(flat), 5, replace=False):
+        e = np.zeros_like(flat)
+        e[k] = h
+        fd = (loss(flat + e) - loss(flat - e)) / (2 * h)
+        assert abs(fd - df[k]) <= 1e-8 * max(1.0, abs(fd))
