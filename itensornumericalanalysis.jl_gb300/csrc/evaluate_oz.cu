@@ -89,14 +89,40 @@ struct OzParams {
   int drop_arrive;      // nonzero: the A-ready arrive of phase 0 is withheld (timeout test)
 };
 
-// The PP digits first+1 .. first+PP (1-based) of xs, |xs| < 1:
-// xs = sum_i d_i 2^(-8i) + O(2^-49).  xs is split into an FP32 pair (48
-// bits); each digit is the rounded leading part of the pair times 256, taken
-// off exactly, and the pair is renormalised by an error-free sum.
+// x 2^-E as an FP32 pair hi + lo: hi is x 2^-E with its significand cut to
+// 24 bits, lo the remaining 29 bits rounded to 24 (48 bits in all), built
+// from the FP64 bit pattern with integer and FP32 operations only (GB300
+// runs FP64 arithmetic and FP64 conversions at 1/64 of the FP32 rate).
+// Results below 2^-126 (far below the row maximum 2^E) flush to zero.
+__device__ __forceinline__ void split_f64(double x, int E, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned w1 = (unsigned)(b >> 32), w0 = (unsigned)b;
+  const int be = (int)((w1 >> 20) & 0x7FF);
+  const int e = be - 1023 - E;  // exponent of x 2^-E
+  if (be == 0 || e < -126 || e > 127) {
+    hi = lo = 0.f;
+    return;
+  }
+  const unsigned sign = w1 & 0x80000000u;
+  hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | ((w1 & 0xFFFFFu) << 3) | (w0 >> 29));
+  const unsigned rem = w0 & 0x1FFFFFFFu;  // weight 2^(e - 52)
+  if (rem == 0 || e - 52 < -126) {
+    lo = 0.f;
+    return;
+  }
+  // float(rem) by the 2^23 bias trick on its two parts, one rounding
+  const float rl = __fsub_rn(__uint_as_float(0x4B000000u | (rem & 0x7FFFFFu)), 8388608.f);
+  const float rh = __fsub_rn(__uint_as_float(0x4B000000u | (rem >> 23)), 8388608.f);
+  const float r = __fmaf_rn(rh, 8388608.f, rl);
+  lo = __uint_as_float(__float_as_uint(__fmul_rn(r, __uint_as_float((unsigned)(e - 52 + 127) << 23))) | sign);
+}
+
+// The PP digits first+1 .. first+PP (1-based) of xs = r + l, |xs| < 1 (an
+// FP32 pair, 48 bits): xs = sum_i d_i 2^(-8i) + O(2^-48).  Each digit is the
+// rounded leading part of the pair times 256, taken off exactly, and the
+// pair is renormalised by an error-free sum.
 template <int PP>
-__device__ __forceinline__ void oz_digits(double xs, int first, float (&d)[PP]) {
-  float r = __double2float_rn(xs);
-  float l = __double2float_rn(xs - (double)r);
+__device__ __forceinline__ void oz_digits(float r, float l, int first, float (&d)[PP]) {
 #pragma unroll
   for (int o = 0; o < PP; ++o) d[o] = 0.f;
 #pragma unroll
@@ -201,7 +227,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (E1 == INT_MIN) E1 = 0;
     if (E2 == INT_MIN) E2 = 0;
     asm volatile("bar.sync 1, 256;" ::: "memory");  // every row read before A overwrites
-    const double s1 = ldexp(1.0, -E1), s2 = ldexp(1.0, -E2);
     const int e_in = valid ? ((P.m1_exp ? P.m1_exp[p] : 0) + (P.m2_exp ? P.m2_exp[p] : 0)) : 0;
     const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
     bool ok = true;
@@ -219,9 +244,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
           for (int t = 0; t < 8; t += 2) {
             const int c = kc * OZ_KC + 32 * h + q * 8 + t;
-            float d0[PP], d1[PP];
-            oz_digits<PP>(valid ? m2row[c] * s2 : 0.0, ph * PP, d0);
-            oz_digits<PP>(valid ? m2row[c + 1] * s2 : 0.0, ph * PP, d1);
+            float d0[PP], d1[PP], r0 = 0.f, l0 = 0.f, r1 = 0.f, l1 = 0.f;
+            if (valid) {
+              split_f64(m2row[c], E2, r0, l0);
+              split_f64(m2row[c + 1], E2, r1, l1);
+            }
+            oz_digits<PP>(r0, l0, ph * PP, d0);
+            oz_digits<PP>(r1, l1, ph * PP, d1);
 #pragma unroll
             for (int i = 0; i < PP; ++i)
               *reinterpret_cast<uint32_t*>(Asm + (i * KCH + kc) * OZ_SLOT_BYTES + off + 2 * t) =
@@ -240,13 +269,21 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           acc64[i] = 0.0;
           sh[i] = sl[i] = 0.f;
         }
+        // m1 of the next N-tile is loaded one N-tile ahead (its latency hides
+        // behind the current N-tile's groups)
+        double m1n[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) m1n[t] = valid ? m1row[t] : 0.0;
         for (int bb = 0; bb < nbb && ok; ++bb) {
           float m1h[8], m1l[8];
 #pragma unroll
           for (int t = 0; t < 8; ++t) {
-            const double x = valid ? m1row[bb * OZ_NB + t] * s1 : 0.0;
-            m1h[t] = __double2float_rn(x);
-            m1l[t] = __double2float_rn(x - (double)m1h[t]);
+            m1h[t] = m1l[t] = 0.f;
+            split_f64(m1n[t], E1, m1h[t], m1l[t]);
+          }
+          if (bb + 1 < nbb) {
+#pragma unroll
+            for (int t = 0; t < 8; ++t) m1n[t] = valid ? m1row[(bb + 1) * OZ_NB + t] : 0.0;
           }
           for (int k = ph * PP + 2; k <= OZ_KMAX; ++k) {
             const int buf = u & 1;
@@ -265,12 +302,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
             for (int t = 0; t < 8; ++t) mw[t] = __fmul_rn(m1h[t], w);
 #pragma unroll
-            for (int cc = 0; cc < 4; ++cc) {  // 4 values of a x 8 of b per load
-              float v[32];
-              tmem_ld32(col + cc * 32, v);
+            for (int cc = 0; cc < 8; ++cc) {  // 2 values of a x 8 of b per load
+              float v[16];
+              tmem_ld16(col + cc * 16, v);
 #pragma unroll
-              for (int q = 0; q < 4; ++q) {
-                const int ai = cc * 4 + q;
+              for (int q = 0; q < 2; ++q) {
+                const int ai = cc * 2 + q;
                 if (pair) {
                   // error-free products, summed pairwise (a tree of depth 3,
                   // so that the dependency chains stay short), then into the
@@ -313,11 +350,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
               sh[i] = t;
             }
           }
-          // the N-tile's double-float sums (8 values of b) go to FP64 once
+          // the double-float sums go to FP64 every four N-tiles (32 values of b)
+          if ((bb & 3) == 3 || bb == nbb - 1) {
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            acc64[i] += (double)sh[i] + (double)sl[i];
-            sh[i] = sl[i] = 0.f;
+            for (int i = 0; i < 16; ++i) {
+              acc64[i] += (double)sh[i] + (double)sl[i];
+              sh[i] = sl[i] = 0.f;
+            }
           }
         }
         if (ok && valid) {
