@@ -140,12 +140,53 @@ __device__ __forceinline__ void oz_digits(float r, float l, int first, float (&d
   }
 }
 
+// Exact widening of an FP32 value by its bit pattern (no FP64 conversion
+// unit); FP32 subnormals, far below every sum here, widen to zero.
+__device__ __forceinline__ double f2d(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xFFu;
+  if (e == 0) return 0.0;
+  return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                          ((unsigned long long)(e + 896u) << 52) |
+                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+
 // s + e = a + b exactly (Knuth's two-sum, no ordering assumption).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   const float t = __fadd_rn(a, b);
   const float bp = __fsub_rn(t, a);
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(t, bp)), __fsub_rn(b, bp));
   s = t;
+}
+
+// Digit groups k = i + j of a phase, in issue order.  Phase 0 holds every
+// group 2..8; its double-float groups (k <= 4, the slow drains) alternate
+// with FP32 ones so that a long drain overlaps a long MMA unit in the
+// two-buffer pipeline.  Later phases hold k = ph * PP + 2 .. 8 in order.
+__device__ __forceinline__ int oz_ngroups(int ph, int pp) {
+  return ph == 0 ? OZ_KMAX - 1 : OZ_KMAX - (ph * pp + 2) + 1;
+}
+__device__ __forceinline__ int oz_group(int ph, int gi, int pp) {
+  if (ph == 0) {
+    constexpr int order = 0x8763542;  // 2, 4, 5, 3, 6, 7, 8 (a nibble each, lowest first)
+    return (order >> (4 * gi)) & 0xF;
+  }
+  return ph * pp + 2 + gi;
+}
+
+// (ah, al) += (bh, bl) in double-float with the accurate addition (Joldes,
+// Muller & Popescu, ACM TOMS 44 (2017), algorithm 6): relative error about
+// 3 * 2^-48.
+__device__ __forceinline__ void dd_add(float& ah, float& al, float bh, float bl) {
+  float s, e, t, f;
+  two_sum(ah, bh, s, e);
+  two_sum(al, bl, t, f);
+  e = __fadd_rn(e, t);
+  const float s2 = __fadd_rn(s, e);
+  e = __fsub_rn(e, __fsub_rn(s2, s));
+  e = __fadd_rn(e, f);
+  ah = __fadd_rn(s2, e);
+  al = __fsub_rn(e, __fsub_rn(ah, s2));
 }
 
 template <int KCH>
@@ -262,13 +303,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       if (!(P.drop_arrive && ph == 0)) mbar_arrive(&a_ready);
 
       for (int ab = 0; ab < nab && ok; ++ab) {
-        double acc64[16];
-        float sh[16], sl[16];
+        float ah[16], al[16];  // the a-block's sums (double-float)
+        float sh[16], sl[16];  // the current four N-tiles' sums
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          acc64[i] = 0.0;
-          sh[i] = sl[i] = 0.f;
-        }
+        for (int i = 0; i < 16; ++i) ah[i] = al[i] = sh[i] = sl[i] = 0.f;
         // m1 of the next N-tile is loaded one N-tile ahead (its latency hides
         // behind the current N-tile's groups)
         double m1n[8];
@@ -285,7 +323,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
             for (int t = 0; t < 8; ++t) m1n[t] = valid ? m1row[(bb + 1) * OZ_NB + t] : 0.0;
           }
-          for (int k = ph * PP + 2; k <= OZ_KMAX; ++k) {
+          for (int gi = 0; gi < oz_ngroups(ph, PP); ++gi) {
+            const int k = oz_group(ph, gi, PP);
             const int buf = u & 1;
             const bool got = mbar_wait(&tfull[buf], (u >> 1) & 1, lim);
             if (!__all_sync(0xffffffffu, got)) {
@@ -350,11 +389,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
               sh[i] = t;
             }
           }
-          // the double-float sums go to FP64 every four N-tiles (32 values of b)
+          // every four N-tiles (32 values of b) the sums join the a-block's by
+          // an accurate double-float addition
           if ((bb & 3) == 3 || bb == nbb - 1) {
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-              acc64[i] += (double)sh[i] + (double)sl[i];
+              dd_add(ah[i], al[i], sh[i], sl[i]);
               sh[i] = sl[i] = 0.f;
             }
           }
@@ -364,9 +404,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           const int* be = P.bexp + (int64_t)g * P.chi_a + ab * OZ_NA + h * 16;
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
-            double t = acc64[i];
+            double t = f2d(ah[i]) + f2d(al[i]);
             if (ph > 0) t += dst[i];  // phase 0's partial sum of this entry
-            if (ph == NPH - 1) t *= ldexp(1.0, be[i] - 16);  // the rows' 2^(E1+E2) goes to the exponent
+            // the slab exponent and the digit weight 2^-16 (the rows' 2^(E1+E2)
+            // goes to the message exponent)
+            if (ph == NPH - 1) t *= __longlong_as_double((long long)(be[i] - 16 + 1023) << 52);
             dst[i] = t;
           }
         }
@@ -382,7 +424,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       for (int ph = 0; ph < NPH && ok; ++ph)
         for (int ab = 0; ab < nab && ok; ++ab)
           for (int bb = 0; bb < nbb && ok; ++bb)
-            for (int k = ph * PP + 2; k <= OZ_KMAX && ok; ++k) {
+            for (int gi = 0; gi < oz_ngroups(ph, PP) && ok; ++gi) {
+              const int k = oz_group(ph, gi, PP);
               const int ilo = max(ph * PP + 1, k - OZ_DIG), ihi = min(ph * PP + PP, k - 1);
               for (int i = ilo; i <= ihi && ok; ++i)
                 for (int kc = 0; kc < KCH; ++kc) {
@@ -418,7 +461,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         tc_fence_after();
         for (int ab = 0; ab < nab && ok; ++ab)
           for (int bb = 0; bb < nbb && ok; ++bb)
-            for (int k = ph * PP + 2; k <= OZ_KMAX && ok; ++k) {
+            for (int gi = 0; gi < oz_ngroups(ph, PP) && ok; ++gi) {
+              const int k = oz_group(ph, gi, PP);
               const int buf = u & 1;
               if (u >= 2 && !mbar_wait(&tempty[buf], ((u >> 1) - 1) & 1, lim)) {
                 ok = false;
