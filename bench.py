@@ -39,9 +39,9 @@ N_VERT, CHI, NDIM = 60, 128, 3
 # captures of this workload (dram__bytes_read.sum + dram__bytes_write.sum):
 # k_contract_tc2 read 2.108 GB + wrote 1.000 GB for 2e6 points
 TC2_DRAM_BYTES_PER_POINT = (2.108e9 + 1.000e9) / 2.0e6
-# k_contract_oz read 67.9 MB + wrote 97.8 MB for 131072 points (capture of a
+# k_contract_oz read 61.8 MB + wrote 91.6 MB for 131072 points (capture of a
 # two-child vertex of this workload at 131072 points)
-OZ_DRAM_BYTES_PER_POINT = (67.9e6 + 97.8e6) / 131072
+OZ_DRAM_BYTES_PER_POINT = (61.8e6 + 91.6e6) / 131072
 # tensor-core passes per algorithmic product
 MMA_PASSES = {"contract_oz": 26, "contract_tc": 3}
 
