@@ -11,6 +11,7 @@
 #include <functional>
 #include <map>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/tnfa.h"
@@ -164,6 +165,12 @@ struct tnfa_ctx {
   // (-1: never), and a cap on Jacobi sweeps (0: the built-in caps)
   int64_t alloc_countdown = -1;
   int jacobi_sweep_cap = 0;
+  // Blocks freed back to this context, by size class, for reuse by later
+  // work on its stream (stream order makes the reuse safe); block -> class
+  // size of every block handed out through the cache.
+  std::map<size_t, std::vector<void*>> free_blocks;
+  std::unordered_map<void*, size_t> block_size;
+  size_t cached_bytes = 0;
 };
 
 struct tnfa_net {
@@ -250,6 +257,7 @@ struct KernelScope {
   ~KernelScope();
 };
 bool trace_on();
+void trace_line(const std::string& line);  // one line to the trace, if tracing
 
 inline unsigned grid_for(int64_t n, int block, int cap = 1 << 20) {
   int64_t g = (n + block - 1) / block;

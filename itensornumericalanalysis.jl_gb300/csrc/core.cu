@@ -38,6 +38,34 @@ void Topo::validate() const {
     TNFA_CHECK(size(v) > 0 && size(v) < (int64_t(1) << 40), TNFA_ERR_SHAPE, "tensor too large");
 }
 
+// Device memory: stream-ordered allocations (cudaMallocAsync) behind a
+// per-context cache of freed blocks.  The batched factorisations allocate and
+// free thousands of small per-problem buffers per sweep step; handing a freed
+// block to the next request of its size class is safe because every launch
+// of the context runs on its one stream, so the earlier user of the block has
+// finished before the next one starts.  Classes: powers of two from 512 B to
+// 1 MiB, then multiples of 2 MiB up to 64 MiB; larger requests are not
+// cached.  While a stream capture is open the cache is bypassed (blocks
+// freed then go back with cudaFreeAsync, as captured graphs require).
+namespace {
+constexpr size_t kCacheMaxBlock = size_t(64) << 20;
+constexpr size_t kCacheMaxBytes = size_t(2) << 30;
+
+size_t size_class(size_t bytes) {
+  if (bytes > (size_t(1) << 20)) return (bytes + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
+  size_t c = 512;
+  while (c < bytes) c <<= 1;
+  return c;
+}
+
+void drop_cache(tnfa_ctx* ctx) {
+  for (auto& kv : ctx->free_blocks)
+    for (void* p : kv.second) cudaFreeAsync(p, ctx->stream);
+  ctx->free_blocks.clear();
+  ctx->cached_bytes = 0;
+}
+}  // namespace
+
 void* dalloc(tnfa_ctx* ctx, size_t bytes) {
   void* p = nullptr;
   if (bytes == 0) return nullptr;
@@ -45,17 +73,48 @@ void* dalloc(tnfa_ctx* ctx, size_t bytes) {
     fail(TNFA_ERR_OUT_OF_MEMORY, "device allocation of " + std::to_string(bytes) +
                                      " bytes failed: injected failure (tnfa_ctx_inject_faults)");
   if (ctx->alloc_countdown > 0) --ctx->alloc_countdown;
-  cudaError_t e = cudaMallocAsync(&p, bytes, ctx->stream);
+  const bool cache = !ctx->capturing && bytes <= kCacheMaxBlock;
+  const size_t cls = cache ? size_class(bytes) : bytes;
+  if (cache) {
+    auto it = ctx->free_blocks.find(cls);
+    if (it != ctx->free_blocks.end() && !it->second.empty()) {
+      p = it->second.back();
+      it->second.pop_back();
+      ctx->cached_bytes -= cls;
+      ctx->block_size[p] = cls;
+      return p;
+    }
+  }
+  cudaError_t e = cudaMallocAsync(&p, cls, ctx->stream);
+  if (e != cudaSuccess && !ctx->capturing && ctx->cached_bytes > 0) {
+    cudaGetLastError();
+    drop_cache(ctx);  // give the cached blocks back to the pool and retry once
+    e = cudaMallocAsync(&p, cls, ctx->stream);
+  }
   if (e != cudaSuccess) {
     cudaGetLastError();
     fail(TNFA_ERR_OUT_OF_MEMORY, "device allocation of " + std::to_string(bytes) +
                                      " bytes failed: " + cudaGetErrorString(e));
   }
+  if (cache) ctx->block_size[p] = cls;
   return p;
 }
 
 void dfree(tnfa_ctx* ctx, void* p) {
-  if (p) cudaFreeAsync(p, ctx->stream);
+  if (!p) return;
+  auto it = ctx->block_size.find(p);
+  if (it == ctx->block_size.end()) {
+    cudaFreeAsync(p, ctx->stream);
+    return;
+  }
+  const size_t cls = it->second;
+  ctx->block_size.erase(it);
+  if (ctx->capturing || ctx->cached_bytes + cls > kCacheMaxBytes) {
+    cudaFreeAsync(p, ctx->stream);
+    return;
+  }
+  ctx->free_blocks[cls].push_back(p);
+  ctx->cached_bytes += cls;
 }
 
 void require_ctx(const tnfa_ctx* ctx) {
@@ -83,6 +142,7 @@ tnfa_net* new_net(tnfa_ctx* ctx, const Topo& topo, int dtype) {
 }
 
 static void ctx_free(tnfa_ctx* ctx) {
+  drop_cache(ctx);
   cudaStreamSynchronize(ctx->stream);
   for (auto& f : ctx->families)
     for (auto& ev : f.events) {
@@ -178,6 +238,13 @@ FILE* trace_file() {
 }  // namespace
 
 bool trace_on() { return trace_file() != nullptr; }
+
+void trace_line(const std::string& line) {
+  if (FILE* f = trace_file()) {
+    fprintf(f, "tnfa-trace %s\n", line.c_str());
+    fflush(f);
+  }
+}
 
 static bool autotune_on(tnfa_ctx* ctx) {
   if (ctx->autotune < 0) {

@@ -12,6 +12,7 @@
 //   lu_solve     : blocked LU with partial pivoting for one dense system
 // Every problem of a batch may have its own shape; one launch covers them all.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <type_traits>
@@ -407,6 +408,325 @@ void qr(tnfa_ctx* ctx, const std::vector<QrJob>& jobs) {
                                                                   dw.as<int64_t>());
     }
     TNFA_LAUNCH_CHECK();
+  }
+}
+
+// ------------------------------------------------------------- qr_rank --
+// Householder QR with column pivoting that stops once the columns left over
+// hold no more than tol^2 of the matrix's squared Frobenius norm: A ~= Q R
+// with Q (m x r, orthonormal) and R (r x n) in A's own column order, r the
+// numerical rank.  Step j reflects the remaining column of largest norm;
+// columns never move (each stays with the CTA that owns it), so R row j holds
+// alpha_j at the pivot column, the reflected row j at the columns not yet
+// pivoted and zeros at the earlier pivots.  The column norms below the
+// current row are recomputed exactly while each column is reflected.  In a
+// cluster every CTA posts its best column and its share of the remaining
+// norm to a slot in global memory; all CTAs reduce the slots in the same
+// order, so they take identical pivot and stop decisions.
+//
+// Workspace: W (m*n) + Qw (m*kq) + alpha (kq) in T as for k_qr; in doubles
+// the column norms (n; -1 marks a pivoted column) and 2 x C slots of
+// (best norm, its column, remaining norm).
+constexpr int QRCP_MAXK = 1024;
+
+__device__ inline void block_argmax_sum(double& best, int& idx, double& sum, double* sb, int* si,
+                                        double* ss) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 16; o; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (ob > best || (ob == best && oi < idx)) {
+      best = ob;
+      idx = oi;
+    }
+  }
+  __syncthreads();
+  if (lane == 0) {
+    sb[warp] = best;
+    si[warp] = idx;
+    ss[warp] = sum;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    best = lane < nw ? sb[lane] : -1.0;
+    idx = lane < nw ? si[lane] : INT_MAX;
+    sum = lane < nw ? ss[lane] : 0.0;
+    for (int o = 16; o; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+      sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (ob > best || (ob == best && oi < idx)) {
+        best = ob;
+        idx = oi;
+      }
+    }
+    if (lane == 0) {
+      sb[0] = best;
+      si[0] = idx;
+      ss[0] = sum;
+    }
+  }
+  __syncthreads();
+  best = sb[0];
+  idx = si[0];
+  sum = ss[0];
+  __syncthreads();
+}
+
+template <class T, bool CL>
+__global__ void __launch_bounds__(512) k_qrcp(const QrJob* __restrict__ jobs, T* __restrict__ work,
+                                              const int64_t* __restrict__ woff, double* __restrict__ dwork,
+                                              const int64_t* __restrict__ doff, double tol2,
+                                              int* __restrict__ ranks) {
+  int C = 1, crank = 0;
+  if constexpr (CL) {
+    C = (int)cg::this_cluster().num_blocks();
+    crank = (int)cg::this_cluster().block_rank();
+  }
+  const int ji = blockIdx.x / C;
+  const QrJob jb = jobs[ji];
+  const int m = jb.m, n = jb.n, kq = min(m, n);
+  T* W = work + woff[ji];
+  T* Qw = W + (int64_t)m * n;
+  T* alpha_g = Qw + (int64_t)m * kq;
+  T* tau = (T*)jb.tau;
+  double* nrm = dwork + doff[ji];
+  double* slot = nrm + n;  // [2][C][3]
+  const T* A = (const T*)jb.A;
+  __shared__ T red[32];
+  __shared__ double sb[32], ss[32];
+  __shared__ int si[32];
+  __shared__ int piv[QRCP_MAXK];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) {
+    const int r = (int)(i / n), c = (int)(i % n);
+    if (c % C == crank) W[(int64_t)c * m + r] = A[i];
+  }
+  __syncthreads();
+  for (int c = crank + C * warp; c < n; c += C * nw) {
+    const T* y = W + (int64_t)c * m;
+    double s = 0.0;
+    for (int r = lane; r < m; r += 32) s += abs2(y[r]);
+    s = warp_sum(s);
+    if (lane == 0) nrm[c] = s;
+  }
+  __syncthreads();
+  double total;
+  {
+    double part = 0.0;
+    for (int c = crank + C * threadIdx.x; c < n; c += C * blockDim.x) part += nrm[c];
+    double b = -1.0;
+    int bi = INT_MAX;
+    block_argmax_sum(b, bi, part, sb, si, ss);
+    if (threadIdx.x == 0) stcg(slot + crank, part);
+    qsync<CL>();
+    total = 0.0;
+    for (int i = 0; i < C; ++i) total += ldcg(slot + i);
+    qsync<CL>();
+  }
+  const double thr = tol2 * total;
+  T* R = (T*)jb.R;
+  int r_keep = kq;
+  for (int j = 0; j < kq; ++j) {
+    double best = -1.0, sum = 0.0;
+    int bi = INT_MAX;
+    for (int c = crank + C * threadIdx.x; c < n; c += C * blockDim.x) {
+      const double v = nrm[c];
+      if (v >= 0.0) {
+        sum += v;
+        if (v > best || (v == best && c < bi)) {
+          best = v;
+          bi = c;
+        }
+      }
+    }
+    block_argmax_sum(best, bi, sum, sb, si, ss);
+    double* my = slot + ((int64_t)(j & 1) * C + crank) * 3;
+    if (threadIdx.x == 0) {
+      stcg(my, best);
+      stcg(my + 1, (double)bi);
+      stcg(my + 2, sum);
+    }
+    qsync<CL>();
+    double gbest = -1.0, gsum = 0.0;
+    int p = INT_MAX;
+    for (int i = 0; i < C; ++i) {
+      const double* o = slot + ((int64_t)(j & 1) * C + i) * 3;
+      const double ob = ldcg(o);
+      const int oi = (int)ldcg(o + 1);
+      gsum += ldcg(o + 2);
+      if (ob > gbest || (ob == gbest && oi < p)) {
+        gbest = ob;
+        p = oi;
+      }
+    }
+    if (p >= n || (j > 0 && (gsum <= thr || !(gbest > 0.0)))) {
+      r_keep = j;  // 0 only when no column has a finite norm
+      break;
+    }
+    if (threadIdx.x == 0) piv[j] = p;
+    T* x = W + (int64_t)p * m;
+    if (p % C == crank) {
+      double part = 0.0;
+      for (int r = j + threadIdx.x; r < m; r += blockDim.x) part += abs2(x[r]);
+      const double nrm2 = re(block_sum<T>(from_real<T>(part), red));
+      if (threadIdx.x == 0) {
+        const T x0 = x[j];
+        const double nv = sqrt(nrm2);
+        if (!(nv > 1e-150)) {
+          stcg(tau + j, from_real<T>(0.0));
+          stcg(alpha_g + j, x0);
+        } else {
+          const T alpha = scal(phase(x0), -nv);
+          const T v0 = x0 - alpha;
+          const double vn2 = nrm2 - abs2(x0) + abs2(v0);
+          stcg(tau + j, from_real<T>(vn2 > 0.0 ? 2.0 / vn2 : 0.0));
+          stcg(x + j, v0);
+          stcg(alpha_g + j, alpha);
+        }
+        nrm[p] = -1.0;
+      }
+    }
+    qsync<CL>();
+    const double beta = re(ldcg(tau + j));
+    for (int c = crank + C * warp; c < n; c += C * nw) {
+      if (nrm[c] < 0.0) continue;  // pivoted earlier (or now, by this CTA)
+      T* y = W + (int64_t)c * m;
+      double s = 0.0;
+      if (beta != 0.0) {
+        T w = from_real<T>(0.0);
+        for (int r = j + lane; r < m; r += 32) w = Sc<T>::fma(conj(ldcg(x + r)), y[r], w);
+        w = warp_sum(w);
+        const T bw = scal(w, beta);
+        for (int r = j + lane; r < m; r += 32) {
+          const T v = y[r] - ldcg(x + r) * bw;
+          y[r] = v;
+          if (r > j) s += abs2(v);
+        }
+      } else {
+        for (int r = j + 1 + lane; r < m; r += 32) s += abs2(y[r]);
+      }
+      s = warp_sum(s);
+      if (lane == 0) nrm[c] = s;
+    }
+    __syncthreads();
+    const T aj = ldcg(alpha_g + j);
+    for (int c = crank + C * threadIdx.x; c < n; c += C * blockDim.x)
+      R[(int64_t)j * n + c] = c == p ? aj : (nrm[c] >= 0.0 ? W[(int64_t)c * m + j] : from_real<T>(0.0));
+  }
+  __syncthreads();
+  // Q = H_0 ... H_{r-1} [I; 0] (m x r), columns owned round-robin
+  for (int c = crank + C * warp; c < r_keep; c += C * nw) {
+    T* y = Qw + (int64_t)c * m;
+    for (int r = lane; r < m; r += 32) y[r] = from_real<T>(r == c ? 1.0 : 0.0);
+  }
+  __syncthreads();
+  for (int j = r_keep - 1; j >= 0; --j) {
+    const double beta = re(ldcg(tau + j));
+    if (beta == 0.0) continue;
+    const T* x = W + (int64_t)piv[j] * m;
+    for (int c = crank + C * warp; c < r_keep; c += C * nw) {
+      if (c < j) continue;
+      T* y = Qw + (int64_t)c * m;
+      T w = from_real<T>(0.0);
+      for (int r = j + lane; r < m; r += 32) w = Sc<T>::fma(conj(ldcg(x + r)), y[r], w);
+      w = warp_sum(w);
+      const T bw = scal(w, beta);
+      for (int r = j + lane; r < m; r += 32) y[r] = y[r] - ldcg(x + r) * bw;
+    }
+  }
+  __syncthreads();
+  T* Q = (T*)jb.Q;
+  for (int64_t i = threadIdx.x; i < (int64_t)m * r_keep; i += blockDim.x) {
+    const int r = (int)(i / r_keep), c = (int)(i % r_keep);
+    if (c % C == crank) Q[i] = Qw[(int64_t)c * m + r];
+  }
+  if (crank == 0 && threadIdx.x == 0) ranks[ji] = r_keep;
+}
+
+template <class T>
+void qr_rank(tnfa_ctx* ctx, const std::vector<QrJob>& jobs, double tol, std::vector<int>& ranks) {
+  ranks.assign(jobs.size(), 0);
+  if (jobs.empty()) return;
+  std::vector<size_t> big, small;
+  const bool few = jobs.size() * 8 <= (size_t)ctx->sm_count;
+  for (size_t i = 0; i < jobs.size(); ++i) {
+    const QrJob& j = jobs[i];
+    TNFA_CHECK(std::min(j.m, j.n) <= QRCP_MAXK, TNFA_ERR_UNSUPPORTED,
+               "rank-revealing QR handles at most 1024 reflectors");
+    (((double)j.m * j.n * std::min(j.m, j.n) >= 4.0e6 && std::min(j.m, j.n) >= 64) ||
+             (few && std::min(j.m, j.n) >= 32)
+         ? big
+         : small)
+        .push_back(i);
+  }
+  // ranks of the cluster launch first, then of the single-CTA launch
+  DBuf rk(ctx, jobs.size() * sizeof(int));
+  for (int pass = 0; pass < 2; ++pass) {
+    const std::vector<size_t>& idx = pass == 0 ? big : small;
+    if (idx.empty()) continue;
+    const int C = pass == 0 ? QR_CLUSTER : 1;
+    int* rl = rk.as<int>() + (pass == 0 ? 0 : big.size());
+    std::vector<QrJob> js;
+    std::vector<int64_t> woff(idx.size() + 1, 0), doff(idx.size() + 1, 0);
+    double fl = 0;
+    for (size_t i = 0; i < idx.size(); ++i) {
+      js.push_back(jobs[idx[i]]);
+      const int64_t m = js[i].m, n = js[i].n, k = std::min(m, n);
+      woff[i + 1] = woff[i] + m * n + m * k + k;
+      doff[i + 1] = doff[i] + n + 6 * C;
+      fl += 4.0 * m * n * k;
+    }
+    DBuf work(ctx, (size_t)woff.back() * sizeof(T));
+    DBuf dwork(ctx, (size_t)doff.back() * sizeof(double));
+    DBuf dw = upload(ctx, woff);
+    DBuf dd = upload(ctx, doff);
+    DBuf d = upload(ctx, js);
+    KernelScope ks(ctx, sizeof(T) == 8 ? "qr_rank_f64" : "qr_rank_c128", fl, 0.0);
+    if (trace_on()) ks.note = (pass == 0 ? "cluster " : "single ") + size_note(js);
+    if (pass == 0) {
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3((unsigned)(js.size() * QR_CLUSTER));
+      cfg.blockDim = dim3(512);
+      cfg.stream = ctx->stream;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = QR_CLUSTER;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      TNFA_CUDA(cudaLaunchKernelEx(&cfg, k_qrcp<T, true>, (const QrJob*)d.as<QrJob>(), work.as<T>(),
+                                   (const int64_t*)dw.as<int64_t>(), dwork.as<double>(),
+                                   (const int64_t*)dd.as<int64_t>(), tol * tol, rl));
+    } else {
+      k_qrcp<T, false><<<(unsigned)js.size(), 512, 0, ctx->stream>>>(
+          d.as<QrJob>(), work.as<T>(), dw.as<int64_t>(), dwork.as<double>(), dd.as<int64_t>(), tol * tol,
+          rl);
+    }
+    TNFA_LAUNCH_CHECK();
+  }
+  std::vector<int> h(jobs.size());
+  TNFA_CUDA(cudaMemcpyAsync(h.data(), rk.p, jobs.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (size_t i = 0; i < big.size(); ++i) ranks[big[i]] = h[i];
+  for (size_t i = 0; i < small.size(); ++i) ranks[small[i]] = h[big.size() + i];
+  for (int r : ranks)
+    TNFA_CHECK(r >= 1, TNFA_ERR_DOMAIN, "rank-revealing QR: no column with a finite norm (NaN or Inf input)");
+  if (trace_on()) {
+    long sr = 0, sk = 0, mx_m = 0, mx_n = 0, mx_r = 0;
+    for (size_t i = 0; i < jobs.size(); ++i) {
+      sr += ranks[i];
+      sk += std::min(jobs[i].m, jobs[i].n);
+      mx_m = std::max<long>(mx_m, jobs[i].m);
+      mx_n = std::max<long>(mx_n, jobs[i].n);
+      mx_r = std::max<long>(mx_r, ranks[i]);
+    }
+    char b[200];
+    snprintf(b, sizeof b, "qr_rank ranks jobs=%zu sum_r=%ld sum_minmn=%ld max_m=%ld max_n=%ld max_r=%ld",
+             jobs.size(), sr, sk, mx_m, mx_n, mx_r);
+    trace_line(b);
   }
 }
 
@@ -1282,7 +1602,7 @@ void copy_blocks(tnfa_ctx* ctx, const std::vector<CopyJob>& jobs) {
 
 template <class T>
 void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cutoff, int maxdim,
-                  int mindim, int precision, std::vector<FactorResult>& out) {
+                  int mindim, int precision, std::vector<FactorResult>& out, double reveal_tol) {
   const size_t nj = jobs.size();
   out.clear();
   out.resize(nj);
@@ -1296,17 +1616,73 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
   //   wide      : M^H = Q R, C = R^H,       L = U_r,   X = U_r^H M
   std::vector<int> n(nj), cm(nj), ku(nj);
   std::vector<char> tall(nj), useq(nj);
-  std::vector<DBuf> Q(nj), R(nj), tau(nj), Mt(nj), J(nj), U(nj), S(nj), sw(nj);
+  std::vector<DBuf> Q(nj), R(nj), tau(nj), Mt(nj), J(nj), U(nj);
   std::vector<const void*> core(nj);
   std::vector<CopyJob> adj;
   std::vector<QrJob> qj;
+  // singular values and sweep counts of all jobs in two buffers, so that the
+  // host reads them back with one copy each
+  std::vector<size_t> soff(nj + 1, 0);
+  for (size_t q = 0; q < nj; ++q) soff[q + 1] = soff[q] + (size_t)std::min(jobs[q].rows, jobs[q].cols);
+  DBuf Sall(ctx, std::max<size_t>(soff[nj], 1) * sizeof(double));
+  DBuf swall(ctx, nj * sizeof(int));
+  auto S_of = [&](size_t q) { return Sall.as<double>() + soff[q]; };
+  auto sw_of = [&](size_t q) { return swall.as<int>() + q; };
+  // Rank-revealing front end (reveal_tol > 0, tall jobs): M = Q1 R1 by
+  // pivoted QR with R1 (r x cols), r the numerical rank; when r < cols the
+  // square core is R2^H from R1^H = Q2 R2, else R1 itself.  The left vectors
+  // of M are Q1 times those of the core, so L = Q1 U_r and X = U_r^H R1, as
+  // for the plain tall case with (Q, R) = (Q1, R1).
+  std::vector<char> rev(nj, 0);
+  if (reveal_tol > 0.0) {
+    std::vector<QrJob> pj;
+    std::vector<size_t> pidx;
+    for (size_t q = 0; q < nj; ++q) {
+      const FactorJob& f = jobs[q];
+      if (f.rows < f.cols) continue;
+      rev[q] = 1;
+      Q[q] = DBuf(ctx, (size_t)f.rows * f.cols * sizeof(T));
+      R[q] = DBuf(ctx, (size_t)f.cols * f.cols * sizeof(T));
+      tau[q] = DBuf(ctx, (size_t)f.cols * sizeof(T));
+      pj.push_back({f.M, Q[q].p, R[q].p, tau[q].p, f.rows, f.cols});
+      pidx.push_back(q);
+    }
+    std::vector<int> rk;
+    qr_rank<T>(ctx, pj, reveal_tol, rk);
+    // R1^H = Q2 R2 for the jobs with r < cols; the core is R2^H
+    std::vector<DBuf> Rt(nj), Q2(nj), R2(nj), t2(nj);
+    std::vector<CopyJob> tr, back;
+    std::vector<QrJob> lq;
+    for (size_t i = 0; i < pidx.size(); ++i) {
+      const size_t q = pidx[i];
+      const int r = rk[i], cols = jobs[q].cols;
+      n[q] = cm[q] = r;
+      tall[q] = useq[q] = 1;
+      if (r == cols) {
+        core[q] = R[q].p;
+        continue;
+      }
+      Rt[q] = DBuf(ctx, (size_t)cols * r * sizeof(T));
+      Q2[q] = DBuf(ctx, (size_t)cols * r * sizeof(T));
+      R2[q] = DBuf(ctx, (size_t)r * r * sizeof(T));
+      t2[q] = DBuf(ctx, (size_t)r * sizeof(T));
+      tr.push_back({R[q].p, Rt[q].p, r, cols, cols, r, 1, 1});
+      lq.push_back({Rt[q].p, Q2[q].p, R2[q].p, t2[q].p, cols, r});
+      J[q] = DBuf(ctx, (size_t)r * r * sizeof(T));
+      back.push_back({R2[q].p, J[q].p, r, r, r, r, 1, 1});
+      core[q] = J[q].p;
+    }
+    copy_blocks<T, T>(ctx, tr);
+    qr<T>(ctx, lq);
+    copy_blocks<T, T>(ctx, back);
+  }
   for (size_t q = 0; q < nj; ++q) {
     const FactorJob& f = jobs[q];
+    if (rev[q]) continue;
     tall[q] = f.rows >= f.cols;
     n[q] = std::min(f.rows, f.cols);
     const int k = n[q];
     useq[q] = tall[q] && !mixed;
-    sw[q] = DBuf(ctx, sizeof(int));
     if (tall[q] && mixed) {
       core[q] = f.M;
       cm[q] = f.rows;
@@ -1346,8 +1722,7 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     for (size_t q = 0; q < nj; ++q) {
       ku[q] = n[q];
       U[q] = DBuf(ctx, (size_t)cm[q] * n[q] * sizeof(T));
-      S[q] = DBuf(ctx, (size_t)n[q] * sizeof(double));
-      sj.push_back({core[q], U[q].p, S[q].as<double>(), nullptr, cm[q], n[q], sw[q].as<int>()});
+      sj.push_back({core[q], U[q].p, S_of(q), nullptr, cm[q], n[q], sw_of(q)});
     }
     jacobi<T>(ctx, sj, 60, opts, real64 ? "svd_f64" : "svd_c128");
   } else {
@@ -1365,7 +1740,9 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     std::vector<double> ss_in(nj), ss_kept(nj);
     for (size_t q = 0; q < nj; ++q) w[q] = n[q];
     for (int pass = 0; pass < 2; ++pass) {
-      std::vector<DBuf> C32(nj), U32(nj), V32(nj), S32(nj), sw32(nj), V(nj), G(nj), Y(nj), Xn(nj);
+      std::vector<DBuf> C32(nj), U32(nj), V32(nj), V(nj), G(nj), Y(nj), Xn(nj);
+      DBuf S32all(ctx, std::max<size_t>(soff[nj], 1) * sizeof(double));
+      DBuf sw32all(ctx, nj * sizeof(int));
       std::vector<CopyJob> down, up;
       std::vector<SvdJob> s32;
       // FP32 copies scaled by a power of two to unit size
@@ -1385,10 +1762,9 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
         C32[q] = DBuf(ctx, (size_t)m * k * sizeof(float));
         U32[q] = DBuf(ctx, (size_t)m * k * sizeof(float));
         V32[q] = DBuf(ctx, (size_t)k * k * sizeof(float));
-        S32[q] = DBuf(ctx, (size_t)k * sizeof(double));
-        sw32[q] = DBuf(ctx, sizeof(int));
         down.push_back({xin[q], C32[q].p, m, k, k, k, 0, 0, ss.as<double>() + q});
-        s32.push_back({C32[q].p, U32[q].p, S32[q].as<double>(), V32[q].p, m, k, sw32[q].as<int>()});
+        s32.push_back({C32[q].p, U32[q].p, S32all.as<double>() + soff[q], V32[q].p, m, k,
+                       sw32all.as<int>() + q});
       }
       copy_blocks<double, float>(ctx, down);
       // pass 1 only has to split kept from dropped directions and hand pass 2
@@ -1402,21 +1778,19 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
         // dropped weight must sit far below the truncation budget (here
         // 1e-6 of it: the FP64 rule below drops it too, and the loss stays
         // near 1e-10 of the norm).  Exactly-deficient ranks still fall away.
-        std::vector<std::vector<double>> sv32(nj);
+        std::vector<double> sv32(soff[nj]);
         const std::vector<double>& hss = ss_in;
-        for (size_t q = 0; q < nj; ++q) {
-          sv32[q].resize(n[q]);
-          TNFA_CUDA(cudaMemcpyAsync(sv32[q].data(), S32[q].p, n[q] * sizeof(double),
-                                    cudaMemcpyDeviceToHost, ctx->stream));
-        }
+        TNFA_CUDA(cudaMemcpyAsync(sv32.data(), S32all.p, soff[nj] * sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
         TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
         for (size_t q = 0; q < nj; ++q) {
           const int k = n[q];
+          double* sq = sv32.data() + soff[q];
           // undo the power-of-two scaling of the FP32 copy
           const double f = std::sqrt(hss[q]);
           const double back = f > 0 && std::isfinite(f) ? std::ldexp(1.0, std::ilogb(f)) : 1.0;
-          for (double& x : sv32[q]) x *= back;
-          int keep = cutoff > 0 ? truncation_rank(sv32[q].data(), k, cutoff * 1e-6, 0, 1) : k;
+          for (int i = 0; i < k; ++i) sq[i] *= back;
+          int keep = cutoff > 0 ? truncation_rank(sq, k, cutoff * 1e-6, 0, 1) : k;
           if (maxdim > 0) keep = std::min(keep, std::min(k, maxdim + 8));
           keep = std::max(keep, std::min(k, std::max(mindim, 1)));
           ku[q] = keep;
@@ -1462,8 +1836,7 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     for (size_t q = 0; q < nj; ++q) extra[q] = std::max(0.0, ss_in[q] - ss_kept[q]);
     for (size_t q = 0; q < nj; ++q) {
       U[q] = DBuf(ctx, (size_t)cm[q] * ku[q] * sizeof(T));
-      S[q] = DBuf(ctx, (size_t)ku[q] * sizeof(double));
-      sj.push_back({X[q].p, U[q].p, S[q].as<double>(), nullptr, cm[q], ku[q], sw[q].as<int>()});
+      sj.push_back({X[q].p, U[q].p, S_of(q), nullptr, cm[q], ku[q], sw_of(q)});
     }
     jacobi<T>(ctx, sj, 60, polish, "svd_polish_f64");
     // Diagnostics (TNFA_DEBUG_DIR with TNFA_DEBUG_SWEEPS=k): the FP64 core of
@@ -1474,7 +1847,7 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
       static int counter = 0;
       for (size_t q = 0; q < nj && counter < 32; ++q) {
         int swq = 0;
-        TNFA_CUDA(cudaMemcpyAsync(&swq, sw[q].p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        TNFA_CUDA(cudaMemcpyAsync(&swq, sw_of(q), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
         if (swq >= 0 && swq < thr) continue;
         const int m = cm[q], k = n[q], c = ku[q];
@@ -1494,14 +1867,19 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
       }
     }
   }
-  // (3) ranks on the host
-  for (size_t q = 0; q < nj; ++q) {
-    out[q].s.resize(ku[q]);
-    TNFA_CUDA(cudaMemcpyAsync(out[q].s.data(), S[q].p, ku[q] * sizeof(double), cudaMemcpyDeviceToHost,
+  // (3) ranks on the host (one read-back of every job's values and sweeps)
+  {
+    std::vector<double> hs(soff[nj]);
+    std::vector<int> hsw(nj);
+    TNFA_CUDA(cudaMemcpyAsync(hs.data(), Sall.p, soff[nj] * sizeof(double), cudaMemcpyDeviceToHost,
                               ctx->stream));
-    TNFA_CUDA(cudaMemcpyAsync(&out[q].sweeps, sw[q].p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    TNFA_CUDA(cudaMemcpyAsync(hsw.data(), swall.p, nj * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (size_t q = 0; q < nj; ++q) {
+      out[q].s.assign(hs.begin() + soff[q], hs.begin() + soff[q] + ku[q]);
+      out[q].sweeps = hsw[q];
+    }
   }
-  TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
   std::vector<GemmJob> gl, gx;
   std::vector<CopyJob> cl;
   for (size_t q = 0; q < nj; ++q) {
@@ -1567,10 +1945,12 @@ template void gemm<double>(tnfa_ctx*, const std::vector<GemmJob>&);
 template void gemm<cplx>(tnfa_ctx*, const std::vector<GemmJob>&);
 template void qr<double>(tnfa_ctx*, const std::vector<QrJob>&);
 template void qr<cplx>(tnfa_ctx*, const std::vector<QrJob>&);
+template void qr_rank<double>(tnfa_ctx*, const std::vector<QrJob>&, double, std::vector<int>&);
+template void qr_rank<cplx>(tnfa_ctx*, const std::vector<QrJob>&, double, std::vector<int>&);
 template void trunc_factor<double>(tnfa_ctx*, const std::vector<FactorJob>&, double, int, int, int,
-                                   std::vector<FactorResult>&);
+                                   std::vector<FactorResult>&, double);
 template void trunc_factor<cplx>(tnfa_ctx*, const std::vector<FactorJob>&, double, int, int, int,
-                                 std::vector<FactorResult>&);
+                                 std::vector<FactorResult>&, double);
 
 }  // namespace la
 }  // namespace tnfa

@@ -46,6 +46,14 @@ struct QrJob {
 template <class T>
 void qr(tnfa_ctx* ctx, const std::vector<QrJob>& jobs);
 
+// Rank-revealing QR (Householder with column pivoting) of the same jobs:
+// A ~= Q R with Q (m x r, orthonormal, written row-major m x r into the Q
+// buffer) and R (r x n, A's column order, the first r rows of the R buffer),
+// where r >= 1 is the first step at which the columns not yet pivoted hold
+// at most tol^2 of |A|_F^2 (r = min(m, n) if none).  ranks[i] = r of job i.
+template <class T>
+void qr_rank(tnfa_ctx* ctx, const std::vector<QrJob>& jobs, double tol, std::vector<int>& ranks);
+
 // One job of the one-sided Jacobi SVD used by trunc_factor: A (m x n, m >=
 // n, lda = n, read only) = U diag(S) V^H with U (m x n, orthonormal columns
 // where S > 0), S (n, real, descending), V (n x n; not accumulated when V is
@@ -85,9 +93,12 @@ struct FactorResult {
   int sweeps = 0;          // FP64 Jacobi sweeps; -1: the sweep cap was hit
   std::vector<double> s;   // singular values, descending
 };
+// reveal_tol > 0: tall jobs first go through the rank-revealing QR (qr_rank
+// with that tolerance) and the core is the square factor of its numerical
+// rank, so the SVD runs on r x r rather than cols x cols.
 template <class T>
 void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cutoff, int maxdim,
-                  int mindim, int precision, std::vector<FactorResult>& out);
+                  int mindim, int precision, std::vector<FactorResult>& out, double reveal_tol = 0.0);
 
 // Rank kept by the reference truncation rule: smallest r >= mindim with
 // sum_{i >= r} s_i^2 <= cutoff * sum s_i^2, capped by maxdim (> 0).

@@ -714,10 +714,13 @@ struct BSlot {
 };
 
 // QR of the listed vertices with their parent axis (1) as columns; each keeps
-// Q and returns R (k x old) in Rs[i]; ks[i] = k.
+// Q and returns R (k x old) in Rs[i]; ks[i] = k.  With reveal_tol > 0 the
+// factorisation is rank revealing (column pivoting): k is the numerical rank,
+// the directions left out holding at most reveal_tol of the matrix's
+// Frobenius norm.
 template <class T>
 void qr_parent_axis_batched(std::vector<Work<T>>& W, const std::vector<BSlot>& sl,
-                            std::vector<DBuf>& Rs, std::vector<int>& ks) {
+                            std::vector<DBuf>& Rs, std::vector<int>& ks, double reveal_tol = 0.0) {
   if (sl.empty()) return;
   tnfa_ctx* ctx = W[sl[0].net].ctx;
   const size_t n = sl.size();
@@ -744,7 +747,10 @@ void qr_parent_axis_batched(std::vector<Work<T>>& W, const std::vector<BSlot>& s
     qj.push_back({M[i].p, Q[i].p, Rs[i].p, tau[i].p, (int)rows, cols});
   }
   move_axes<T>(ctx, mv);
-  la::qr<T>(ctx, qj);
+  if (reveal_tol > 0.0)
+    la::qr_rank<T>(ctx, qj, reveal_tol, ks);
+  else
+    la::qr<T>(ctx, qj);
   mv.clear();
   for (size_t i = 0; i < n; ++i) {
     std::vector<int> qshp = shp[i];
@@ -797,13 +803,21 @@ void absorb_batched(std::vector<Work<T>>& W, const std::vector<BSlot>& sl, const
   for (size_t i = 0; i < n; ++i) W[sl[i].net].t[sl[i].v] = std::move(c[i]);
 }
 
+// Relative Frobenius weight below which the batched orthogonalisation drops
+// directions (a few hundred times the FP64 rounding of a QR step).
+constexpr double kRevealTol = 1e-13;
+
 template <class T>
 void truncate_paths_batched(std::vector<Work<T>>& W, const tnfa_trunc_params& prm) {
   if (W.empty()) return;
   tnfa_ctx* ctx = W[0].ctx;
   int maxV = 0;
   for (auto& w : W) maxV = std::max(maxV, w.topo.V);
-  // (1) orthogonalise toward vertex 0, from the far end of every path
+  // (1) orthogonalise toward vertex 0, from the far end of every path.  The
+  // QR is rank revealing: an operator's exact product carries bonds of D chi
+  // whose numerical rank is often far lower (a shift adds one direction per
+  // bond), and dropping the directions at the FP64 rounding floor here
+  // shrinks every later factorisation.
   for (int t = 0; t + 1 < maxV; ++t) {
     std::vector<BSlot> sl;
     for (int i = 0; i < (int)W.size(); ++i) {
@@ -812,7 +826,7 @@ void truncate_paths_batched(std::vector<Work<T>>& W, const tnfa_trunc_params& pr
     }
     std::vector<DBuf> Rs;
     std::vector<int> ks;
-    qr_parent_axis_batched(W, sl, Rs, ks);
+    qr_parent_axis_batched(W, sl, Rs, ks, kRevealTol);
     std::vector<BSlot> ps;
     std::vector<int> ax;
     std::vector<const void*> Ms;
@@ -849,7 +863,7 @@ void truncate_paths_batched(std::vector<Work<T>>& W, const tnfa_trunc_params& pr
     }
     move_axes<T>(ctx, mv);
     std::vector<la::FactorResult> res;
-    la::trunc_factor<T>(ctx, fj, prm.cutoff, prm.maxdim, prm.mindim, prm.precision, res);
+    la::trunc_factor<T>(ctx, fj, prm.cutoff, prm.maxdim, prm.mindim, prm.precision, res, kRevealTol);
     mv.clear();
     for (size_t q = 0; q < n; ++q) {
       TNFA_CHECK(res[q].sweeps >= 0, TNFA_ERR_NOT_CONVERGED, "Jacobi SVD hit its sweep cap");

@@ -229,10 +229,12 @@ def test_mixed_truncation_matches_fp64(ina, L, chi):
     assert a.linkdims() == b.linkdims()
     ref = a.evaluate_batch(X)
     assert rel_err(b.evaluate_batch(X), ref) < 1e-9
-    bb = ina.operate_batched([op] * 3, [f] * 3, cutoff=1e-10, precision="mixed")
-    for g in bb:
-        assert g.linkdims() == a.linkdims()
-        assert rel_err(g.evaluate_batch(X), ref) < 1e-9
+    # the batched sweeps (rank-revealing QR front ends) in both precisions
+    for prec in ("mixed", "f64"):
+        bb = ina.operate_batched([op] * 3, [f] * 3, cutoff=1e-10, precision=prec)
+        for g in bb:
+            assert g.linkdims() == a.linkdims()
+            assert rel_err(g.evaluate_batch(X), ref) < 1e-9
 
 
 @pytest.mark.parametrize("precision", ["f64", "mixed"])
