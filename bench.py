@@ -277,8 +277,11 @@ def _timed(fn, reps=1):
 
 def integrate_rates(f32net, f64net, peaks) -> dict:
     """integrate() over [0,1)^3 of the benchmark network: the HBM-bound member
-    of the path (k_integrate_level reads every tensor byte once), FP32 and
-    FP64 copies, CUDA events on the current stream around 5 calls."""
+    of the path (one persistent k_integrate launch reads every tensor byte
+    once), FP32 and FP64 copies.  Per call: CUDA events on the current stream
+    around 5 calls (host set-up and the read-back included); per kernel: the
+    library's own CUDA events around each k_integrate launch (on its
+    stream)."""
     import torch
 
     out = {}
@@ -294,8 +297,17 @@ def integrate_rates(f32net, f64net, peaks) -> dict:
         torch.cuda.synchronize()
         ti = ev0.elapsed_time(ev1) / 1e3 / reps
         nbytes = nt.info()[2] * (4 if name == "f32" else 8)
+        nt.ctx.kernel_stats(reset=True)
+        nt.ctx.set_timing(True)
+        for _ in range(reps):
+            nt.integrate()
+        nt.ctx.set_timing(False)
+        st = nt.ctx.kernel_stats(reset=True).get("integrate", {})
+        tk = st["ms"] / st["launches"] / 1e3 if st.get("launches") else float("nan")
         out[name] = {"ms": ti * 1e3, "tensor_bytes": nbytes, "GBps": nbytes / ti / 1e9,
-                     "frac_of_hbm": nbytes / ti / 1e9 / peaks["hbm_gbs"]}
+                     "frac_of_hbm": nbytes / ti / 1e9 / peaks["hbm_gbs"],
+                     "kernel_ms": tk * 1e3, "kernel_GBps": nbytes / tk / 1e9,
+                     "kernel_frac_of_hbm": nbytes / tk / 1e9 / peaks["hbm_gbs"]}
     return out
 
 

@@ -1,7 +1,7 @@
 // Inline-PTX building blocks of the tcgen05 kernels (sm_103a): mbarriers with
-// bounded waits, TMA tensor loads, shared-memory matrix descriptors, MMA issue
-// and commit, tensor-memory loads.  Shared by evaluate_tc.cu and
-// evaluate_oz.cu.
+// bounded waits, TMA tensor loads and untiled bulk copies, shared-memory
+// matrix descriptors, MMA issue and commit, tensor-memory loads.  Shared by
+// evaluate_tc.cu, evaluate_oz.cu and integrate.cu.
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -49,6 +49,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
   return false;
 }
 
+// Non-blocking test of the phase with the given parity.
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
@@ -80,6 +93,17 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
       "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
       "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+// Contiguous bulk copy global -> shared (no tensor map): both addresses
+// 16-byte aligned, bytes a multiple of 16; completes as transaction bytes on
+// `bar`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
 
