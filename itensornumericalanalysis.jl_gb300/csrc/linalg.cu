@@ -103,6 +103,8 @@ void permute(tnfa_ctx* ctx, const std::vector<PermJob>& jobs) {
   int64_t nmax = 1;
   for (const auto& j : jobs) nmax = std::max(nmax, j.n);
   TNFA_CHECK(jobs.size() <= 65535, TNFA_ERR_UNSUPPORTED, "permute batch too large");
+  for (const auto& j : jobs)
+    TNFA_CHECK(j.nd >= 1 && j.nd <= MAXD, TNFA_ERR_UNSUPPORTED, "permute: tensor order above 16");
   DBuf d = upload(ctx, jobs);
   dim3 grid(grid_for(nmax, 256, 2048), (unsigned)jobs.size());
   KernelScope ks(ctx, "permute", 0.0, 2.0 * sizeof(T) * nmax * jobs.size());

@@ -7,7 +7,7 @@
 namespace tnfa {
 namespace la {
 
-constexpr int MAXD = 10;  // tensor order handled by permute
+constexpr int MAXD = 16;  // tensor order handled by permute
 
 // dst = transpose of src: dst axis i is src axis perm[i].
 struct PermJob {

@@ -14,6 +14,7 @@
 // centre into c (S V^H absorbed), recurse, then QR c back toward v.  Every
 // SVD therefore sees the exact Schmidt spectrum of its bond.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdlib>
 #include <functional>
@@ -119,7 +120,7 @@ void move_axis(tnfa_ctx* ctx, const void* src, void* dst, const std::vector<int>
   j.src = src;
   j.dst = dst;
   j.nd = (int)shp.size();
-  TNFA_CHECK(j.nd <= la::MAXD, TNFA_ERR_UNSUPPORTED, "tensor order above 10");
+  TNFA_CHECK(j.nd <= la::MAXD, TNFA_ERR_UNSUPPORTED, "tensor order above 16");
   std::vector<int> order(j.nd);
   std::iota(order.begin(), order.end(), 0);
   order.erase(order.begin() + ax);
@@ -691,7 +692,7 @@ void move_axes(tnfa_ctx* ctx, const std::vector<MoveJob>& mv) {
     j.src = m.src;
     j.dst = m.dst;
     j.nd = (int)m.shp.size();
-    TNFA_CHECK(j.nd <= la::MAXD, TNFA_ERR_UNSUPPORTED, "tensor order above 10");
+    TNFA_CHECK(j.nd <= la::MAXD, TNFA_ERR_UNSUPPORTED, "tensor order above 16");
     std::vector<int> order(j.nd);
     std::iota(order.begin(), order.end(), 0);
     order.erase(order.begin() + m.ax);
@@ -1048,6 +1049,8 @@ Dense permuted(tnfa_ctx* ctx, const double* src, const std::vector<int>& shp,
     d.shp[a] = shp[order[a]];
     n *= shp[a];
   }
+  TNFA_CHECK(shp.size() == order.size() && (int)shp.size() <= la::MAXD, TNFA_ERR_UNSUPPORTED,
+             "permute: tensor order above 16");
   d.b = DBuf(ctx, (size_t)n * 8);
   la::PermJob j{};
   j.src = src;
@@ -1668,11 +1671,15 @@ tnfa_net* linsolve_path(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, con
   return store_work(wb, TNFA_F64);
 }
 
-// linsolve_path followed by iterative refinement on the caller's layout.
+tnfa_net* linsolve_any(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnfa_net* x0,
+                       const tnfa_linsolve_params& prm, double* rel_res);
+
+// linsolve (path or tree sweep) followed by iterative refinement on the
+// caller's layout.
 tnfa_net* linsolve_refined(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnfa_net* x0,
                            const tnfa_linsolve_params& prm, double* rel_res) {
   double res = 0.0;
-  NetHold x(linsolve_path(ctx, A, b, x0, prm, &res));
+  NetHold x(linsolve_any(ctx, A, b, x0, prm, &res));
   if (prm.refinements > 0 && res > prm.tol) {
     const double bnorm = qr_norm(ctx, b);
     const tnfa_trunc_params tr{prm.refine_cutoff, prm.maxdim, 1, 0, TNFA_PREC_F64};
@@ -1686,7 +1693,7 @@ tnfa_net* linsolve_refined(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, 
       abi(ctx, tnfa_net_scale(ctx, r.p, 0, -1.0, 0.0));
       NetHold rt(truncate_net(ctx, r.p, tr));
       double eres = 0.0;
-      NetHold e(linsolve_path(ctx, A, rt.p, rt.p, pe, &eres));
+      NetHold e(linsolve_any(ctx, A, rt.p, rt.p, pe, &eres));
       NetHold sum(direct_sum_ext(ctx, x.p, e.p));
       NetHold xn(truncate_net(ctx, sum.p, tr));
       Work<double> xnw = load_work<double>(ctx, xn.p);
@@ -1783,6 +1790,382 @@ tnfa_net* dmrg_path(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* x0, const 
   for (int k = 0; k < L; ++k) pos[ord[k]] = k;
   Work<double> wb = relayout<double>(ctx, xp.p->topo, xp.p->d, back, pos);
   return store_work(wb, TNFA_F64);
+}
+
+// ------------------------------------------------------- tree solvers ----
+// linsolve and dmrg on any tree (vertices of any degree, one site leg each),
+// the sweep ITensorNetworks runs with nsites = 2 on a TreeTensorNetwork:
+// the orthogonality centre walks a depth-first tour from the root, every
+// edge (u, c) is updated twice per sweep (on the way down the centre moves
+// to c, on the way back to u), and each update solves the system projected
+// onto the environments of all other edges, then splits the two-site tensor
+// by a truncated SVD.  Environments are kept per directed edge (a -> b: the
+// part of the network on a's side); those pointing at the centre stay valid
+// along the tour.  Contractions are labelled: every tensor carries one label
+// per axis and a pairwise contraction (permute + GEMM on the device) sums
+// over the labels the two share.
+
+// A device tensor with labelled axes; views (LV) borrow the data.
+struct LT {
+  Dense d;
+  std::vector<int> lab;
+};
+struct LV {
+  const double* p;
+  std::vector<int> shp, lab;
+};
+LV view(const LT& t) { return {t.d.p(), t.d.shp, t.lab}; }
+
+int64_t numel(const std::vector<int>& s) {
+  int64_t n = 1;
+  for (int x : s) n *= x;
+  return n;
+}
+
+// Axes of A put in label order `order`.
+LT lt_perm(tnfa_ctx* ctx, const LV& A, const std::vector<int>& order) {
+  TNFA_CHECK(order.size() == A.lab.size(), TNFA_ERR_INVALID_ARGUMENT, "tree solver: label count");
+  std::vector<int> p(order.size());
+  for (size_t i = 0; i < order.size(); ++i) {
+    const auto it = std::find(A.lab.begin(), A.lab.end(), order[i]);
+    TNFA_CHECK(it != A.lab.end(), TNFA_ERR_INVALID_ARGUMENT, "tree solver: missing label");
+    p[i] = (int)(it - A.lab.begin());
+  }
+  return LT{permuted(ctx, A.p, A.shp, p), order};
+}
+
+// Sum over the labels A and B share; result axes: A's other labels, then B's.
+LT lt_contract(tnfa_ctx* ctx, const LV& A, const LV& B) {
+  std::vector<int> sh, fa, fb, sa_dims, fa_dims, fb_dims;
+  for (size_t i = 0; i < A.lab.size(); ++i) {
+    const auto it = std::find(B.lab.begin(), B.lab.end(), A.lab[i]);
+    if (it == B.lab.end()) {
+      fa.push_back(A.lab[i]);
+      fa_dims.push_back(A.shp[i]);
+    } else {
+      TNFA_CHECK(B.shp[it - B.lab.begin()] == A.shp[i], TNFA_ERR_SHAPE, "tree solver: bond dims disagree");
+      sh.push_back(A.lab[i]);
+      sa_dims.push_back(A.shp[i]);
+    }
+  }
+  for (size_t i = 0; i < B.lab.size(); ++i)
+    if (std::find(A.lab.begin(), A.lab.end(), B.lab[i]) == A.lab.end()) {
+      fb.push_back(B.lab[i]);
+      fb_dims.push_back(B.shp[i]);
+    }
+  const int64_t m = numel(fa_dims), k = numel(sa_dims), n = numel(fb_dims);
+  TNFA_CHECK(m < (int64_t(1) << 31) && n < (int64_t(1) << 31) && k < (int64_t(1) << 31),
+             TNFA_ERR_UNSUPPORTED, "tree solver: contraction too large");
+  // A as [free][shared] (or [shared][free], transposed), B as [shared][free]
+  // (or [free][shared]); permute only when neither order holds
+  auto cat = [](std::vector<int> a, const std::vector<int>& b) {
+    a.insert(a.end(), b.begin(), b.end());
+    return a;
+  };
+  LT ta, tb;
+  const double* pa = A.p;
+  const double* pb = B.p;
+  int opA = 0, opB = 0;
+  if (A.lab == cat(fa, sh)) {
+    opA = 0;
+  } else if (A.lab == cat(sh, fa)) {
+    opA = 1;
+  } else {
+    ta = lt_perm(ctx, A, cat(fa, sh));
+    pa = ta.d.p();
+  }
+  if (B.lab == cat(sh, fb)) {
+    opB = 0;
+  } else if (B.lab == cat(fb, sh)) {
+    opB = 1;
+  } else {
+    tb = lt_perm(ctx, B, cat(sh, fb));
+    pb = tb.d.p();
+  }
+  LT out;
+  out.lab = cat(fa, fb);
+  out.d = mm(ctx, pa, pb, (int)m, (int)n, (int)k, opA, opB, cat(fa_dims, fb_dims));
+  return out;
+}
+
+struct TreeSolve {
+  tnfa_ctx* ctx;
+  int V, d, root;
+  Work<double> x, A, b;
+  bool has_b = true;
+  std::map<std::pair<int, int>, LT> EA, Eb;  // directed edge (from, to); from -1: the root's open end
+  enum { S = 0, SP = 1, K = 2, KP = 3, W = 4, B = 5 };
+  int lab(int kind, int id) const { return kind * V + id; }  // id: a vertex or an edge (its child)
+  // edges of u: (edge id, neighbour); the edge to the parent has u's id (the
+  // root's is its open end, neighbour -1), the edge to a child that child's
+  std::vector<std::pair<int, int>> edges(int u) const {
+    std::vector<std::pair<int, int>> e{{u, x.topo.parent[u]}};
+    for (int c : x.topo.children[u]) e.push_back({c, c});
+    return e;
+  }
+  std::vector<int> xlab(int u, int ks = K, int ss = S) const {
+    std::vector<int> l{lab(ss, u), lab(ks, u)};
+    for (int c : x.topo.children[u]) l.push_back(lab(ks, c));
+    return l;
+  }
+  LV xv(int u) const { return {x.t[u].as<double>(), x.shape(u), xlab(u)}; }
+  LV xbra(int u) const { return {x.t[u].as<double>(), x.shape(u), xlab(u, KP, SP)}; }
+  LV av(int u) const {
+    std::vector<int> shp = A.shape(u);
+    shp.erase(shp.begin());
+    shp.insert(shp.begin(), {d, d});  // fused site leg out * d + in
+    std::vector<int> l{lab(SP, u), lab(S, u), lab(W, u)};
+    for (int c : A.topo.children[u]) l.push_back(lab(W, c));
+    return {A.t[u].as<double>(), shp, l};
+  }
+  LV bv(int u) const {
+    std::vector<int> l{lab(S, u), lab(B, u)};
+    for (int c : b.topo.children[u]) l.push_back(lab(B, c));
+    return {b.t[u].as<double>(), b.shape(u), l};
+  }
+  // environments of the edge from a toward `to` (a is orthonormal toward it)
+  void env(int a, int to) {
+    const int e = to == x.topo.parent[a] ? a : to;
+    LT T{Dense{}, {}};
+    bool have = false;
+    auto cur = [&](const LV& base) { return have ? view(T) : base; };
+    const LV xa = xv(a);
+    for (auto [f, w] : edges(a)) {
+      if (f == e) continue;
+      LT n = lt_contract(ctx, cur(xa), view(EA.at({w, a})));
+      T = std::move(n);
+      have = true;
+    }
+    {
+      LT n = lt_contract(ctx, cur(xa), av(a));
+      T = std::move(n);
+      have = true;
+    }
+    LT n = lt_contract(ctx, view(T), xbra(a));
+    EA[{a, to}] = lt_perm(ctx, view(n), {lab(KP, e), lab(W, e), lab(K, e)});
+    if (!has_b) return;
+    have = false;
+    const LV ba = bv(a);
+    for (auto [f, w] : edges(a)) {
+      if (f == e) continue;
+      LT m = lt_contract(ctx, cur(ba), view(Eb.at({w, a})));
+      T = std::move(m);
+      have = true;
+    }
+    LT m = lt_contract(ctx, cur(ba), xa);
+    Eb[{a, to}] = lt_perm(ctx, view(m), {lab(K, e), lab(B, e)});
+  }
+  void open_end() {
+    LT ea{ones(ctx, {1, 1, 1}), {lab(KP, root), lab(W, root), lab(K, root)}};
+    EA[{-1, root}] = std::move(ea);
+    if (has_b) {
+      LT eb{ones(ctx, {1, 1}), {lab(K, root), lab(B, root)}};
+      Eb[{-1, root}] = std::move(eb);
+    }
+  }
+  // the external edges of the two-site block (u, c): (edge, neighbour, owner)
+  std::vector<std::array<int, 3>> outer(int u, int c) const {
+    std::vector<std::array<int, 3>> o;
+    for (auto [f, w] : edges(u))
+      if (f != c) o.push_back({f, w, u});
+    for (int g : x.topo.children[c]) o.push_back({g, g, c});
+    return o;
+  }
+  // y = a0 th + a1 H th for a two-site tensor with labels tl
+  void matvec(int u, int c, const std::vector<int>& tl, const std::vector<int>& ts, const double* th,
+              double* y, double a0, double a1) {
+    // u's environments, then A_u, then c's environments, then A_c: keeps the
+    // intermediate's order low on high-degree vertices
+    LT T{Dense{}, {}};
+    bool have = false;
+    const LV t0{th, ts, tl};
+    for (int side = 0; side < 2; ++side) {
+      const int owner = side == 0 ? u : c;
+      for (auto& o : outer(u, c)) {
+        if (o[2] != owner) continue;
+        LT n = lt_contract(ctx, have ? view(T) : t0, view(EA.at({o[1], o[2]})));
+        T = std::move(n);
+        have = true;
+      }
+      LT n = lt_contract(ctx, have ? view(T) : t0, av(owner));
+      T = std::move(n);
+      have = true;
+    }
+    // primed labels back to unprimed, axes in the order of th
+    for (int& l : T.lab) {
+      const int kind = l / V, id = l % V;
+      if (kind == SP) l = lab(S, id);
+      if (kind == KP) l = lab(K, id);
+    }
+    LT r = lt_perm(ctx, view(T), tl);
+    const int64_t n = numel(ts);
+    TNFA_CUDA(cudaMemcpyAsync(y, r.d.p(), n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (a1 != 1.0) {
+      k_scale_copy<<<grid_for(n, 256, 1024), 256, 0, ctx->stream>>>(y, y, n, a1);
+      TNFA_LAUNCH_CHECK();
+    }
+    if (a0 != 0.0) {
+      k_axpy<<<grid_for(n, 256, 1024), 256, 0, ctx->stream>>>(y, th, n, a0);
+      TNFA_LAUNCH_CHECK();
+    }
+  }
+  // two-site right-hand side with labels tl
+  LT rhs(int u, int c, const std::vector<int>& tl) {
+    LT T = lt_contract(ctx, bv(u), bv(c));
+    for (auto& o : outer(u, c)) {
+      LT n = lt_contract(ctx, view(T), view(Eb.at({o[1], o[2]})));
+      T = std::move(n);
+    }
+    return lt_perm(ctx, view(T), tl);
+  }
+  // update of edge (u, c) (c a child of u), the centre moving to c (down) or
+  // back to u; returns the local eigenvalue for dmrg
+  double update(int u, int c, bool down, double a0, double a1, const tnfa_trunc_params& tp, int kdim,
+                int restarts) {
+    LT th = lt_contract(ctx, xv(u), xv(c));
+    const std::vector<int> tl = th.lab, ts = th.d.shp;
+    const int64_t n64 = numel(ts);
+    TNFA_CHECK(n64 < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "tree solver: two-site problem too large");
+    const int n = (int)n64;
+    double E = 0.0;
+    MatVec H = [&](const double* in, double* out) { matvec(u, c, tl, ts, in, out, a0, a1); };
+    if (has_b) {
+      LT g = rhs(u, c, tl);
+      gmres(ctx, H, n, g.d.p(), th.d.p(), 40, 20, 1e-12);
+    } else {
+      E = lanczos_min(ctx, H, n, th.d.p(), kdim, restarts, 1e-12);
+    }
+    // split: rows are the side that keeps orthonormal columns
+    std::vector<int> ul{lab(S, u), lab(K, u)}, cl{lab(S, c)};
+    for (int w : x.topo.children[u])
+      if (w != c) ul.push_back(lab(K, w));
+    for (int g : x.topo.children[c]) cl.push_back(lab(K, g));
+    const std::vector<int>& rl = down ? ul : cl;
+    const std::vector<int>& kl = down ? cl : ul;
+    std::vector<int> order = rl;
+    order.insert(order.end(), kl.begin(), kl.end());
+    LT M = lt_perm(ctx, view(th), order);
+    int64_t rows = 1, cols = 1;
+    for (size_t i = 0; i < rl.size(); ++i) rows *= M.d.shp[i];
+    for (size_t i = rl.size(); i < order.size(); ++i) cols *= M.d.shp[i];
+    std::vector<la::FactorResult> res;
+    la::trunc_factor<double>(ctx, {la::FactorJob{M.d.p(), (int)rows, (int)cols}}, tp.cutoff, tp.maxdim,
+                             tp.mindim, TNFA_PREC_F64, res);
+    TNFA_CHECK(res[0].sweeps >= 0, TNFA_ERR_NOT_CONVERGED, "Jacobi SVD hit its sweep cap");
+    const int r = res[0].r;
+    std::vector<int> lshp(M.d.shp.begin(), M.d.shp.begin() + rl.size());
+    lshp.push_back(r);
+    std::vector<int> xshp{r};
+    xshp.insert(xshp.end(), M.d.shp.begin() + rl.size(), M.d.shp.end());
+    std::vector<int> llab = rl;
+    llab.push_back(lab(K, c));
+    std::vector<int> xlb{lab(K, c)};
+    xlb.insert(xlb.end(), kl.begin(), kl.end());
+    x.topo.link[c] = r;
+    const int ortho = down ? u : c, centre = down ? c : u;
+    LT no = lt_perm(ctx, LV{res[0].L.as<double>(), lshp, llab}, xlab(ortho));
+    LT nc = lt_perm(ctx, LV{res[0].X.as<double>(), xshp, xlb}, xlab(centre));
+    x.t[ortho] = std::move(no.d.b);
+    x.t[centre] = std::move(nc.d.b);
+    if (!has_b) {
+      // keep the state normalised after truncation: rescale the centre
+      const int64_t nn = x.size(centre);
+      const double nr = host_norm<double>(ctx, x.t[centre], nn);
+      if (nr > 0) {
+        k_scale_copy<<<grid_for(nn, 256, 1024), 256, 0, ctx->stream>>>(x.t[centre].as<double>(),
+                                                                         x.t[centre].as<double>(), nn, 1.0 / nr);
+        TNFA_LAUNCH_CHECK();
+      }
+    }
+    env(ortho, centre);
+    return E;
+  }
+  double tour(int u, double a0, double a1, const tnfa_trunc_params& tp, int kdim, int restarts) {
+    double E = 0.0;
+    for (int c : x.topo.children[u]) {
+      E = update(u, c, true, a0, a1, tp, kdim, restarts);
+      const double Ec = tour(c, a0, a1, tp, kdim, restarts);
+      if (!x.topo.children[c].empty()) E = Ec;
+      E = update(u, c, false, a0, a1, tp, kdim, restarts);
+    }
+    return E;
+  }
+  void init() {
+    orthogonalize_to_roots(x);  // every vertex orthonormal toward its parent, centre at the root
+    x.topo.finalize();
+    open_end();
+    for (int v = V - 1; v >= 0; --v)  // children have larger indices than their parent
+      if (v != root) env(v, x.topo.parent[v]);
+  }
+};
+
+bool path_shaped(const Topo& T) {
+  if (T.roots().size() != 1) return false;
+  for (int v = 0; v < T.V; ++v)
+    if ((int)T.children[v].size() + (T.parent[v] >= 0 ? 1 : 0) > 2) return false;
+  return true;
+}
+
+void check_tree_solve(const tnfa_net* A, const tnfa_net* f, const char* what) {
+  TNFA_CHECK(A->dtype == TNFA_F64 && f->dtype == TNFA_F64, TNFA_ERR_DTYPE,
+             std::string(what) + " works on FP64 networks");
+  check_same_tree(A->topo, f->topo, what);
+  TNFA_CHECK(f->topo.V >= 2 && f->topo.roots().size() == 1, TNFA_ERR_UNSUPPORTED,
+             std::string(what) + " needs one connected tree of at least two vertices");
+  TNFA_CHECK(f->topo.roots()[0] == 0, TNFA_ERR_TOPOLOGY, std::string(what) + ": the root must be vertex 0");
+  for (int v = 0; v < f->topo.V; ++v)
+    TNFA_CHECK(f->topo.nlegs[v] == 1, TNFA_ERR_UNSUPPORTED, std::string(what) + " needs one site leg per vertex");
+  for (int l = 0; l < f->topo.leg_off[f->topo.V]; ++l) {
+    TNFA_CHECK(A->topo.leg_kind[l] == TNFA_LEG_OPERATOR && f->topo.leg_kind[l] != TNFA_LEG_OPERATOR,
+               TNFA_ERR_INVALID_ARGUMENT, std::string(what) + ": an operator and a function");
+    TNFA_CHECK(f->topo.leg_dim[l] == f->topo.leg_dim[0] && A->topo.leg_dim[l] == f->topo.leg_dim[l] * f->topo.leg_dim[l],
+               TNFA_ERR_SHAPE, std::string(what) + ": site dimensions disagree");
+  }
+}
+
+tnfa_net* linsolve_tree(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnfa_net* x0,
+                        const tnfa_linsolve_params& prm, double* rel_res) {
+  check_tree_solve(A, b, "linsolve (A, b)");
+  check_same_tree(x0->topo, b->topo, "linsolve (x0, b)");
+  TNFA_CHECK(x0->dtype == TNFA_F64, TNFA_ERR_DTYPE, "linsolve works on FP64 networks");
+  TreeSolve S{ctx, b->topo.V, b->topo.leg_dim[0], 0, load_work<double>(ctx, x0), load_work<double>(ctx, A),
+              load_work<double>(ctx, b)};
+  const double bnorm = qr_norm(ctx, b);
+  TNFA_CHECK(bnorm > 0, TNFA_ERR_INVALID_ARGUMENT, "linsolve: b is zero");
+  S.init();
+  const tnfa_trunc_params tp{prm.cutoff, prm.maxdim, 1, 0, TNFA_PREC_F64};
+  double res = residual(ctx, A, b, S.x, prm.a0, prm.a1, bnorm);
+  for (int sweep = 0; sweep < prm.nsweeps && res > prm.tol; ++sweep) {
+    S.tour(S.root, prm.a0, prm.a1, tp, 0, 0);
+    res = residual(ctx, A, b, S.x, prm.a0, prm.a1, bnorm);
+  }
+  if (rel_res) *rel_res = res;
+  return store_work(S.x, TNFA_F64);
+}
+
+tnfa_net* dmrg_tree(tnfa_ctx* ctx, const tnfa_net* H, const tnfa_net* x0, const tnfa_dmrg_params& prm,
+                    double* energy) {
+  check_tree_solve(H, x0, "dmrg (H, psi0)");
+  TreeSolve S{ctx, x0->topo.V, x0->topo.leg_dim[0], 0, load_work<double>(ctx, x0), load_work<double>(ctx, H),
+              Work<double>{ctx, Topo{}, {}}};
+  S.has_b = false;
+  S.init();
+  const tnfa_trunc_params tp{prm.cutoff, prm.maxdim, 1, 0, TNFA_PREC_F64};
+  const int kd = prm.krylov_dim > 0 ? prm.krylov_dim : 30;
+  double E = 0.0, Eprev = 0.0;
+  for (int sweep = 0; sweep < std::max(1, prm.nsweeps); ++sweep) {
+    E = S.tour(S.root, 0.0, 1.0, tp, kd, std::max(0, prm.restarts));
+    if (sweep > 0 && std::fabs(E - Eprev) <= prm.tol * std::max(1.0, std::fabs(E))) break;
+    Eprev = E;
+  }
+  if (energy) *energy = E;
+  return store_work(S.x, TNFA_F64);
+}
+
+tnfa_net* linsolve_any(tnfa_ctx* ctx, const tnfa_net* A, const tnfa_net* b, const tnfa_net* x0,
+                       const tnfa_linsolve_params& prm, double* rel_res) {
+  return path_shaped(b->topo) ? linsolve_path(ctx, A, b, x0, prm, rel_res)
+                              : linsolve_tree(ctx, A, b, x0, prm, rel_res);
 }
 
 void inner_product(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_net* g, bool conjF, double* out) {
@@ -1960,7 +2343,8 @@ int tnfa_dmrg(tnfa_ctx* ctx, const tnfa_net* H, const tnfa_net* psi0, const tnfa
   TNFA_CHECK(params && psi, TNFA_ERR_INVALID_ARGUMENT, "null params or out");
   TNFA_CHECK(params->maxdim >= 0 && params->cutoff >= 0 && params->tol >= 0, TNFA_ERR_INVALID_ARGUMENT,
              "negative dmrg parameter");
-  *psi = dmrg_path(ctx, H, psi0, *params, energy);
+  *psi = path_shaped(psi0->topo) ? dmrg_path(ctx, H, psi0, *params, energy)
+                                 : dmrg_tree(ctx, H, psi0, *params, energy);
   TNFA_API_END
 }
 

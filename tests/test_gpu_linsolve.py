@@ -144,12 +144,68 @@ def test_maxdim_caps_solution(ina):
     assert np.isfinite(x.rel_residual) and x.rel_residual > 0
 
 
-def test_non_path_rejected(ina):
-    s = ina.continuous_siteinds(ina.named_binary_tree(7))
+@pytest.mark.parametrize("a0,a1", [(0.0, 1.0), (1.0, -1e-3)])
+def test_linsolve_binary_tree(ina, a0, a1):
+    """(a0 + a1 d2/dx2) x = b on a 7-vertex binary tree (the root has two
+    children, so the sweep is the tree tour, not the path one), against the
+    dense solve."""
+    L = 7
+    s = ina.continuous_siteinds(ina.named_binary_tree(L))
     b = ina.rand_itn(s, link_space=2, rng=74)
     A = ina.second_derivative_operator(s)
-    with pytest.raises(ina.TnfaError, match="path"):
-        ina.linsolve(A, b)
+    x = ina.linsolve(A, b, a0=a0, a1=a1, nsweeps=6, cutoff=0.0, tol=1e-12)
+    M = _dense_operator(O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2), L,
+                        {(1, k): k - 1 for k in range(1, L + 1)})
+    xs = _grid_1d(L)
+    err, res = _check(M, a0, a1, b.evaluate_batch(xs), x.evaluate_batch(xs), x.rel_residual)
+    assert res < 1e-10, (res, x.rel_residual)
+    assert err < 1e-8, err
+    assert abs(x.rel_residual - res) < 1e-11 + 1e-3 * res
+
+
+def _random_tree_laplacian(ina, n_vertices, seed):
+    """A uniformly random labelled tree with one digit per vertex and two
+    variables (continuous_siteinds(g; map_dimension=2)), and the dense
+    unscaled Laplacian on its 2^n grid."""
+    g = ina.uniform_tree(n_vertices, seed)
+    s = ina.continuous_siteinds(g, map_dimension=2)
+    L = n_vertices // 2
+    terms = (O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2, dim=1, scale=False)
+             + O.stencil_terms(L, [0.0, 1.0, -2.0, 1.0, 0.0], 2, dim=2, scale=False))
+    axis_of = {(1, k): k - 1 for k in range(1, L + 1)}
+    axis_of.update({(2, k): L + k - 1 for k in range(1, L + 1)})
+    return g, s, _dense_operator(terms, 2 * L, axis_of), L
+
+
+def test_dmrg_random_tree_laplace_example(ina):
+    """examples/2d_laplace_solver.jl: a random tree of 12 vertices
+    (uniform_tree(12)), two variables, the unscaled Laplacian, two-site DMRG
+    with maxdim 30 from a random start.  The energy is the lowest eigenvalue
+    of the dense stencil matrix and the state its eigenvector."""
+    g, s, M, L = _random_tree_laplacian(ina, 12, 1234)
+    assert max(len(list(g.neighbors(v))) for v in g.vertices()) >= 3  # not a path
+    A = ina.laplacian_operator(s, scale=False)
+    psi0 = ina.rand_itn(s, link_space=3, rng=80)
+    E, psi = ina.dmrg(A, psi0, nsweeps=15, maxdim=30, cutoff=1e-12)
+    w, V = np.linalg.eigh((M + M.T) / 2)
+    assert abs(E - w[0]) < 1e-8 * abs(w[0]), (E, w[:3])
+    v = psi.evaluate_batch(_grid_2d(L), [1, 2])
+    assert abs(abs(v @ V[:, 0]) / np.linalg.norm(v) - 1) < 1e-7
+    assert psi.maxlinkdim() <= 30
+
+
+def test_linsolve_random_tree(ina):
+    """(1 - 0.05 Laplacian) x = b on a random 10-vertex tree, against the dense
+    solve."""
+    g, s, M, L = _random_tree_laplacian(ina, 10, 7)
+    b = ina.rand_itn(s, link_space=2, rng=81)
+    A = ina.laplacian_operator(s, scale=False)
+    x = ina.linsolve(A, b, a0=1.0, a1=-0.05, nsweeps=8, cutoff=0.0, tol=1e-12)
+    X = _grid_2d(L)
+    err, res = _check(M, 1.0, -0.05, b.evaluate_batch(X, [1, 2]), x.evaluate_batch(X, [1, 2]),
+                      x.rel_residual)
+    assert res < 1e-10, (res, x.rel_residual)
+    assert err < 1e-9, err
 
 
 def test_dmrg_lowest_laplacian_mode(ina):
