@@ -306,6 +306,37 @@ int tnfa_net_gather(tnfa_ctx* ctx, const tnfa_net* f, const tnfa_topology* targe
 /* Element-type conversion: F64 <-> F32, F64 -> C128, F32 -> C128. */
 int tnfa_net_convert(tnfa_ctx* ctx, const tnfa_net* f, int dtype, tnfa_net** out);
 
+/* ---- operator construction ----------------------------------------------- */
+
+/* Boundary conditions of the shift operators (src/elementary_operators.jl:32-57). */
+typedef enum { TNFA_BC_DIRICHLET = 0, TNFA_BC_NEUMANN = 1, TNFA_BC_PERIODIC = 2 } tnfa_boundary;
+
+/* A sum of product terms as an operator network on the tree of `topo` (a
+ * function topology: digit legs of kind REAL or IMAG).  Term t has
+ * coefficient coefs[t] and n_factors[t] site factors, listed term after term:
+ * factor k acts on leg factor_leg[k] (index into topo's leg arrays) with the
+ * leg_dim x leg_dim matrix M[out][in] that follows in factor_mat (row-major,
+ * matrices back to back); legs without a factor carry the identity.  The
+ * terms form a direct sum (bond = number of terms, coefficients on vertex 0)
+ * compressed on the device by truncation with the relative cutoff, 64 terms
+ * at a time.  Replaces ITensorNetworks' ttn(OpSum, s; cutoff) as the
+ * reference calls it (src/elementary_operators.jl:114,119,151).  FP64. */
+int tnfa_op_from_terms(tnfa_ctx* ctx, const tnfa_topology* topo, int32_t n_terms, const double* coefs,
+                       const int32_t* n_factors, const int32_t* factor_leg, const double* factor_mat,
+                       double cutoff, tnfa_net** op);
+/* Finite-difference stencil along variable `dim` (base-2 digits) as an
+ * operator network: weights[5] multiply f(x + 2d), f(x + d), f(x), f(x - d),
+ * f(x - 2d); the forward shifts use right_bc and the backward ones left_bc
+ * (tnfa_boundary); scale != 0 multiplies every vertex with a digit of `dim`
+ * by 2^delta_power.  Replaces stencil (src/elementary_operators.jl:122-160)
+ * and with weights (0, 1/2, 0, -1/2, 0), power 1 / (0, 1, -2, 1, 0), 2 /
+ * (1/2, -1, 0, 1, -1/2), 3 / (1, -4, 6, -4, 1), 4 the first..fourth
+ * derivative operators (:162-176); laplacian_operator (:178-189) is the
+ * tnfa_add of the second derivatives of each variable. */
+int tnfa_op_build_stencil(tnfa_ctx* ctx, const tnfa_topology* topo, int32_t dim, const double* weights,
+                          int32_t delta_power, int32_t left_bc, int32_t right_bc, int32_t scale,
+                          double cutoff, tnfa_net** op);
+
 /* ---- operator application and truncation -------------------------------- */
 
 /* y = O f, contracted exactly site by site then truncated with `params`.

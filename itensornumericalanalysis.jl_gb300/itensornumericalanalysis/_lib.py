@@ -105,6 +105,8 @@ class LinsolveParams(C.Structure):
     ]
 
 
+BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC = 0, 1, 2
+
 _P = C.c_void_p
 _PP = C.POINTER(C.c_void_p)
 _I32 = C.c_int32
@@ -162,6 +164,14 @@ SIGNATURES = {
     "tnfa_add": (C.c_int, [_P, _P, _P, _PP]),
     "tnfa_multiply": (C.c_int, [_P, _P, _P, _PP]),
     "tnfa_operator_proj": (C.c_int, [_P, _P, _PP]),
+    "tnfa_op_from_terms": (
+        C.c_int,
+        [_P, C.POINTER(Topology), _I32, _PD, _PI32, _PI32, _PD, C.c_double, _PP],
+    ),
+    "tnfa_op_build_stencil": (
+        C.c_int,
+        [_P, C.POINTER(Topology), _I32, _PD, _I32, _I32, _I32, _I32, C.c_double, _PP],
+    ),
     "tnfa_apply": (C.c_int, [_P, _P, _P, C.POINTER(TruncParams), _PP]),
     "tnfa_apply_batched": (C.c_int, [_P, _I32, _PP, _PP, C.POINTER(TruncParams), _PP]),
     "tnfa_apply_exact": (C.c_int, [_P, _P, _P, _PP]),

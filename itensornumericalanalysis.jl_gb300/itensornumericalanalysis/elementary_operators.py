@@ -17,7 +17,7 @@ import numpy as np
 
 from . import _lib
 from .indexmap import IndsNetworkMap
-from .network import ITensorNetworkFunction
+from .network import ITensorNetworkFunction, topology_struct
 
 default_boundary = "Dirichlet"
 
@@ -157,6 +157,49 @@ def _site_op(s: IndsNetworkMap, v, ops: dict) -> np.ndarray:
 OPSUM_BLOCK = 64
 
 
+def _native_map(s: IndsNetworkMap) -> bool:
+    """Maps the library builds operators for directly (tnfa_op_from_terms /
+    tnfa_op_build_stencil): a tree (or forest) of real digit legs."""
+    return s.graph.is_forest() and not s.is_complex
+
+
+def _native_terms(s: IndsNetworkMap, terms, cutoff: float):
+    """tnfa_op_from_terms on real terms: None when a coefficient or a site
+    matrix is complex (those are assembled here and compressed on the
+    device)."""
+    if any(np.iscomplexobj(c) and np.imag(c) != 0 for c, _ in terms):
+        return None
+    lay = s.layout
+    legidx, k = {}, 0
+    for v in lay.order:
+        for l in s.legs[v]:
+            legidx[(l.dim, l.digit)] = (k, l.base)
+            k += 1
+    coefs, nf, fl, fm = [], [], [], []
+    for c, ops in terms:
+        items = [(key, op) for key, op in ops.items() if not (isinstance(op, str) and op == "I")]
+        coefs.append(float(np.real(c)))
+        nf.append(len(items))
+        for key, op in items:
+            if key not in legidx:
+                raise ValueError(f"no digit {key} in the index map")
+            leg, base = legidx[key]
+            m = _op_matrix(op, base)
+            if np.iscomplexobj(m) and np.any(np.imag(m) != 0):
+                return None
+            fl.append(leg)
+            fm.extend(np.real(m).astype(np.float64).ravel().tolist())
+    t, arrays = topology_struct(s, [1] * lay.n)
+    ctx = _lib.default_context()
+    h = C.c_void_p()
+    cd = (C.c_double * max(1, len(coefs)))(*coefs)
+    md = (C.c_double * max(1, len(fm)))(*fm)
+    nfa = (C.c_int32 * max(1, len(nf)))(*nf)
+    fla = (C.c_int32 * max(1, len(fl)))(*fl)
+    ctx.call("tnfa_op_from_terms", C.byref(t), len(coefs), cd, nfa, fla, md, float(cutoff), C.byref(h))
+    return ITensorNetworkOperator(s, h, ctx, operator_legs(s))
+
+
 def opsum_to_operator(s: IndsNetworkMap, opsum: OpSum, cutoff: float = 1e-15,
                       scale_dims: dict | None = None, compress: bool = True):
     """The OpSum as a tree operator (ITensorNetworks' ttn(OpSum; cutoff), used
@@ -164,10 +207,19 @@ def opsum_to_operator(s: IndsNetworkMap, opsum: OpSum, cutoff: float = 1e-15,
     of the product terms (bond = number of terms), coefficients on the first
     vertex, then compressed on the device by truncation with the relative
     cutoff.  Up to gauge this is the operator ttn(OpSum) returns; the ranks
-    are the SVD-minimal ones at that cutoff."""
+    are the SVD-minimal ones at that cutoff.  Real terms on a tree go through
+    the library's own builder (tnfa_op_from_terms); complex ones are
+    assembled here and compressed on the device the same way."""
     terms = opsum.terms
     if not terms:
         raise ValueError("an empty OpSum has no operator")
+    if compress and _native_map(s):
+        op = _native_terms(s, terms, cutoff)
+        if op is not None:
+            if scale_dims:
+                for v, f in scale_dims.items():
+                    op.scale_vertex(v, f)
+            return op
     if compress and len(terms) > OPSUM_BLOCK:
         op = None
         for b0 in range(0, len(terms), OPSUM_BLOCK):
@@ -244,6 +296,19 @@ def stencil(s: IndsNetworkMap, shifts: Sequence[float], delta_power: int, dim: i
     if len(shifts) != 5:
         raise ValueError("stencil needs 5 weights")
     b = s.base()
+    bcs = {"Dirichlet": _lib.BC_DIRICHLET, "Neumann": _lib.BC_NEUMANN, "Periodic": _lib.BC_PERIODIC}
+    for bc in (left_boundary, right_boundary):
+        if bc not in bcs:
+            raise ValueError(f"unknown boundary {bc!r}")
+    if _native_map(s) and b == 2:
+        # the library builds the carry-string terms and compresses them
+        t, arrays = topology_struct(s, [1] * s.layout.n)
+        ctx = _lib.default_context()
+        h = C.c_void_p()
+        w = (C.c_double * 5)(*[float(x) for x in shifts])
+        ctx.call("tnfa_op_build_stencil", C.byref(t), int(dim), w, int(delta_power),
+                 bcs[left_boundary], bcs[right_boundary], int(bool(scale)), float(cutoff), C.byref(h))
+        return ITensorNetworkOperator(s, h, ctx, operator_legs(s))
     ops = shifts[2] * no_shift_opsum(s)
     for i in (0, 1):
         if shifts[i] != 0:
