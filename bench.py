@@ -453,9 +453,20 @@ def secondary_measurements(ctx, ws, rank, args, f32net=None, f64net=None, Xd=Non
         X2 = np.random.default_rng(2).random((4096, 2))
         exact2 = -np.sin(np.pi * X2[:, 0]) * np.sin(np.pi * X2[:, 1]) / (2 * np.pi**2)
         got2 = x2.evaluate_batch(X2, [1, 2])
+        # the FP64 floor of any stored solution: each value of x carries a
+        # rounding of up to eps |x|, which the operator turns into a residual
+        # of eps || |A| |x| || / ||b|| (|A| = the stencil with absolute
+        # weights; x is one-signed here, so |A| |x| = |A| x up to sign)
+        absA = None
+        for d in (1, 2):
+            op = ina.stencil(s2, [0.0, 1.0, 2.0, 1.0, 0.0], 2, dim=d)
+            absA = op if absA is None else absA + op
+        floor2 = 2.0**-53 * ina.operate(absA, x2, cutoff=0.0).norm() / b2.norm()
         out["laplace_linsolve"] = {
             "value": t2, "unit": "s", "what": "linsolve(laplacian, sin(pi x) sin(pi y)), 2 sweeps, maxdim 40, cutoff 1e-20, 2 refinement steps",
-            "rel_residual": x2.rel_residual, "maxlinkdim": x2.maxlinkdim(),
+            "rel_residual": x2.rel_residual, "rel_residual_fp64_floor": floor2,
+            "floor_what": "eps_64 * || |A| |x| || / ||b||: the residual that rounding x to FP64 alone can cause",
+            "maxlinkdim": x2.maxlinkdim(),
             "max_err_vs_continuum": float(np.max(np.abs(got2 - exact2)) / np.max(np.abs(exact2))),
         }
     if want("config1"):

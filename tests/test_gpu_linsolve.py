@@ -273,3 +273,53 @@ def test_matrix_free_two_site_paths(ina):
     out = json.loads(r.stdout.strip().splitlines()[-1])
     assert out["lin_res"] < 1e-9 and out["lin_err"] < 1e-9, out
     assert abs(out["E"] - out["E_ref"]) < 1e-9 * abs(out["E_ref"]), out
+
+
+def test_laplace_residual_is_at_its_fp64_floor_2x12(ina):
+    """The Laplace workload at 2 x 12 bits (the 1/h^2 Laplacian, source
+    sin(pi x) sin(pi y)): the residual tnfa_linsolve reports equals the true
+    residual of the stored solution, measured on the dense 4096 x 4096 grid
+    in extended precision, and sits within a small factor of the FP64 floor
+    eps || |A| |x| || / ||b|| that rounding x to FP64 alone causes.  The same
+    floor, computed on the networks, is what bench.py reports at 2 x 16 bits,
+    where it lies above the 1e-8 the workload asks for."""
+    L = 12
+    g = ina.named_comb_tree((2, L))
+    s = ina.continuous_siteinds(g, [[(1, j) for j in range(L, 0, -1)],
+                                    [(2, j) for j in range(1, L + 1)]])
+    b = ina.sin_itn(s, k=np.pi, dim=1) * ina.sin_itn(s, k=np.pi, dim=2)
+    A = ina.laplacian_operator(s)
+    x = ina.linsolve(A, b, nsweeps=2, maxdim=40, cutoff=1e-20, tol=1e-12, refinements=3)
+    n = 2**L
+    P = _grid_2d(L)
+    X = x.evaluate_batch(P, [1, 2]).reshape(n, n)
+    B = b.evaluate_batch(P, [1, 2]).reshape(n, n)
+    # A X - B with Dirichlet zeros outside the grid, in extended precision
+    # (the factor 4^L is a power of two: exact)
+    Xl = X.astype(np.longdouble)
+    AX = -4.0 * Xl
+    AX[1:, :] += Xl[:-1, :]
+    AX[:-1, :] += Xl[1:, :]
+    AX[:, 1:] += Xl[:, :-1]
+    AX[:, :-1] += Xl[:, 1:]
+    AX *= np.longdouble(4.0) ** L
+    res_true = float(np.sqrt(np.sum((AX - B.astype(np.longdouble)) ** 2) / np.sum(B.astype(np.longdouble) ** 2)))
+    aX = np.abs(X)
+    absAX = 4.0 * aX
+    absAX[1:, :] += aX[:-1, :]
+    absAX[:-1, :] += aX[1:, :]
+    absAX[:, 1:] += aX[:, :-1]
+    absAX[:, :-1] += aX[:, 1:]
+    absAX *= 4.0**L
+    floor_dense = 2.0**-53 * np.linalg.norm(absAX) / np.linalg.norm(B)
+    # the floor on the networks (what bench.py computes at 16 bits)
+    absA = None
+    for d in (1, 2):
+        op = ina.stencil(s, [0.0, 1.0, 2.0, 1.0, 0.0], 2, dim=d)
+        absA = op if absA is None else absA + op
+    floor_net = 2.0**-53 * ina.operate(absA, x, cutoff=0.0).norm() / b.norm()
+    assert abs(floor_net - floor_dense) <= 1e-3 * floor_dense, (floor_net, floor_dense)
+    # the dense values come from an FP64 evaluation of the network, whose own
+    # rounding is of the order of the floor
+    assert abs(x.rel_residual - res_true) <= 0.5 * res_true + 2.0 * floor_dense, (x.rel_residual, res_true)
+    assert res_true <= 30.0 * floor_dense, (res_true, floor_dense)
