@@ -425,7 +425,7 @@ def secondary_measurements(ctx, ws, rank, args, f32net=None, f64net=None, Xd=Non
         out["mpo_apply_truncate"] = {
             "value": c5["mixed"]["value"], "unit": "MPS/s", "batch": args.mps,
             "scaling": "strong (LPT split of the batch over the ranks)" if ws > 1 else None,
-            "precision": "mixed (FP32-preconditioned Jacobi, FP64 polish, FP64 rank-revealing QR)",
+            "precision": "mixed (FP32-preconditioned Jacobi, double-float polish, FP64 rank-revealing QR)",
             "mixed": c5["mixed"], "fp64_batched": c5["f64"], "fp64_plain": plain,
             "mixed_over_fp64_plain": c5["mixed"]["value"] / plain["value"],
             "mixed_over_fp64_batched": c5["mixed"]["value"] / c5["f64"]["value"],

@@ -60,7 +60,8 @@ typedef enum {
   TNFA_PREC_MIXED = 2,     /* FP64 messages; two-child vertices (bonds 64/128) as exact
                               products of 8-bit integer slices on the tcgen05 tensor cores
                               (26 BF16 passes, FP32 accumulation exact), FP64-class result.
-                              In truncation: FP32-preconditioned Jacobi with FP64 polish.  */
+                              In truncation: FP32-preconditioned Jacobi with a
+                              double-float (FP32 pair) polish.                             */
   TNFA_PREC_MIXED_FAST = 3 /* FP32 messages, tcgen05 split-BF16 (hi/lo, 3 passes) products:
                               about 1e-5 relative (norm-wise) on random bond-128 trees     */
 } tnfa_precision;

@@ -26,6 +26,66 @@ namespace cg = cooperative_groups;
 namespace tnfa {
 namespace la {
 
+// ------------------------------------------------------ double-float --
+// x = hi + lo (FP32 pair, |lo| <= ulp(hi) / 2): about 48 significant bits
+// from FP32 arithmetic, with the error-free sum of Knuth (TAOCP vol. 2,
+// 4.2.2) and the error-free product by FMA (after Dekker 1971); division and
+// square root take one Newton correction of the FP32 quotient / root.  Used
+// where GB300's FP64 rate (1/64 of its FP32 rate) would bound a kernel; the
+// range is FP32's, so callers scale by powers of two.
+struct dfl {
+  float hi, lo;
+  __host__ __device__ dfl() : hi(0.f), lo(0.f) {}
+  __host__ __device__ constexpr dfl(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ dfl(int x) : hi((float)x), lo(0.f) {}
+  __host__ __device__ explicit dfl(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+  __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ dfl df_fast2sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dfl df_2sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ dfl operator+(dfl a, dfl b) {
+  const dfl s = df_2sum(a.hi, b.hi);
+  return df_fast2sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ dfl operator-(dfl a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+__device__ __forceinline__ dfl& operator+=(dfl& a, dfl b) { return a = a + b; }
+__device__ __forceinline__ dfl operator*(dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_fast2sum(p, e);
+}
+__device__ __forceinline__ dfl operator/(dfl a, dfl b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const dfl r = a - b * dfl(q1, 0.f);
+  return df_fast2sum(q1, __fdiv_rn(r.hi, b.hi));
+}
+__device__ __forceinline__ bool operator<(dfl a, dfl b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(dfl a, dfl b) { return b < a; }
+__device__ __forceinline__ bool operator<=(dfl a, dfl b) { return !(b < a); }
+__device__ __forceinline__ bool operator>=(dfl a, dfl b) { return !(a < b); }
+__device__ __forceinline__ bool operator==(dfl a, dfl b) { return a.hi == b.hi && a.lo == b.lo; }
+using ::fabs;
+using ::sqrt;
+__device__ __forceinline__ dfl fabs(dfl a) { return a.hi < 0.f ? -a : a; }
+__device__ __forceinline__ dfl sqrt(dfl a) {
+  if (!(a.hi > 0.f)) return dfl(0.f, 0.f);
+  const float x = __fsqrt_rn(a.hi);
+  const float xx = __fmul_rn(x, x);
+  const dfl r = a - dfl(xx, __fmaf_rn(x, x, -xx));
+  return df_fast2sum(x, __fdiv_rn(r.hi, __fmul_rn(2.f, x)));
+}
+
+
 // ---------------------------------------------------------- scalar ops --
 __host__ __device__ inline double re(double x) { return x; }
 __host__ __device__ inline double re(cplx x) { return x.re; }
@@ -62,6 +122,16 @@ __device__ inline double phase(double x) { return x < 0 ? -1.0 : 1.0; }
 __device__ inline cplx phase(cplx x) {
   double a = hypot(x.re, x.im);
   return a > 0 ? cplx{x.re / a, x.im / a} : cplx{1.0, 0.0};
+}
+__device__ inline dfl re(dfl x) { return x; }
+__device__ inline dfl abs2(dfl x) { return x * x; }
+__device__ inline dfl conj(dfl x) { return x; }
+__device__ inline dfl scal(dfl x, dfl a) { return x * a; }
+template <> __host__ __device__ inline dfl from_real<dfl>(double a) { return dfl(a); }
+__device__ inline dfl absval(dfl x) { return fabs(x); }
+__device__ inline dfl phase(dfl x) { return x.hi < 0.f ? dfl(-1) : dfl(1); }
+__device__ inline dfl shfl_xor(dfl v, int o) {
+  return {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
 }
 
 template <class Job>
@@ -226,9 +296,15 @@ __device__ inline cplx ldcg(const cplx* p) {
 __device__ inline void stcg(double* p, double v) { __stcg(p, v); }
 __device__ inline void stcg(float* p, float v) { __stcg(p, v); }
 __device__ inline void stcg(cplx* p, cplx v) { __stcg((double2*)p, make_double2(v.re, v.im)); }
+__device__ inline dfl ldcg(const dfl* p) {
+  const float2 v = __ldcg((const float2*)p);
+  return {v.x, v.y};
+}
+__device__ inline void stcg(dfl* p, dfl v) { __stcg((float2*)p, make_float2(v.hi, v.lo)); }
 __device__ inline float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ inline double fmaT(double a, double b, double c) { return fma(a, b, c); }
 __device__ inline cplx fmaT(cplx a, cplx b, cplx c) { return Sc<cplx>::fma(a, b, c); }
+__device__ inline dfl fmaT(dfl a, dfl b, dfl c) { return a * b + c; }
 
 // ------------------------------------------------------------------ qr --
 template <class T>
@@ -792,6 +868,19 @@ __device__ inline void rr_pair(int n2, int r, int i, int& p, int& q) {
 // drops all of it, and decides exactly like on the full decomposition.
 template <class T> struct RealOf { using type = double; };
 template <> struct RealOf<float> { using type = float; };
+template <> struct RealOf<dfl> { using type = dfl; };
+
+// Per arithmetic: unit roundoff, the weight (relative to |A|_F^2) below which
+// a column is rounding noise, and the largest |zeta| handled directly.
+template <class R> struct JacobiTraits {
+  static constexpr double eps = 2.220446049250313e-16, negl = 1e-30, big = 1e150;
+};
+template <> struct JacobiTraits<float> {
+  static constexpr double eps = 1.1920929e-7, negl = 1e-13, big = 1e18;
+};
+template <> struct JacobiTraits<dfl> {  // 2^-46: the pair arithmetic's error with some margin
+  static constexpr double eps = 1.4210854715202004e-14, negl = 1e-26, big = 1e18;
+};
 
 struct JacobiOpts {
   double stop_rel;   // sweep-level stop threshold (relative |g| / sqrt(a b))
@@ -845,9 +934,9 @@ __global__ void __launch_bounds__(512) k_jacobi(const SvdJob* __restrict__ jobs,
   double part = 0.0;
   for (int64_t i = threadIdx.x; i < (int64_t)m * n; i += blockDim.x) part += (double)abs2(A[i]);
   const double fro2 = block_sum<double>(part, red);
-  const double eps = sizeof(R) == 4 ? 1.1920929e-7 : 2.220446049250313e-16;
+  const double eps = JacobiTraits<R>::eps;
   // columns below this are rounding noise of the whole matrix
-  const double negl = (sizeof(R) == 4 ? 1e-13 : 1e-30) * fro2;
+  const double negl = JacobiTraits<R>::negl * fro2;
   const R tol = (R)(8.0 * sqrt((double)m) * eps);
   const R stop = (R)fmax((double)tol, opt.stop_rel);
   // pairs of columns both below this are left alone (deflation for truncation)
@@ -900,7 +989,7 @@ __global__ void __launch_bounds__(512) k_jacobi(const SvdJob* __restrict__ jobs,
         if (ag > stop * nab) busy = 1;
         if (ag <= tol * nab || ag == (R)0) continue;
         const R zeta = (b - a) / ((R)2 * ag);
-        const R big = sizeof(R) == 4 ? (R)1e18 : (R)1e150;
+        const R big = (R)JacobiTraits<R>::big;
         const R t = fabs(zeta) > big ? (R)0.5 / zeta
                                      : (zeta >= 0 ? (R)1 : (R)-1) / (fabs(zeta) + sqrt((R)1 + zeta * zeta));
         if (t == (R)0) continue;
@@ -1572,6 +1661,8 @@ __device__ inline double cvt(double x, double*) { return x; }
 __device__ inline float cvt(double x, float*) { return (float)x; }
 __device__ inline double cvt(float x, double*) { return (double)x; }
 __device__ inline cplx cvt(cplx x, cplx*) { return x; }
+__device__ inline dfl cvt(double x, dfl*) { return dfl(x); }
+__device__ inline double cvt(dfl x, double*) { return (double)x; }
 
 template <class S, class D>
 __global__ void k_copy_block(const CopyJob* __restrict__ jobs) {
@@ -1719,6 +1810,7 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
   const JacobiOpts polish{1e-6, opts.small_rel};
   // (2) Jacobi on the core: U (cm x ku); extra[q] = weight outside U's span
   std::vector<double> extra(nj, 0.0);
+  std::vector<double> polish_scale;  // mixed: sum of squares of each polish input
   std::vector<SvdJob> sj;
   if (!mixed) {
     for (size_t q = 0; q < nj; ++q) {
@@ -1836,11 +1928,34 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     }
     TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
     for (size_t q = 0; q < nj; ++q) extra[q] = std::max(0.0, ss_in[q] - ss_kept[q]);
-    for (size_t q = 0; q < nj; ++q) {
-      U[q] = DBuf(ctx, (size_t)cm[q] * ku[q] * sizeof(T));
-      sj.push_back({X[q].p, U[q].p, S_of(q), nullptr, cm[q], ku[q], sw_of(q)});
+    // The polish in double-float (FP32 pairs, ~48 bits) on the FP32 pipe:
+    // X is scaled by a power of two to unit size on the way in, U comes back
+    // to FP64, and the singular values are scaled back on the host.
+    DBuf ssx(ctx, nj * sizeof(double));
+    {
+      std::vector<SumsqJob> sq;
+      for (size_t q = 0; q < nj; ++q) sq.push_back({X[q].p, (int64_t)cm[q] * ku[q], ssx.as<double>() + q});
+      DBuf dq = upload(ctx, sq);
+      k_sumsq<<<(unsigned)nj, 256, 0, ctx->stream>>>(dq.as<SumsqJob>());
+      TNFA_LAUNCH_CHECK();
     }
-    jacobi<T>(ctx, sj, 60, polish, "svd_polish_f64");
+    std::vector<DBuf> Xd(nj), Ud(nj);
+    std::vector<CopyJob> dn, upj;
+    for (size_t q = 0; q < nj; ++q) {
+      const size_t ne = (size_t)cm[q] * ku[q];
+      Xd[q] = DBuf(ctx, ne * sizeof(dfl));
+      Ud[q] = DBuf(ctx, ne * sizeof(dfl));
+      U[q] = DBuf(ctx, ne * sizeof(T));
+      dn.push_back({X[q].p, Xd[q].p, cm[q], ku[q], ku[q], ku[q], 0, 0, ssx.as<double>() + q});
+      sj.push_back({Xd[q].p, Ud[q].p, S_of(q), nullptr, cm[q], ku[q], sw_of(q)});
+      upj.push_back({Ud[q].p, U[q].p, cm[q], ku[q], ku[q], ku[q], 0, 0});
+    }
+    copy_blocks<double, dfl>(ctx, dn);
+    jacobi<dfl>(ctx, sj, 60, polish, "svd_polish_df");
+    copy_blocks<dfl, double>(ctx, upj);
+    polish_scale.resize(nj);
+    TNFA_CUDA(cudaMemcpyAsync(polish_scale.data(), ssx.p, nj * sizeof(double), cudaMemcpyDeviceToHost,
+                              ctx->stream));
     // Diagnostics (TNFA_DEBUG_DIR with TNFA_DEBUG_SWEEPS=k): the FP64 core of
     // every mixed job whose polish took k sweeps or more, with its polish input
     static const char* dbg = getenv("TNFA_DEBUG_DIR");
@@ -1870,6 +1985,8 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     }
   }
   // (3) ranks on the host (one read-back of every job's values and sweeps)
+  if (!polish_scale.empty())
+    TNFA_CUDA(cudaStreamSynchronize(ctx->stream));  // polish_scale arrives with the values
   {
     std::vector<double> hs(soff[nj]);
     std::vector<int> hsw(nj);
@@ -1880,6 +1997,12 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     for (size_t q = 0; q < nj; ++q) {
       out[q].s.assign(hs.begin() + soff[q], hs.begin() + soff[q] + ku[q]);
       out[q].sweeps = hsw[q];
+      if (!polish_scale.empty()) {
+        // undo the power of two the polish input was scaled by
+        const double f = std::sqrt(polish_scale[q]);
+        const double back = f > 0 && std::isfinite(f) ? std::ldexp(1.0, std::ilogb(f)) : 1.0;
+        for (double& x : out[q].s) x *= back;
+      }
     }
   }
   std::vector<GemmJob> gl, gx;

@@ -80,8 +80,9 @@ bool lu_solve(tnfa_ctx* ctx, double* A, double* b, int n);
 // M^H = QR) is diagonalised by one-sided Jacobi without accumulating V:
 // L = Q U_r (or U_r) and X = U_r^H R (or U_r^H M).  precision MIXED / F32
 // (real FP64 only): Jacobi first runs in FP32 with V accumulated, V is
-// re-orthonormalised in FP64 (two Newton-Schulz steps), and FP64 Jacobi on
-// J V polishes U and the singular values to FP64 accuracy in a few sweeps.
+// re-orthonormalised in FP64 (two Newton-Schulz steps), and Jacobi on J V
+// in double-float (FP32 pairs, about 48 bits, on the FP32 pipe) polishes U
+// and the singular values in a few sweeps.
 struct FactorJob {
   void* M;
   int rows, cols;
