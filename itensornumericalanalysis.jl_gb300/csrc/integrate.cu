@@ -358,11 +358,25 @@ __global__ void __launch_bounds__(INT_THREADS, 1) k_integrate(const T* __restric
   const int sidx = (warp - 1) / INT_CPS, part = (warp - 1) % INT_CPS;
   const T* sbuf = (const T*)(stages + (size_t)sidx * INT_STAGE_BYTES);
   int ready_vi = -1;
+  // The completion count of a task is read after the next fill has arrived
+  // (the atomic's round trip overlaps the copy); the warp that completed a
+  // vertex finishes it then.
+  int pend_vi = -1, pend_old = 0;
+  auto settle = [&]() {
+    if (pend_vi < 0) return;
+    int fin = 0;
+    if (lane == 0) fin = pend_old == (int)(vt[pend_vi].ntask * INT_CPS - 1);
+    fin = __shfl_sync(0xffffffffu, fin, 0);
+    if (fin) integrate_finish<T>(vt[pend_vi], st);
+    pend_vi = -1;
+  };
   for (int n = 0;; ++n) {
     if (!mbar_wait(&full[sidx], n & 1, st.wait_limit)) {
       if (lane == 0) atomicOr(st.err, 1);
+      settle();
       break;
     }
+    settle();
     const IntSlot sl = slot[sidx];
     if (sl.t < 0) break;
     const IntVertex& iv = vt[sl.vi];
@@ -484,15 +498,13 @@ __global__ void __launch_bounds__(INT_THREADS, 1) k_integrate(const T* __restric
         partial = partial + __shfl_xor_sync(0xffffffffu, partial, o);
       }
     }
-    int finished = 0;
     if (lane == 0) {
       atomicAddAcc(&st.msgs[(int64_t)iv.v * st.chimax + sl.a], mulw(to_acc(partial, A{}), iv.w));
-      int old;
-      asm volatile("atom.add.acq_rel.gpu.global.s32 %0, [%1], 1;" : "=r"(old) : "l"(st.done + iv.v) : "memory");
-      finished = old == (int)(iv.ntask * INT_CPS - 1);
+      // release: the message add is visible before the count; the finisher
+      // acquires (integrate_finish begins with a fence)
+      asm volatile("atom.add.release.gpu.global.s32 %0, [%1], 1;" : "=r"(pend_old) : "l"(st.done + iv.v) : "memory");
     }
-    finished = __shfl_sync(0xffffffffu, finished, 0);
-    if (finished) integrate_finish<T>(iv, st);
+    pend_vi = sl.vi;
   }
 }
 
