@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <cstdio>
@@ -269,8 +270,22 @@ inline unsigned grid_for(int64_t n, int block, int cap = 1 << 20) {
 }  // namespace tnfa
 
 // Entry-point wrappers: map exceptions to statuses, record the message.
-#define TNFA_API_BEGIN(ctxp) \
-  tnfa_ctx* __tnfa_ctx = (ctxp); \
+// Every entry point is an NVTX range named after the function, so a
+// profiler's timeline (ncu --nvtx, Nsight Systems) shows the C-ABI calls
+// around their kernels; without a profiler attached the push / pop cost a
+// branch each.
+namespace tnfa {
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+}  // namespace tnfa
+
+#define TNFA_API_BEGIN(ctxp)              \
+  tnfa::NvtxRange __tnfa_nvtx(__func__); \
+  tnfa_ctx* __tnfa_ctx = (ctxp);         \
   try {
 #define TNFA_API_END                                                   \
   }                                                                    \
