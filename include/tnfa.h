@@ -338,6 +338,23 @@ int tnfa_op_build_stencil(tnfa_ctx* ctx, const tnfa_topology* topo, int32_t dim,
                           int32_t delta_power, int32_t left_bc, int32_t right_bc, int32_t scale,
                           double cutoff, tnfa_net** op);
 
+/* ---- interpolation ------------------------------------------------------- */
+
+/* Cross approximation (adaptive cross with full pivoting) of one sampled
+ * block M (rows x cols, row-major FP64, host or device memory per `mem`):
+ * repeatedly the entry of largest magnitude of the residual (the smallest
+ * flat index among equal ones) becomes a pivot unless it is at most
+ * tol * max|M|, and the residual loses its rank-one cross; at most maxrank
+ * pivots.  piv_rows / piv_cols receive the pivots in order (room for
+ * min(maxrank, rows, cols)), *rank their number, err[0] the largest residual
+ * entry left (the rejected pivot, or the whole residual's maximum when the
+ * rank cap was reached) and err[1] = max|M|.  The factorisation step of the
+ * two-site tensor cross interpolation that ITensorTCI runs for the
+ * reference's TCI extension (ext/ITensorNumericalAnalysisTCIExt/
+ * tci_util.jl:21-55). */
+int tnfa_cross(tnfa_ctx* ctx, const double* block, int mem, int32_t rows, int32_t cols, double tol,
+               int32_t maxrank, int32_t* piv_rows, int32_t* piv_cols, int32_t* rank, double* err);
+
 /* ---- operator application and truncation -------------------------------- */
 
 /* y = O f, contracted exactly site by site then truncated with `params`.

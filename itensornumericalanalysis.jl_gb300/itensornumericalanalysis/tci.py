@@ -19,29 +19,30 @@ vectorised NumPy function can be interpolated.
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
+
+from . import _lib
 
 
 def _aca_full(M: np.ndarray, tol: float, maxrank: int):
-    """Cross (adaptive cross approximation with full pivoting) of M: pivot rows
-    and columns, and the largest entry left in the residual."""
-    R = np.array(M, dtype=np.result_type(M, float), copy=True)
-    scale = np.max(np.abs(M)) if M.size else 0.0
-    rows, cols = [], []
-    err = scale
-    while len(rows) < min(maxrank, *M.shape):
-        k = int(np.argmax(np.abs(R)))
-        i, j = divmod(k, R.shape[1])
-        piv = R[i, j]
-        err = abs(piv)
-        if scale == 0.0 or err <= tol * scale:
-            break
-        rows.append(i)
-        cols.append(j)
-        R = R - np.outer(R[:, j], R[i, :]) / piv
-    if len(rows) == min(maxrank, *M.shape):
-        err = float(np.max(np.abs(R))) if R.size else 0.0
-    return rows, cols, float(err), float(scale)
+    """Cross (adaptive cross approximation with full pivoting) of the sampled
+    block M on the device (tnfa_cross): pivot rows and columns, the largest
+    entry left in the residual, and max|M|."""
+    M = np.ascontiguousarray(np.asarray(M, dtype=np.float64))
+    rows, cols = M.shape
+    if M.size == 0:
+        return [], [], 0.0, 0.0
+    k = max(0, min(int(maxrank), rows, cols))
+    pr = (C.c_int32 * max(k, 1))()
+    pc = (C.c_int32 * max(k, 1))()
+    rk = C.c_int32(0)
+    err = (C.c_double * 2)()
+    _lib.default_context().call("tnfa_cross", M.ctypes.data_as(C.c_void_p), _lib.MEM_HOST, rows, cols,
+                                float(tol), int(maxrank), pr, pc, C.byref(rk), err)
+    n = rk.value
+    return list(pr[:n]), list(pc[:n]), float(err[0]), float(err[1])
 
 
 class _PathSampler:

@@ -21,7 +21,7 @@ __all__ = [
     "delta_p", "random_net", "net_add", "net_multiply", "net_scale",
     "evaluate", "evaluate_batch", "integrate", "dense", "dense_grid_1d",
     "forward_shift_terms", "backward_shift_terms", "stencil_terms", "apply_terms_dense",
-    "bond_spectrum", "gradient",
+    "bond_spectrum", "gradient", "aca_full",
 ]
 
 _next_id = itertools.count()
@@ -741,3 +741,32 @@ def gradient(f: Net, X, dims, dout) -> dict:
             idx = tuple(iv[i] for i in f.s.site[v])
             out[v][idx] += w * env.arr
     return out
+
+
+def aca_full(M: np.ndarray, tol: float, maxrank: int):
+    """Cross of a sampled block by adaptive cross approximation with full
+    pivoting (the factorisation step of the two-site TCI that ITensorTCI runs
+    for the reference's TCI extension, ext/ITensorNumericalAnalysisTCIExt/
+    tci_util.jl:21-55; ITensorTCI is not part of the reference, so this
+    restates the published algorithm): the entry of largest magnitude of the
+    residual (first in row-major order among equal ones) becomes a pivot
+    unless it is at most tol * max|M|, and the residual loses its rank-one
+    cross R[:, j] R[i, :] / R[i, j].  Returns pivot rows, pivot columns, the
+    largest residual entry left and max|M|."""
+    R = np.array(M, dtype=np.result_type(M, float), copy=True)
+    scale = np.max(np.abs(M)) if M.size else 0.0
+    rows, cols = [], []
+    err = scale
+    while len(rows) < min(maxrank, *M.shape):
+        k = int(np.argmax(np.abs(R)))
+        i, j = divmod(k, R.shape[1])
+        piv = R[i, j]
+        err = abs(piv)
+        if scale == 0.0 or err <= tol * scale:
+            break
+        rows.append(i)
+        cols.append(j)
+        R = R - np.outer(R[:, j], R[i, :]) / piv
+    if len(rows) == min(maxrank, *M.shape):
+        err = float(np.max(np.abs(R))) if R.size else 0.0
+    return rows, cols, float(err), float(scale)

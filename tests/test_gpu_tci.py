@@ -46,3 +46,27 @@ def test_interpolate_binary_tree_3d(ina):
     X = np.floor(np.random.default_rng(3).random((4000, 3)) * 2**15) / 2**15
     assert np.max(np.abs(g.evaluate_batch(X, [1, 2, 3]) - f(X))) < 1e-9
     assert g.maxlinkdim() <= 16
+
+
+@pytest.mark.parametrize("shape,rank", [((30, 40), 3), ((64, 64), 64), ((128, 96), 20), ((200, 150), 7)])
+def test_device_cross_matches_oracle(ina, shape, rank):
+    """tnfa_cross (one CTA on the device, residual in shared memory or, for
+    the largest block, in global memory) against the oracle's cross: the same
+    pivots in the same order and the same residual, on low-rank, full-rank and
+    rank-capped blocks."""
+    from itensornumericalanalysis.tci import _aca_full
+
+    import oracle as O
+
+    rng = np.random.default_rng(95 + rank)
+    m, n = shape
+    M = rng.standard_normal((m, rank)) @ rng.standard_normal((rank, n))
+    for tol, cap in ((1e-12, 64), (1e-3, 64), (1e-12, 5), (0.0, 0)):
+        got = _aca_full(M, tol, cap)
+        ref = O.aca_full(M, tol, cap)
+        assert got[0] == ref[0] and got[1] == ref[1], (tol, cap)
+        assert got[2] == ref[2] and got[3] == ref[3], (got[2:], ref[2:])
+    # ties: a block of equal magnitudes takes the first in row-major order
+    T = np.ones((5, 7))
+    T[2, 3] = -1.0
+    assert _aca_full(T, 0.0, 3)[:2] == O.aca_full(T, 0.0, 3)[:2]

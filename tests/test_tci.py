@@ -1,11 +1,24 @@
-"""Tensor cross interpolation: the cross (host) part on CPU."""
+"""Tensor cross interpolation: the sweep logic on CPU, with the oracle's
+cross (numpy) standing in for the device's tnfa_cross (compared with each
+other in tests/test_gpu_tci.py)."""
 import sys
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 sys.path.insert(0, str(Path(__file__).resolve().parent.parent / "itensornumericalanalysis.jl_gb300"))
-from itensornumericalanalysis.tci import _aca_full, tci_path  # noqa: E402
+sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
+import oracle as O  # noqa: E402
+from itensornumericalanalysis import tci as _tci  # noqa: E402
+from itensornumericalanalysis.tci import tci_path  # noqa: E402
+
+_aca_full = O.aca_full
+
+
+@pytest.fixture(autouse=True)
+def _oracle_cross(monkeypatch):
+    monkeypatch.setattr(_tci, "_aca_full", O.aca_full)
 
 
 def _mps_values(cores, idx):
