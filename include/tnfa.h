@@ -334,6 +334,16 @@ int tnfa_op_from_terms(tnfa_ctx* ctx, const tnfa_topology* topo, int32_t n_terms
  * (1/2, -1, 0, 1, -1/2), 3 / (1, -4, 6, -4, 1), 4 the first..fourth
  * derivative operators (:162-176); laplacian_operator (:178-189) is the
  * tnfa_add of the second derivatives of each variable. */
+/* The stencil's product terms without building the operator (no context, no
+ * device): the layout tnfa_op_from_terms takes (2 x 2 factor matrices), the
+ * identity term first, before the 2^delta_power vertex scaling.  *n_terms
+ * and *n_factors_total always receive the counts; the arrays are filled only
+ * when max_terms / max_factors are large enough (call once with 0 to size
+ * them). */
+int tnfa_op_stencil_terms(const tnfa_topology* topo, int32_t dim, const double* weights, int32_t left_bc,
+                          int32_t right_bc, int32_t max_terms, int32_t max_factors, double* coefs,
+                          int32_t* n_factors, int32_t* factor_leg, double* factor_mat, int32_t* n_terms,
+                          int32_t* n_factors_total);
 int tnfa_op_build_stencil(tnfa_ctx* ctx, const tnfa_topology* topo, int32_t dim, const double* weights,
                           int32_t delta_power, int32_t left_bc, int32_t right_bc, int32_t scale,
                           double cutoff, tnfa_net** op);

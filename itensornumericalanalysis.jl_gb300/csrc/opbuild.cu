@@ -261,6 +261,51 @@ int tnfa_op_from_terms(tnfa_ctx* ctx, const tnfa_topology* topo, int32_t n_terms
   TNFA_API_END
 }
 
+namespace {
+// The stencil's product terms (src/elementary_operators.jl:122-160, before
+// the base^power scaling, which acts on vertices).
+std::vector<Term> stencil_terms(const Topo& F, int dim, const double* weights, int left_bc, int right_bc) {
+  TNFA_CHECK(F.roots().size() == 1, TNFA_ERR_UNSUPPORTED, "shift operators need a tree");
+  const Digits D = digits_of(F, dim);
+  std::vector<Term> terms;
+  terms.push_back(Term{weights[2], {}});  // the identity, always present (possibly 0)
+  for (int i = 0; i < 2; ++i)
+    if (weights[i] != 0) shift_terms(D, i == 0 ? 1 : 0, true, right_bc, weights[i], terms);
+  for (int i = 3; i < 5; ++i)
+    if (weights[i] != 0) shift_terms(D, i == 4 ? 1 : 0, false, left_bc, weights[i], terms);
+  return terms;
+}
+}  // namespace
+
+int tnfa_op_stencil_terms(const tnfa_topology* topo, int32_t dim, const double* weights, int32_t left_bc,
+                          int32_t right_bc, int32_t max_terms, int32_t max_factors, double* coefs,
+                          int32_t* n_factors, int32_t* factor_leg, double* factor_mat, int32_t* n_terms,
+                          int32_t* n_factors_total) {
+  TNFA_API_BEGIN(nullptr);
+  TNFA_CHECK(topo && weights && n_terms && n_factors_total, TNFA_ERR_INVALID_ARGUMENT,
+             "op_stencil_terms: null argument");
+  const Topo F = topo_from_abi(topo);
+  const std::vector<Term> terms = stencil_terms(F, dim, weights, left_bc, right_bc);
+  int64_t nf = 0;
+  for (const Term& t : terms) nf += (int64_t)t.f.size();
+  *n_terms = (int32_t)terms.size();
+  *n_factors_total = (int32_t)nf;
+  if (max_terms < (int)terms.size() || max_factors < nf) return TNFA_OK;  // sizes only
+  TNFA_CHECK(coefs && n_factors && (nf == 0 || (factor_leg && factor_mat)), TNFA_ERR_INVALID_ARGUMENT,
+             "op_stencil_terms: null output");
+  int64_t k = 0;
+  for (size_t t = 0; t < terms.size(); ++t) {
+    coefs[t] = terms[t].coef;
+    n_factors[t] = (int32_t)terms[t].f.size();
+    for (const Factor& f : terms[t].f) {
+      factor_leg[k] = f.leg;
+      std::copy(f.m.begin(), f.m.end(), factor_mat + 4 * k);  // base 2: 2 x 2 each
+      ++k;
+    }
+  }
+  TNFA_API_END
+}
+
 int tnfa_op_build_stencil(tnfa_ctx* ctx, const tnfa_topology* topo, int32_t dim, const double* weights,
                           int32_t delta_power, int32_t left_bc, int32_t right_bc, int32_t scale, double cutoff,
                           tnfa_net** op) {
@@ -269,15 +314,8 @@ int tnfa_op_build_stencil(tnfa_ctx* ctx, const tnfa_topology* topo, int32_t dim,
   TNFA_CHECK(topo && weights && op, TNFA_ERR_INVALID_ARGUMENT, "op_build_stencil: null argument");
   TNFA_CHECK(cutoff >= 0 && delta_power >= 0, TNFA_ERR_INVALID_ARGUMENT, "negative cutoff or power");
   const Topo F = topo_from_abi(topo);
-  TNFA_CHECK(F.roots().size() == 1, TNFA_ERR_UNSUPPORTED, "shift operators need a tree");
-  const Digits D = digits_of(F, dim);
   // shifts [x+2d, x+d, x, x-d, x-2d] (src/elementary_operators.jl:122-160)
-  std::vector<Term> terms;
-  terms.push_back(Term{weights[2], {}});  // the identity, always present (possibly 0)
-  for (int i = 0; i < 2; ++i)
-    if (weights[i] != 0) shift_terms(D, i == 0 ? 1 : 0, true, right_bc, weights[i], terms);
-  for (int i = 3; i < 5; ++i)
-    if (weights[i] != 0) shift_terms(D, i == 4 ? 1 : 0, false, left_bc, weights[i], terms);
+  const std::vector<Term> terms = stencil_terms(F, dim, weights, left_bc, right_bc);
   std::vector<int> sv;
   if (scale)
     for (int v = 0; v < F.V; ++v)

@@ -165,6 +165,10 @@ SIGNATURES = {
     "tnfa_multiply": (C.c_int, [_P, _P, _P, _PP]),
     "tnfa_operator_proj": (C.c_int, [_P, _P, _PP]),
     "tnfa_cross": (C.c_int, [_P, _P, C.c_int, _I32, _I32, C.c_double, _I32, _PI32, _PI32, _PI32, _PD]),
+    "tnfa_op_stencil_terms": (
+        C.c_int,
+        [C.POINTER(Topology), _I32, _PD, _I32, _I32, _I32, _I32, _PD, _PI32, _PI32, _PD, _PI32, _PI32],
+    ),
     "tnfa_op_from_terms": (
         C.c_int,
         [_P, C.POINTER(Topology), _I32, _PD, _PI32, _PI32, _PD, C.c_double, _PP],

@@ -271,3 +271,66 @@ def test_delta_kernel_overlaps_match_reference_cases():
         assert _kernel_value(s, [x, 0.5, 0], P, D) == 0
         assert _kernel_value(s, [x, delta, 0], P, D) == 1
         assert _kernel_value(s, [delta, x, 0], P, D) == 1
+
+
+_NAMES = {(0.0, 1.0, 0.0, 0.0): "D+", (0.0, 0.0, 1.0, 0.0): "D-", (1.0, 0.0, 0.0, 0.0): "Ddn",
+          (0.0, 0.0, 0.0, 1.0): "Dup"}
+
+
+@pytest.mark.parametrize("weights,power", [([0.0, 0.5, 0.0, -0.5, 0.0], 1), ([0.0, 1.0, -2.0, 1.0, 0.0], 2),
+                                           ([0.5, -1.0, 0.0, 1.0, -0.5], 3), ([1.0, -4.0, 6.0, -4.0, 1.0], 4)])
+@pytest.mark.parametrize("left,right", [("Dirichlet", "Dirichlet"), ("Neumann", "Periodic"),
+                                        ("Periodic", "Neumann")])
+def test_library_stencil_terms_match_oracle(weights, power, left, right):
+    """The carry-string terms the library builds its stencils from
+    (tnfa_op_stencil_terms, no device involved) equal the oracle's
+    (src/elementary_operators.jl:32-160) term by term, for variable 2 of a
+    two-variable comb."""
+    import itensornumericalanalysis as ina
+    from itensornumericalanalysis import _lib
+    from itensornumericalanalysis.network import topology_struct
+
+    L = _lib.load()
+    s = ina.continuous_siteinds(ina.named_comb_tree((2, 5)), map_dimension=2)
+    t, _keep = topology_struct(s, [1] * s.layout.n)
+    nlegs, ldim, lvar, ldig, lkind = s.leg_arrays()
+    bc = {"Dirichlet": 0, "Neumann": 1, "Periodic": 2}
+    w = (C.c_double * 5)(*weights)
+    nt, nf = C.c_int32(0), C.c_int32(0)
+    assert L.tnfa_op_stencil_terms(C.byref(t), 2, w, bc[left], bc[right], 0, 0, None, None, None, None,
+                                   C.byref(nt), C.byref(nf)) == 0
+    coefs = (C.c_double * nt.value)()
+    nfac = (C.c_int32 * nt.value)()
+    legs = (C.c_int32 * max(nf.value, 1))()
+    mats = (C.c_double * max(4 * nf.value, 1))()
+    assert L.tnfa_op_stencil_terms(C.byref(t), 2, w, bc[left], bc[right], nt, nf, coefs, nfac, legs, mats,
+                                   C.byref(nt), C.byref(nf)) == 0
+    got, k = [], 0
+    for i in range(nt.value):
+        ops = {}
+        for _ in range(nfac[i]):
+            ops[(lvar[legs[k]], ldig[legs[k]])] = _NAMES[tuple(mats[4 * k:4 * k + 4])]
+            k += 1
+        got.append((coefs[i], ops))
+    Lv = s.ndigits(2)
+    ref = O.stencil_terms(Lv, weights, power, dim=2, left=left, right=right, scale=False)
+    assert len(got) == len(ref)
+    for (cg, og), (cr, orf) in zip(got, ref):
+        assert cg == cr and og == orf, ((cg, og), (cr, orf))
+
+
+def test_library_stencil_terms_reject_bad_input():
+    import itensornumericalanalysis as ina
+    from itensornumericalanalysis import _lib
+    from itensornumericalanalysis.network import topology_struct
+
+    L = _lib.load()
+    s = ina.continuous_siteinds(ina.named_path_graph(4))
+    t, _keep = topology_struct(s, [1] * s.layout.n)
+    w = (C.c_double * 5)(0.0, 1.0, -2.0, 1.0, 0.0)
+    nt, nf = C.c_int32(0), C.c_int32(0)
+    # variable 2 has no digits; a boundary code out of range
+    assert L.tnfa_op_stencil_terms(C.byref(t), 2, w, 0, 0, 0, 0, None, None, None, None,
+                                   C.byref(nt), C.byref(nf)) == _lib.ERR_INVALID_ARGUMENT
+    assert L.tnfa_op_stencil_terms(C.byref(t), 1, w, 7, 0, 0, 0, None, None, None, None,
+                                   C.byref(nt), C.byref(nf)) == _lib.ERR_INVALID_ARGUMENT
