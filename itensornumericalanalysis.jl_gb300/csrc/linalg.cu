@@ -1832,6 +1832,7 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
     // |C|_F^2 and |C V_kept|_F^2 in FP64: their difference is the weight of
     // the directions dropped after pass 1, exact to FP64 rounding
     std::vector<double> ss_in(nj), ss_kept(nj);
+    DBuf ss_keep;  // pass 2's sums of squares, read after the passes
     for (size_t q = 0; q < nj; ++q) w[q] = n[q];
     for (int pass = 0; pass < 2; ++pass) {
       std::vector<DBuf> C32(nj), U32(nj), V32(nj), V(nj), G(nj), Y(nj), Xn(nj);
@@ -1848,8 +1849,6 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
         DBuf dq = upload(ctx, sq);
         k_sumsq<<<(unsigned)nj, 256, 0, ctx->stream>>>(dq.as<SumsqJob>());
         TNFA_LAUNCH_CHECK();
-        TNFA_CUDA(cudaMemcpyAsync(pass == 0 ? ss_in.data() : ss_kept.data(), ss.p, nj * sizeof(double),
-                                  cudaMemcpyDeviceToHost, ctx->stream));
       }
       for (size_t q = 0; q < nj; ++q) {
         const int k = w[q], m = cm[q];
@@ -1872,8 +1871,12 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
         // dropped weight must sit far below the truncation budget (here
         // 1e-6 of it: the FP64 rule below drops it too, and the loss stays
         // near 1e-10 of the norm).  Exactly-deficient ranks still fall away.
+        // (the sums of squares are read here, where the host waits anyway: a
+        // copy to pageable memory returns only once it has completed)
         std::vector<double> sv32(soff[nj]);
         const std::vector<double>& hss = ss_in;
+        TNFA_CUDA(cudaMemcpyAsync(ss_in.data(), ss.p, nj * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
         TNFA_CUDA(cudaMemcpyAsync(sv32.data(), S32all.p, soff[nj] * sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));
         TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1925,7 +1928,10 @@ void trunc_factor(tnfa_ctx* ctx, const std::vector<FactorJob>& jobs, double cuto
         xin[q] = X[q].p;
         w[q] = ku[q];
       }
+      if (pass == 1) ss_keep = std::move(ss);
     }
+    TNFA_CUDA(cudaMemcpyAsync(ss_kept.data(), ss_keep.p, nj * sizeof(double), cudaMemcpyDeviceToHost,
+                              ctx->stream));
     TNFA_CUDA(cudaStreamSynchronize(ctx->stream));
     for (size_t q = 0; q < nj; ++q) extra[q] = std::max(0.0, ss_in[q] - ss_kept[q]);
     // The polish in double-float (FP32 pairs, ~48 bits) on the FP32 pipe:

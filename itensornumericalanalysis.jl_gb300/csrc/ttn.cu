@@ -264,20 +264,49 @@ struct ApplyJob {
   int dO[AP_MAXD], dF[AP_MAXD];
   int nlegs;
   int base[8];
+  // k_apply_exact: this vertex's operator, function and output tensors, and
+  // the first of its blocks in the flat grid (ascending over the job list)
+  const void* o;
+  const void* f;
+  void* y;
+  int64_t first_block;
 };
 
+constexpr int AP_THREADS = 256;
+constexpr int AP_PER_BLOCK = 4 * AP_THREADS;  // outputs per block
+
+// The job that owns flat block b: the last one whose first block is <= b.
+template <class Job>
+__device__ __forceinline__ const Job& job_of_block(const Job* __restrict__ jobs, int njobs, int64_t b) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].first_block <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return jobs[lo];
+}
+
+// Every vertex of every listed (operator, function) pair in one launch: the
+// jobs' outputs are cut into runs of AP_PER_BLOCK entries, one block each.
 template <class T>
-__global__ void k_apply_exact(const T* __restrict__ O, const T* __restrict__ F, T* __restrict__ Y,
-                              const ApplyJob* __restrict__ jobs) {
-  const ApplyJob& jb = jobs[blockIdx.y];
+__global__ void __launch_bounds__(AP_THREADS) k_apply_exact(const ApplyJob* __restrict__ jobs, int njobs) {
+  const int64_t b = blockIdx.x;
+  const ApplyJob& jb = job_of_block(jobs, njobs, b);
+  const T* __restrict__ O = (const T*)jb.o;
+  const T* __restrict__ F = (const T*)jb.f;
+  T* __restrict__ Y = (T*)jb.y;
   int64_t obond = 1, fbond = 1;
   for (int a = 1; a < jb.nd; ++a) {
     obond *= jb.dO[a];
     fbond *= jb.dF[a];
   }
   const int sdim = jb.dF[0];
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < jb.n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t i0 = (b - jb.first_block) * AP_PER_BLOCK;
+  const int64_t i1 = i0 + AP_PER_BLOCK < jb.n ? i0 + AP_PER_BLOCK : jb.n;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += AP_THREADS) {
     int64_t r = i, oi = 0, fi = 0, os = 1, fs = 1;
     for (int a = jb.nd - 1; a >= 1; --a) {
       const int64_t d = (int64_t)jb.dO[a] * jb.dF[a];
@@ -294,17 +323,37 @@ __global__ void k_apply_exact(const T* __restrict__ O, const T* __restrict__ F, 
       // fused operator site index: per leg (out * b + in), first leg most significant
       int so = s_out, si = s_in, osite = 0, mul = 1;
       for (int l = jb.nlegs - 1; l >= 0; --l) {
-        const int b = jb.base[l];
-        const int o = so % b, in = si % b;
-        so /= b;
-        si /= b;
-        osite += (o * b + in) * mul;
-        mul *= b * b;
+        const int bb = jb.base[l];
+        const int o = so % bb, in = si % bb;
+        so /= bb;
+        si /= bb;
+        osite += (o * bb + in) * mul;
+        mul *= bb * bb;
       }
-      acc = Sc<T>::fma(O[jb.ooff + osite * obond + oi], F[jb.foff + s_in * fbond + fi], acc);
+      acc = Sc<T>::fma(O[osite * obond + oi], F[s_in * fbond + fi], acc);
     }
-    Y[jb.yoff + i] = acc;
+    Y[i] = acc;
   }
+}
+
+// Contiguous copies of many tensors in one launch (runs of AP_PER_BLOCK
+// elements, one block each).
+struct CopyRun {
+  const void* src;
+  void* dst;
+  int64_t n;  // elements
+  int64_t first_block;
+};
+
+template <class T>
+__global__ void __launch_bounds__(AP_THREADS) k_copy_runs(const CopyRun* __restrict__ runs, int nruns) {
+  const int64_t b = blockIdx.x;
+  const CopyRun& c = job_of_block(runs, nruns, b);
+  const T* __restrict__ src = (const T*)c.src;
+  T* __restrict__ dst = (T*)c.dst;
+  const int64_t i0 = (b - c.first_block) * AP_PER_BLOCK;
+  const int64_t i1 = i0 + AP_PER_BLOCK < c.n ? i0 + AP_PER_BLOCK : c.n;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += AP_THREADS) dst[i] = src[i];
 }
 
 // Adjoint of k_apply_exact with respect to f:
@@ -446,34 +495,78 @@ std::vector<ApplyJob> apply_jobs(const Topo& A, const Topo& B, Topo& Y) {
   return jobs;
 }
 
+// Give every job its first block in the flat grid; the total block count.
+template <class Job>
+int64_t number_blocks(std::vector<Job>& jobs) {
+  int64_t nb = 0;
+  for (auto& j : jobs) {
+    j.first_block = nb;
+    nb += (j.n + AP_PER_BLOCK - 1) / AP_PER_BLOCK;
+  }
+  TNFA_CHECK(nb < (int64_t(1) << 31), TNFA_ERR_UNSUPPORTED, "too many blocks for one launch");
+  return nb;
+}
+
+// y_i = O_i f_i exactly, vertex by vertex, for every pair in one launch; each
+// W[i] receives y_i's per-vertex tensors, written in place by the kernel.
+template <class T>
+void apply_exact_many(tnfa_ctx* ctx, int n, const tnfa_net* const* ops, const tnfa_net* const* fs,
+                      std::vector<Work<T>>& W) {
+  W.clear();
+  W.reserve(n);
+  std::vector<ApplyJob> jobs;
+  double fl = 0;
+  for (int i = 0; i < n; ++i) {
+    const Topo& A = ops[i]->topo;
+    const Topo& B = fs[i]->topo;
+    check_apply(A, B);
+    Topo Y;
+    std::vector<ApplyJob> ji = apply_jobs(A, B, Y);
+    W.push_back(Work<T>{ctx, Y, {}});
+    Work<T>& w = W.back();
+    w.t.reserve(Y.V);
+    for (int v = 0; v < Y.V; ++v) {
+      w.t.emplace_back(ctx, (size_t)Y.size(v) * sizeof(T));
+      ApplyJob& j = ji[v];
+      j.o = (const T*)ops[i]->d + j.ooff;
+      j.f = (const T*)fs[i]->d + j.foff;
+      j.y = w.t.back().p;
+      fl += 2.0 * j.n * j.dF[0];
+      jobs.push_back(j);
+    }
+  }
+  if (jobs.empty()) return;
+  const int64_t nb = number_blocks(jobs);
+  DBuf dj = upload_jobs(ctx, jobs);
+  KernelScope ks(ctx, "apply_exact", fl, 0.0);
+  k_apply_exact<T><<<(unsigned)nb, AP_THREADS, 0, ctx->stream>>>(dj.as<ApplyJob>(), (int)jobs.size());
+  TNFA_LAUNCH_CHECK();
+}
+
 template <class T>
 Work<T> apply_exact(tnfa_ctx* ctx, const tnfa_net* op, const tnfa_net* f) {
-  const Topo& A = op->topo;
-  const Topo& B = f->topo;
-  check_apply(A, B);
-  Topo Y;
-  std::vector<ApplyJob> jobs = apply_jobs(A, B, Y);
-  int64_t nmax = 1;
-  for (auto& j : jobs) nmax = std::max(nmax, j.n);
-  Work<T> w{ctx, Y, {}};
-  DBuf ybuf(ctx, (size_t)Y.n_elem * sizeof(T));
-  DBuf dj = upload_jobs(ctx, jobs);
-  dim3 grid(grid_for(nmax, 256, 4096), B.V);
-  {
-    double fl = 0;
-    for (auto& j : jobs) fl += 2.0 * j.n * j.dF[0];
-    KernelScope ks(ctx, "apply_exact", fl, 0.0);
-    k_apply_exact<T><<<grid, 256, 0, ctx->stream>>>((const T*)op->d, (const T*)f->d, ybuf.as<T>(),
-                                                     dj.as<ApplyJob>());
-    TNFA_LAUNCH_CHECK();
+  std::vector<Work<T>> W;
+  apply_exact_many<T>(ctx, 1, &op, &f, W);
+  return std::move(W[0]);
+}
+
+// One network per Work (canonical layout), all tensors copied in one launch.
+template <class T>
+void store_works(std::vector<Work<T>>& W, int dtype, tnfa_net** outs) {
+  if (W.empty()) return;
+  tnfa_ctx* ctx = W[0].ctx;
+  std::vector<CopyRun> runs;
+  for (size_t i = 0; i < W.size(); ++i) {
+    Work<T>& w = W[i];
+    w.topo.finalize();
+    outs[i] = new_net(ctx, w.topo, dtype);
+    for (int v = 0; v < w.topo.V; ++v)
+      runs.push_back({w.t[v].p, (T*)outs[i]->d + w.topo.off[v], w.size(v), 0});
   }
-  w.t.reserve(Y.V);
-  for (int v = 0; v < Y.V; ++v) {
-    w.t.emplace_back(ctx, (size_t)Y.size(v) * sizeof(T));
-    TNFA_CUDA(cudaMemcpyAsync(w.t.back().p, ybuf.as<T>() + Y.off[v], Y.size(v) * sizeof(T),
-                              cudaMemcpyDeviceToDevice, ctx->stream));
-  }
-  return w;
+  const int64_t nb = number_blocks(runs);
+  DBuf dr = upload_jobs(ctx, runs);
+  k_copy_runs<T><<<(unsigned)nb, AP_THREADS, 0, ctx->stream>>>(dr.as<CopyRun>(), (int)runs.size());
+  TNFA_LAUNCH_CHECK();
 }
 
 // df += J^T dy for y = apply_exact(op, f) (dy in y's canonical layout).
@@ -906,11 +999,14 @@ template <class T>
 void batch_apply_truncate(tnfa_ctx* ctx, int n, const tnfa_net* const* ops, const tnfa_net* const* fs,
                           const tnfa_trunc_params& prm, int dtype, tnfa_net** outs) {
   std::vector<Work<T>> W;
-  W.reserve(n);
-  for (int i = 0; i < n; ++i)
-    W.push_back(ops ? apply_exact<T>(ctx, ops[i], fs[i]) : load_work<T>(ctx, fs[i]));
+  if (ops) {
+    apply_exact_many<T>(ctx, n, ops, fs, W);
+  } else {
+    W.reserve(n);
+    for (int i = 0; i < n; ++i) W.push_back(load_work<T>(ctx, fs[i]));
+  }
   truncate_paths_batched(W, prm);
-  for (int i = 0; i < n; ++i) outs[i] = store_work(W[i], dtype);
+  store_works(W, dtype, outs);
 }
 
 // ------------------------------------------------------------ linsolve ----
