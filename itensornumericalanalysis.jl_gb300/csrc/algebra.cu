@@ -149,8 +149,7 @@ static void same_shape(const Topo& A, const Topo& B, const char* what) {
 template <class Job>
 static DBuf upload_jobs(tnfa_ctx* ctx, const std::vector<Job>& jobs) {
   DBuf d(ctx, jobs.size() * sizeof(Job));
-  TNFA_CUDA(cudaMemcpyAsync(d.p, jobs.data(), jobs.size() * sizeof(Job), cudaMemcpyHostToDevice,
-                            ctx->stream));
+  h2d(ctx, d.p, jobs.data(), jobs.size() * sizeof(Job));
   return d;
 }
 

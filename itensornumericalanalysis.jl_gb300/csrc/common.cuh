@@ -172,6 +172,15 @@ struct tnfa_ctx {
   std::map<size_t, std::vector<void*>> free_blocks;
   std::unordered_map<void*, size_t> block_size;
   size_t cached_bytes = 0;
+  // Pinned host blocks that stage large host -> device uploads (tnfa::h2d);
+  // a block is free again once the event recorded after its copy completes.
+  struct PinnedBlock {
+    void* p;
+    size_t bytes;
+    cudaEvent_t ev;
+  };
+  std::vector<PinnedBlock> pinned;
+  size_t pinned_bytes = 0;
 };
 
 struct tnfa_net {
@@ -194,6 +203,11 @@ namespace tnfa {
 // Device memory from the stream-ordered allocator of the context's stream.
 void* dalloc(tnfa_ctx* ctx, size_t bytes);
 void dfree(tnfa_ctx* ctx, void* p);
+
+// Host -> device copy of host data (job tables and the like) on the
+// context's stream that returns without waiting for the stream: the source
+// may be reused as soon as the call returns.
+void h2d(tnfa_ctx* ctx, void* dst, const void* src, size_t bytes);
 
 // RAII scratch buffer.
 struct DBuf {

@@ -1,5 +1,7 @@
 // Context and network objects of libtnfa: creation, validation, transfer,
 // copies and scalar scaling.
+#include <cstring>
+
 #include "common.cuh"
 
 namespace tnfa {
@@ -117,6 +119,66 @@ void dfree(tnfa_ctx* ctx, void* p) {
   ctx->cached_bytes += cls;
 }
 
+// A copy from pageable host memory returns at once only up to 64 KB (the
+// driver stages it); a larger one returns after the stream has drained, so
+// every large job table would stall the host behind the GPU.  Those go
+// through pinned blocks instead: copied in, sent with an asynchronous copy,
+// and reused only after the event recorded behind that copy has completed.
+// Inside a stream capture (where a captured copy would read the block again
+// at every replay) and beyond the pinned cap the plain copy is used.
+constexpr size_t kPageableAsyncMax = size_t(64) << 10;
+constexpr size_t kPinnedMaxBytes = size_t(256) << 20;
+
+void h2d(tnfa_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (bytes > kPageableAsyncMax && !ctx->capturing)
+    TNFA_CUDA(cudaStreamIsCapturing(ctx->stream, &cap));
+  if (bytes <= kPageableAsyncMax || ctx->capturing || cap != cudaStreamCaptureStatusNone) {
+    TNFA_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return;
+  }
+  tnfa_ctx::PinnedBlock* blk = nullptr;
+  for (auto& b : ctx->pinned) {
+    if (b.bytes < bytes) continue;
+    const cudaError_t q = cudaEventQuery(b.ev);
+    if (q == cudaSuccess) {
+      blk = &b;
+      break;
+    }
+    if (q != cudaErrorNotReady) TNFA_CUDA(q);
+    // "not ready" is a status, not a failure: keep it out of the error state
+    if (cudaPeekAtLastError() == cudaErrorNotReady) cudaGetLastError();
+  }
+  if (!blk) {
+    size_t cls = size_t(128) << 10;
+    while (cls < bytes) cls <<= 1;
+    if (ctx->pinned_bytes + cls > kPinnedMaxBytes) {
+      TNFA_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+      return;
+    }
+    void* p = nullptr;
+    if (cudaMallocHost(&p, cls) != cudaSuccess) {
+      cudaGetLastError();
+      TNFA_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+      return;
+    }
+    cudaEvent_t ev = nullptr;
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFreeHost(p);
+      TNFA_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+      return;
+    }
+    ctx->pinned.push_back({p, cls, ev});
+    ctx->pinned_bytes += cls;
+    blk = &ctx->pinned.back();
+  }
+  std::memcpy(blk->p, src, bytes);
+  TNFA_CUDA(cudaMemcpyAsync(dst, blk->p, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  TNFA_CUDA(cudaEventRecord(blk->ev, ctx->stream));
+}
+
 void require_ctx(const tnfa_ctx* ctx) {
   TNFA_CHECK(ctx != nullptr, TNFA_ERR_INVALID_ARGUMENT, "null context");
 }
@@ -150,6 +212,10 @@ static void ctx_free(tnfa_ctx* ctx) {
       cudaEventDestroy(ev.second);
     }
   for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+  for (auto& b : ctx->pinned) {
+    cudaEventDestroy(b.ev);
+    cudaFreeHost(b.p);
+  }
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

@@ -137,8 +137,7 @@ __device__ inline dfl shfl_xor(dfl v, int o) {
 template <class Job>
 static DBuf upload(tnfa_ctx* ctx, const std::vector<Job>& jobs) {
   DBuf d(ctx, jobs.size() * sizeof(Job));
-  TNFA_CUDA(cudaMemcpyAsync(d.p, jobs.data(), jobs.size() * sizeof(Job), cudaMemcpyHostToDevice,
-                            ctx->stream));
+  h2d(ctx, d.p, jobs.data(), jobs.size() * sizeof(Job));
   return d;
 }
 

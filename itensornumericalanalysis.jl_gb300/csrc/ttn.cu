@@ -443,8 +443,7 @@ __global__ void k_reduce_out(const T* __restrict__ O, T* __restrict__ D,
 template <class Job>
 DBuf upload_jobs(tnfa_ctx* ctx, const std::vector<Job>& jobs) {
   DBuf d(ctx, jobs.size() * sizeof(Job));
-  TNFA_CUDA(cudaMemcpyAsync(d.p, jobs.data(), jobs.size() * sizeof(Job), cudaMemcpyHostToDevice,
-                            ctx->stream));
+  h2d(ctx, d.p, jobs.data(), jobs.size() * sizeof(Job));
   return d;
 }
 
