@@ -5,10 +5,13 @@ with the same graphs, points and tolerances.  Where the reference draws
 random parameters with Julia's RNG (seed 1234 / 42), numpy-seeded values are
 used instead: the expected value is analytic either way.
 """
+import zlib
+
 import numpy as np
 import pytest
 
 import oracle as O
+from oracle import itn as OI
 
 RTOL = np.sqrt(np.finfo(float).eps)  # Julia's default isapprox rtol
 
@@ -72,7 +75,7 @@ FUNCS = [
 
 @pytest.mark.parametrize("name,net,fn", FUNCS)
 def test_functions_binary(name, net, fn):  # test/test_realitensorfunction.jl:65-80
-    rng = np.random.default_rng(hash(name) % 2**32)
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
     a, k, c = rng.random(3)
     s = O.siteinds(O.comb_tree_graph((2, 3)))
     x = 0.625
@@ -81,7 +84,7 @@ def test_functions_binary(name, net, fn):  # test/test_realitensorfunction.jl:65
 
 @pytest.mark.parametrize("name,net,fn", FUNCS)
 def test_functions_trinary(name, net, fn):  # test/test_realitensorfunction.jl:89-104
-    rng = np.random.default_rng(hash(name) % 2**32 + 1)
+    rng = np.random.default_rng(zlib.crc32(name.encode()) + 1)
     a, k, c = rng.random(3)
     s = O.siteinds(O.comb_tree_graph((2, 3)), base=3)
     x = 5.0 / 9.0
@@ -98,8 +101,6 @@ def test_tanh():  # test/test_realitensorfunction.jl:106-121
 
 def _random_tree(n, rng):
     """Pruefer-code random tree on vertices (i, 1), as Graphs.uniform_tree."""
-    from itertools import count  # noqa: F401
-
     verts = [(i, 1) for i in range(1, n + 1)]
     code = list(rng.integers(1, n + 1, size=n - 2))
     deg = [1] * (n + 1)
@@ -135,7 +136,7 @@ def test_const_3d():  # test/test_realitensorfunction.jl:147-160
 
 @pytest.mark.parametrize("name,net,fn", FUNCS)
 def test_sum_of_1d_functions_2d(name, net, fn):  # test/test_realitensorfunction.jl:162-189
-    rng = np.random.default_rng(hash(name) % 2**32 + 2)
+    rng = np.random.default_rng(zlib.crc32(name.encode()) + 2)
     a, k, c = rng.random(3)
     s = O.siteinds(O.grid_graph((10, 1)), map_dimension=2)
     x, y = 0.625, 0.25
@@ -170,12 +171,76 @@ def test_delta_p():  # test/test_realitensorfunction.jl:210-259
 
 @pytest.mark.parametrize("name,net,fn", FUNCS)
 def test_complex_functions(name, net, fn):  # test/test_complexitensorfunction.jl:57-80
-    rng = np.random.default_rng(hash(name) % 2**32 + 3)
+    rng = np.random.default_rng(zlib.crc32(name.encode()) + 3)
     a, k, c = rng.random(3) + 1j * rng.random(3)
     s = O.complex_siteinds(O.comb_tree_graph((2, 3)), [[(1, 1), (1, 2), (1, 3)]],
                            [[(2, 1), (2, 2), (2, 3)]])
     z = 0.625 + 0.25j
     assert approx(O.evaluate(net(s, k=k, a=a, c=c), [z]), c * fn(k * z + a))
+
+
+@pytest.mark.parametrize("name,net,fn", FUNCS)
+def test_complex_functions_trinary(name, net, fn):  # test/test_complexitensorfunction.jl:92-110
+    rng = np.random.default_rng(zlib.crc32(name.encode()) + 4)
+    a, k, c = rng.random(3) + 1j * rng.random(3)
+    s = O.complex_siteinds(O.comb_tree_graph((2, 3)), [[(1, 1), (1, 2), (1, 3)]],
+                           [[(2, 1), (2, 2), (2, 3)]], base=3)
+    z = 5.0 / 9.0 + 4.0j / 9.0
+    assert approx(O.evaluate(net(s, k=k, a=a, c=c), [z]), c * fn(k * z + a))
+
+
+def test_complex_tanh():  # test/test_complexitensorfunction.jl:113-130
+    rng = np.random.default_rng(13)
+    a, k, c = rng.random(3) + 1j * rng.random(3)
+    L = 10
+    s = O.complex_siteinds(O.grid_graph((L, 1)), [[(i, 1) for i in range(1, L + 1, 2)]],
+                           [[(i, 1) for i in range(2, L + 1, 2)]])
+    z = 0.625 + 0.125j
+    assert approx(O.evaluate(O.tanh_itn(s, k=k, a=a, c=c, nterms=50), [z]), c * np.tanh(k * z + a))
+
+
+def test_complex_poly():  # test/test_complexitensorfunction.jl:132-157
+    rng = np.random.default_rng(4321)
+    L = 6
+    for deg in range(1, 12):
+        s = O.complex_siteinds(_random_tree(L, rng), [[(i, 1) for i in range(1, L + 1, 2)]],
+                               [[(i, 1) for i in range(2, L + 1, 2)]])
+        k, c = rng.random(2) + 1j * rng.random(2)
+        coeffs = rng.random(deg + 1) + 1j * rng.random(deg + 1)
+        z = 0.875 + 0.25j
+        val = O.evaluate(O.poly_itn(s, list(coeffs), k=k, c=c), [z])
+        exact = c * sum(coeffs[i] * (k * z) ** i for i in range(deg + 1))
+        assert abs(val - exact) <= 1e-4
+
+
+def test_complex_const_3d():  # test/test_complexitensorfunction.jl:161-172
+    s = O.complex_siteinds(O.grid_graph((3, 3)), map_dimension=3)
+    z = [0.5 + 0.125j, 0.25 + 0.875j, 0.0]
+    assert approx(O.evaluate(O.const_itn(s, c=1.5), z, [1, 2, 3]), 1.5)
+
+
+@pytest.mark.parametrize("name,net,fn", FUNCS)
+def test_complex_sum_of_1d_functions_2d(name, net, fn):  # test/test_complexitensorfunction.jl:174-208
+    rng = np.random.default_rng(zlib.crc32(name.encode()) + 5)
+    a, k, c = rng.random(3) + 1j * rng.random(3)
+    L = 10
+    h = L // 2
+    real_dv = [[(i, 1) for i in range(1, h + 1)], [(i, 1) for i in range(h + 1, L + 1)]]
+    imag_dv = [[(i, 1) for i in range(h + 1, L + 1)], [(i, 1) for i in range(1, h + 1)]]
+    s = O.complex_siteinds(O.grid_graph((L, 1)), real_dv, imag_dv)
+    z1, z2 = 0.625 + 0.875j, 0.25 + 0.125j
+    f = O.net_add(net(s, k=k, a=a, c=c, dim=1), net(s, k=k, a=a, c=c, dim=2))
+    assert approx(O.evaluate(f, [z1, z2], [1, 2]), c * fn(k * z1 + a) + c * fn(k * z2 + a))
+
+
+def test_complex_tanh_2d():  # test/test_complexitensorfunction.jl:210-227
+    rng = np.random.default_rng(17)
+    a, k, c = rng.random(3) + 1j * rng.random(3)
+    s = O.complex_siteinds(O.grid_graph((3, 2)), map_dimension=2)
+    z1, z2 = 0.5 + 0.125j, 0.625 + 0.25j
+    f = O.net_add(O.tanh_itn(s, k=k, a=a, c=c, nterms=50, dim=1),
+                  O.tanh_itn(s, k=k, a=a, c=c, nterms=50, dim=2))
+    assert approx(O.evaluate(f, [z1, z2], [1, 2]), c * np.tanh(k * z1 + a) + c * np.tanh(k * z2 + a))
 
 
 # ------------------------------------------------------------ operators ----
@@ -261,3 +326,132 @@ def test_integrate_2d():  # test/test_integration.jl:28-38
     s = O.siteinds(O.comb_tree_graph((3, L // 3)), map_dimension=2)
     f = O.net_multiply(O.exp_itn(s, dim=1), O.exp_itn(s, dim=2))
     assert abs(O.integrate(f) - (np.e - 1) ** 2) <= 1e-4
+
+
+def _grid(f, dims):
+    """f on the full grid of the listed variables (axes: each variable's digits
+    1..L in turn, so the flat index is the grid position) and the
+    (dimension, digit) -> axis map apply_terms_dense takes."""
+    inds, axis = [], {}
+    for d in dims:
+        di = sorted((i for i, (dd, k, r) in f.s.info.items() if dd == d and r), key=lambda i: f.s.info[i][1])
+        for i in di:
+            axis[(d, f.s.info[i][1])] = len(inds)
+            inds.append(i)
+    return O.dense(f, inds), axis
+
+
+def test_first_derivative_on_comb():  # test/test_operators.jl:48-64
+    s = O.siteinds(O.comb_tree_graph((4, 3)))
+    L = 12
+    F, axis = _grid(O.sin_itn(s, k=np.pi), [1])
+    G = O.apply_terms_dense(O.stencil_terms(L, [0.0, 0.5, 0.0, -0.5, 0.0], 1), F, axis).reshape(-1)
+    d = 2.0**-L
+    for x in [d, 0.125, 0.25, 0.625, 0.875]:
+        assert abs(G[int(round(x / d))].real - np.pi * np.cos(np.pi * x)) <= 1e-3
+
+
+def test_first_derivative_of_3d_function():  # test/test_operators.jl:66-97
+    """On the 45-site path (15 digits per variable) the derivative along y is
+    taken on the y-grid of f(x, ., z), the x and z digits projected out as
+    evaluate does: the stencil only acts on y's digits."""
+    s = O.siteinds(O.path_graph(45), map_dimension=3)
+    f = O.net_multiply(O.net_multiply(O.poly_itn(s, [0.0, -1.0, 1.0], dim=1), O.sin_itn(s, k=np.pi, dim=2)),
+                       O.sin_itn(s, k=np.pi, dim=3))
+    pts = [0.125, 0.25, 0.675]
+    Ly = 15
+    d = 2.0**-Ly
+    yinds = sorted((i for i, (dd, k, r) in s.info.items() if dd == 2), key=lambda i: s.info[i][1])
+    terms = O.stencil_terms(Ly, [0.0, 0.5, 0.0, -0.5, 0.0], 1, dim=2)
+    for x in pts:
+        for z in pts:
+            iv = O.calculate_ind_values(s, [x, z], [1, 3])
+            ts = []
+            for v, T in f.T.items():
+                for i in s.site[v]:
+                    if i in iv:
+                        T = O.contract([T, OI.onehot(i, iv[i])])
+                ts.append(T)
+            Fy = O.contract(ts).permute(yinds).arr
+            G = O.apply_terms_dense(terms, Fy, {(2, k): k - 1 for k in range(1, Ly + 1)}).reshape(-1)
+            for y in pts:
+                exact = (x * x - x) * np.sin(np.pi * y) * np.sin(np.pi * z)
+                assert abs(O.evaluate(f, [x, y, z], [1, 2, 3]).real - exact) <= 1e-3
+                dexact = np.pi * (x * x - x) * np.cos(np.pi * y) * np.sin(np.pi * z)
+                assert abs(G[int(y / d)].real - dexact) <= 1e-3
+
+
+def test_multiplication_1d():  # test/test_operators.jl:99-116 and :148-166
+    """g f on a comb; operator_proj(f) applied to g is the same pointwise product."""
+    s = O.siteinds(O.comb_tree_graph((4, 3)))
+    g, f = O.sin_itn(s, k=0.5 * np.pi), O.cos_itn(s, k=0.25 * np.pi)
+    fg, ff = O.net_multiply(g, f), O.net_multiply(f, f)
+    for x in [0.025, 0.1, 0.25, 0.625, 0.875]:
+        assert abs(O.evaluate(fg, [x]).real - np.sin(0.5 * np.pi * x) * np.cos(0.25 * np.pi * x)) <= 1e-3
+        assert abs(O.evaluate(ff, [x]).real - np.cos(0.25 * np.pi * x) ** 2) <= 1e-3
+
+
+def test_multiplication_2d_random_tree():  # test/test_operators.jl:118-146
+    s = O.siteinds(_random_tree(8, np.random.default_rng(8)), map_dimension=2)
+    fx, gy = O.cos_itn(s, k=0.25 * np.pi, dim=1), O.sin_itn(s, k=0.5 * np.pi, dim=2)
+    fg, gg = O.net_multiply(fx, gy), O.net_multiply(gy, gy)
+    pts = [0.125, 0.25, 0.625, 0.875]
+    for x in pts:
+        for y in pts:
+            assert approx(O.evaluate(fx, [x, y], [1, 2]).real, np.cos(0.25 * np.pi * x))
+            assert approx(O.evaluate(gy, [x, y], [1, 2]).real, np.sin(0.5 * np.pi * y))
+            assert abs(O.evaluate(fg, [x, y], [1, 2]).real
+                       - np.cos(0.25 * np.pi * x) * np.sin(0.5 * np.pi * y)) <= 1e-3
+            assert abs(O.evaluate(gg, [x, y], [1, 2]).real - np.sin(0.5 * np.pi * y) ** 2) <= 1e-3
+
+
+@pytest.mark.parametrize("boundary", ["Dirichlet", "Periodic", "Neumann"])
+@pytest.mark.parametrize("case", ["reference", "x_plus_y"])
+def test_shift_operators_2d(boundary, case):  # test/test_operators.jl:289-351
+    """Shifts of variable 2 on a 3 x 3 comb.  The reference's function is
+    f_x + f_x (a function of x alone, so only the boundary rows move); the
+    second case adds cos(y) so every row moves."""
+    s = O.siteinds(O.comb_tree_graph((3, 3)), map_dimension=2)
+    fx = O.poly_itn(s, [1.0, 0.5, 0.25], dim=1)
+    f = O.net_add(fx, fx) if case == "reference" else O.net_add(fx, O.cos_itn(s, dim=2))
+    L1 = sum(1 for (d, k, r) in s.info.values() if d == 1)
+    L2 = sum(1 for (d, k, r) in s.info.values() if d == 2)
+    F, axis = _grid(f, [1, 2])
+    fwd = O.apply_terms_dense(O.forward_shift_terms(L2, 2, boundary), F, axis).reshape(2**L1, 2**L2)
+    bwd = O.apply_terms_dense(O.backward_shift_terms(L2, 2, boundary), F, axis).reshape(2**L1, 2**L2)
+    F = F.reshape(2**L1, 2**L2)
+    d = 2.0**-L2
+    ix = int(0.5 * 2**L1)
+    for y in [0.0, d, 0.25, 0.5, 0.625, 0.875, 1.0 - d]:
+        iy = int(round(y / d))
+        if y + d < 1:
+            assert abs(fwd[ix, iy] - F[ix, iy + 1]) <= 1e-8
+        else:
+            want = {"Dirichlet": 0.0, "Periodic": F[ix, 0], "Neumann": F[ix, iy]}[boundary]
+            assert abs(fwd[ix, iy] - want) <= 1e-8
+        if y - d >= 0:
+            assert abs(bwd[ix, iy] - F[ix, iy - 1]) <= 1e-8
+        else:
+            want = {"Dirichlet": 0.0, "Periodic": F[ix, -1], "Neumann": F[ix, 0]}[boundary]
+            assert abs(bwd[ix, iy] - want) <= 1e-8
+
+
+def test_partial_integrate_3d():  # test/test_integration.jl:40-54 (src/integration.jl:35-54)
+    """exp(x) cos(y) exp(z) on a 3 x 30 comb (one tooth per variable), its
+    y and z digits summed with weight 1/2 each (partial_integrate over [2, 3];
+    merging the leg-less vertices does not change the value), then evaluated
+    at x = 0.875."""
+    L = 90
+    s = O.siteinds(O.comb_tree_graph((3, L // 3)), [[(i, j) for j in range(1, L // 3 + 1)] for i in range(1, 4)])
+    f = O.net_multiply(O.net_multiply(O.exp_itn(s, dim=1), O.cos_itn(s, dim=2)), O.exp_itn(s, dim=3))
+    x = 0.875
+    iv = O.calculate_ind_values(s, [x], [1])
+    ts = []
+    for v in s.verts:
+        t = f.T[v]
+        for i in s.site[v]:
+            w = np.full(i.dim, 1.0 / s.base) if s.info[i][0] in (2, 3) else OI.onehot(i, iv[i]).arr
+            t = O.contract([t, O.Tensor(w, [i])])
+        ts.append(t)
+    val = O.contract(ts).scalar()
+    assert abs(val - (np.e - 1) * np.sin(1) * np.exp(x)) <= 1e-8
