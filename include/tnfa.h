@@ -408,16 +408,18 @@ typedef struct {
   int32_t maxdim;       /* bond cap of the solution                               */
   double cutoff;        /* truncation of the two-site updates                     */
   double tol;           /* stop when ||A x - b|| / ||b|| <= tol                   */
-  int32_t krylov_dim;   /* reserved (local systems are solved densely)            */
+  int32_t krylov_dim;   /* reserved (local systems: dense LU; GMRES(40) above it) */
   int32_t precision;    /* reserved (FP64)                                        */
   double a0, a1;        /* solve (a0 + a1*A) x = b                                */
   int32_t refinements;  /* iterative-refinement steps after the sweeps            */
   double refine_cutoff; /* truncation of residuals and corrections in refinement  */
 } tnfa_linsolve_params;
 
-/* Solve (a0 + a1 A) x = b on a path-shaped tree by two-site alternating
- * sweeps (dense FP64 LU per two-site system, truncated SVD split); x0 seeds
- * the sweep.  Then up to `refinements` steps of iterative refinement: r = b -
+/* Solve (a0 + a1 A) x = b on a tree with one site leg per vertex by
+ * two-site updates (a path by alternating sweeps, any other tree by a
+ * depth-first tour that updates every edge twice per sweep; each two-site
+ * system by dense FP64 LU, or matrix-free GMRES(40) when large; truncated SVD
+ * split); x0 seeds the sweep.  Then up to `refinements` steps of iterative refinement: r = b -
  * (a0 + a1 A) x formed exactly and truncated with refine_cutoff, the same
  * sweeps solve for a correction e, x <- truncate(x + e, refine_cutoff).
  * Replaces ITensorNetworks.linsolve as named for the Laplace solve
@@ -436,9 +438,11 @@ typedef struct {
   int32_t restarts;     /* Lanczos restarts per two-site update                   */
 } tnfa_dmrg_params;
 
-/* Lowest eigenpair of a symmetric operator H on a path-shaped tree by two-site
- * DMRG sweeps: the two-site operator is assembled densely on the device,
- * Lanczos (full re-orthogonalisation, restarts) finds its lowest eigenvector,
+/* Lowest eigenpair of a symmetric operator H on a tree with one site leg per
+ * vertex by two-site DMRG updates (a path by alternating sweeps, any other
+ * tree by a depth-first tour): the two-site operator is applied densely on the
+ * device or matrix-free for large systems, Lanczos (full
+ * re-orthogonalisation, restarts) finds its lowest eigenvector,
  * a truncated SVD splits it, and the state is kept normalised.  Replaces
  * ITensorNetworks.dmrg as called by examples/2d_laplace_solver.jl:33-34
  * (nsites = 2, normalize = true).  energy receives the final eigenvalue. */
