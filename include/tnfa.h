@@ -46,7 +46,7 @@ typedef enum {
   TNFA_ERR_NOT_CONVERGED = 7,    /* iterative factorisation / solver hit its cap  */
   TNFA_ERR_TIMEOUT = 8,          /* a device-side wait ran out of its budget      */
   TNFA_ERR_DOMAIN = 9,           /* a coordinate is negative or not finite        */
-  TNFA_ERR_UNSUPPORTED = 10      /* valid request this build does not implement   */
+  TNFA_ERR_UNSUPPORTED = 10      /* valid request the library does not implement  */
 } tnfa_status;
 
 typedef enum { TNFA_F64 = 0, TNFA_F32 = 1, TNFA_C128 = 2 } tnfa_dtype;
