@@ -455,3 +455,17 @@ def test_partial_integrate_3d():  # test/test_integration.jl:40-54 (src/integrat
         ts.append(t)
     val = O.contract(ts).scalar()
     assert abs(val - (np.e - 1) * np.sin(1) * np.exp(x)) <= 1e-8
+
+
+def test_multi_dimensional_complex_example():  # examples/construct_multi_dimensional_function.jl
+    """z1^3 (z2 + z2^2) + cosh(pi z3)^2 on a 3 x 4 comb, each variable's real
+    digits on one tooth and its imaginary digits on another, reversed."""
+    L = 4
+    real_dv = [[(j, i) for i in range(1, L + 1)] for j in range(1, 4)]
+    imag_dv = [[(j, i) for i in range(L, 0, -1)] for j in range(3, 0, -1)]
+    s = O.complex_siteinds(O.comb_tree_graph((3, L)), real_dv, imag_dv)
+    f = O.net_add(O.net_multiply(O.poly_itn(s, [0.0, 0.0, 0.0, 1.0], dim=1), O.poly_itn(s, [0.0, 1.0, 1.0], dim=2)),
+                  O.net_multiply(O.cosh_itn(s, k=np.pi, dim=3), O.cosh_itn(s, k=np.pi, dim=3)))
+    z1, z2, z3 = 0.125 + 0.5j, 0.625 + 0.875j, 0.5
+    exact = z1**3 * (z2 + z2**2) + np.cosh(np.pi * z3) ** 2
+    assert approx(O.evaluate(f, [z1, z2, z3], [1, 2, 3]), exact)
