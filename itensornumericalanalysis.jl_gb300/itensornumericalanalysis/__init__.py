@@ -59,7 +59,10 @@ from .graphs import (
     uniform_tree,
 )
 from .indexmap import (
+    AbstractIndexMap,
+    ComplexIndexMap,
     IndsNetworkMap,
+    RealIndexMap,
     SiteLeg,
     calculate_ind_values,
     calculate_p,

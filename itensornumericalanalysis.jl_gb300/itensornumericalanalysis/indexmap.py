@@ -525,12 +525,26 @@ def indsnetwork(x):
     return m.graph, {v: list(m.legs[v]) for v in m.vertices()}
 
 
-def indexmap(x) -> dict:
+class AbstractIndexMap(dict):
+    """An index map: site leg -> (variable, digit) (src/IndexMaps/abstractindexmap.jl)."""
+
+
+class RealIndexMap(AbstractIndexMap):
+    """The index map of real variables (src/IndexMaps/realindexmap.jl:6-9)."""
+
+
+class ComplexIndexMap(AbstractIndexMap):
+    """The index map of complex variables, real and imaginary digit legs
+    (src/IndexMaps/complexindexmap.jl)."""
+
+
+def indexmap(x) -> AbstractIndexMap:
     """The index map (indsnetworkmap.jl:16): leg -> (variable, digit)."""
     m = _map(x)
-    return {l: (l.dim, l.digit) for v in m.vertices() for l in m.legs[v]}
+    cls = ComplexIndexMap if m.is_complex else RealIndexMap
+    return cls({l: (l.dim, l.digit) for v in m.vertices() for l in m.legs[v]})
 
 
-def indexmaptype(x) -> str:
-    """'complex' for a ComplexIndexMap, else 'real' (indsnetworkmap.jl:20)."""
-    return "complex" if _map(x).is_complex else "real"
+def indexmaptype(x) -> type:
+    """RealIndexMap or ComplexIndexMap (indsnetworkmap.jl:20)."""
+    return ComplexIndexMap if _map(x).is_complex else RealIndexMap

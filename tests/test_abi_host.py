@@ -181,8 +181,10 @@ def test_reference_named_free_functions():
     assert graph is s.graph and set(legs) == set(s.vertices())
     im = ina.indexmap(s)
     assert sorted(im.values()) == sorted((d, k) for d in (1, 2) for k in range(1, L + 1))
-    assert ina.indexmaptype(s) == "real"
-    assert ina.indexmaptype(ina.complex_continuous_siteinds(ina.named_path_graph(4))) == "complex"
+    assert isinstance(im, ina.RealIndexMap) and isinstance(im, ina.AbstractIndexMap)
+    assert ina.indexmaptype(s) is ina.RealIndexMap
+    sc = ina.complex_continuous_siteinds(ina.named_path_graph(4))
+    assert ina.indexmaptype(sc) is ina.ComplexIndexMap and isinstance(ina.indexmap(sc), ina.ComplexIndexMap)
 
 
 @pytest.mark.parametrize("boundary", ["Dirichlet", "Periodic", "Neumann"])
