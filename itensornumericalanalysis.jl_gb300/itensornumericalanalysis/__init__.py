@@ -82,8 +82,15 @@ from .indexmap import (
     real_continuous_siteinds,
     reduced_indsnetworkmap,
     tree_groups,
+    base,
+    digit,
+    index_value_to_scalar,
+    indsnetworkmap,
+    vertex,
     vertex_digit,
+    vertex_digits,
     vertex_dimension,
+    vertex_dimensions,
     vertices_digits,
     vertices_dimensions,
 )

@@ -509,6 +509,45 @@ def vertices_digits(x, verts) -> list[int]:
     return _map(x).vertices_digits(verts)
 
 
+def vertex_dimensions(x, v) -> list[int]:
+    """The variables of every leg of v (indsnetworkmap.jl:127-129)."""
+    return [l.dim for l in _map(x).legs[v]]
+
+
+def vertex_digits(x, v) -> list[int]:
+    """The digits of every leg of v (indsnetworkmap.jl:131-133)."""
+    return [l.digit for l in _map(x).legs[v]]
+
+
+def vertex(x, dim: int, digit: int):
+    """The vertex holding the real leg of (dim, digit) (indsnetworkmap.jl:147-150)."""
+    (v,) = [v for v, ls in _map(x).legs.items() for l in ls
+            if l.dim == dim and l.digit == digit and l.kind == REAL]
+    return v
+
+
+def digit(x, leg: SiteLeg) -> int:
+    """The digit of a leg (abstractindexmap.jl:76)."""
+    return leg.digit
+
+
+def base(x) -> int:
+    """The base of the map's digits (indsnetworkmap.jl:113)."""
+    legs = _map(x).inds()
+    return legs[0].base if legs else 2
+
+
+def index_value_to_scalar(x, leg: SiteLeg, value: int):
+    """The contribution of one digit value to its coordinate (realindexmap.jl:13-15,
+    complexindexmap.jl:25-32)."""
+    return leg.value_to_scalar(value)
+
+
+def indsnetworkmap(f) -> IndsNetworkMap:
+    """The map of a function (itensornetworkfunction.jl:25)."""
+    return _map(f)
+
+
 def calculate_ind_values(x, xs, dims=None) -> dict:
     """Digits of a point: leg -> value (abstractindexmap.jl:121-160)."""
     return _map(x).calculate_ind_values(xs, dims)

@@ -167,7 +167,12 @@ def test_reference_named_free_functions():
     assert sorted(ina.dimension_vertices(s, 2)) == sorted((2, j) for j in range(1, L + 1))
     for v in s.vertices():
         d, k = ina.vertex_dimension(s, v), ina.vertex_digit(s, v)
-        assert s.vertex(d, k) == v
+        assert s.vertex(d, k) == v and ina.vertex(s, d, k) == v
+        assert ina.vertex_dimensions(s, v) == [d] and ina.vertex_digits(s, v) == [k]
+        (leg,) = s.inds(v)
+        assert ina.digit(s, leg) == k and ina.index_value_to_scalar(s, leg, 1) == 2.0**-k
+    assert ina.base(s) == 2 and ina.base(ina.continuous_siteinds(g, base=3)) == 3
+    assert ina.indsnetworkmap(s) is s
     vs = s.vertices()
     assert ina.vertices_dimensions(s, vs) == [ina.vertex_dimension(s, v) for v in vs]
     assert ina.vertices_digits(s, vs) == [ina.vertex_digit(s, v) for v in vs]
