@@ -61,12 +61,15 @@ from .graphs import (
 from .indexmap import (
     AbstractIndexMap,
     ComplexIndexMap,
+    ComplexIndsNetworkMap,
     IndsNetworkMap,
     RealIndexMap,
+    RealIndsNetworkMap,
     SiteLeg,
     calculate_ind_values,
     calculate_p,
     complex_continuous_siteinds,
+    complex_digit_siteinds,
     continuous_siteinds,
     default_dimension_vertices,
     digit_siteinds,

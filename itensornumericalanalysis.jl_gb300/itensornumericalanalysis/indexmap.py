@@ -440,7 +440,15 @@ def complex_continuous_siteinds(
     base: int = 2,
     map_dimension: int = 1,
 ) -> IndsNetworkMap:
-    """ComplexIndsNetworkMap (src/indsnetworkmap.jl:66-81; legs src/digit_inds.jl:88-115)."""
+    """ComplexIndsNetworkMap (src/indsnetworkmap.jl:66-81)."""
+    legs = complex_digit_siteinds(g, real_dimension_vertices, imag_dimension_vertices, base, map_dimension)
+    return IndsNetworkMap(g, legs, True)
+
+
+def complex_digit_siteinds(g: NamedGraph, real_dimension_vertices=None, imag_dimension_vertices=None,
+                           base: int = 2, map_dimension: int = 1):
+    """Legs of a complex map: every vertex's real digit legs, then its
+    imaginary ones (src/digit_inds.jl:88-115)."""
     if not real_dimension_vertices or not real_dimension_vertices[0]:
         real_dimension_vertices = default_dimension_vertices(g, map_dimension)
     if not imag_dimension_vertices or not imag_dimension_vertices[0]:
@@ -452,7 +460,11 @@ def complex_continuous_siteinds(
     for d, verts in enumerate(imag_dimension_vertices, start=1):
         for k, v in enumerate(verts, start=1):
             legs[v].append(SiteLeg(v, d, k, base, IMAG))
-    return IndsNetworkMap(g, legs, True)
+    return legs
+
+
+RealIndsNetworkMap = continuous_siteinds
+ComplexIndsNetworkMap = complex_continuous_siteinds
 
 
 def reduced_indsnetworkmap(s: IndsNetworkMap, dims) -> IndsNetworkMap:

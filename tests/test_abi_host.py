@@ -173,6 +173,11 @@ def test_reference_named_free_functions():
         assert ina.digit(s, leg) == k and ina.index_value_to_scalar(s, leg, 1) == 2.0**-k
     assert ina.base(s) == 2 and ina.base(ina.continuous_siteinds(g, base=3)) == 3
     assert ina.indsnetworkmap(s) is s
+    sc = ina.ComplexIndsNetworkMap(g)
+    legs = ina.complex_digit_siteinds(g)
+    assert sc.is_complex and all(sc.inds(v) == legs[v] for v in g.vertices())
+    assert all([l.kind for l in legs[v]] == ["real", "imag"] or len(legs[v]) != 2 for v in g.vertices())
+    assert ina.RealIndsNetworkMap is ina.continuous_siteinds
     vs = s.vertices()
     assert ina.vertices_dimensions(s, vs) == [ina.vertex_dimension(s, v) for v in vs]
     assert ina.vertices_digits(s, vs) == [ina.vertex_digit(s, v) for v in vs]
