@@ -297,13 +297,20 @@ class IndsNetworkMap:
         return [sum(l.value_to_scalar(v) for l, v in ind_values.items() if l.dim == d) for d in dims]
 
     def grid_points(self, N: int, d: int) -> list:
-        """N uniform grid points of dimension d (src/IndexMaps/realindexmap.jl:78-86)."""
-        legs = [l for l in self.inds() if l.dim == d and l.kind == REAL]
-        base = float(legs[0].base)
-        L = len(legs)
+        """N uniform grid points of dimension d (src/IndexMaps/realindexmap.jl:78-86);
+        for a complex map the N x N points of the real and imaginary grids
+        (src/IndexMaps/complexindexmap.jl:134-144)."""
+        re = [l for l in self.inds() if l.dim == d and l.kind == REAL]
+        base = float(re[0].base)
+        L = len(re)
         a = round(base**L / N)
-        pts = [i * (a / base**L) for i in range(N + 2)]
-        return [x for x in pts if x < 1]
+        if not self.is_complex:
+            pts = [i * (a / base**L) for i in range(N + 2)]
+            return [x for x in pts if x < 1]
+        Li = sum(1 for l in self.inds() if l.dim == d and l.kind == IMAG)
+        ai = round(base**Li / N)
+        pts = [i * (a / base**L) + 1j * j * (ai / base**Li) for i in range(N + 2) for j in range(N + 2)]
+        return [z for z in pts if z.real < 1 and z.imag < 1]
 
     # -- derived maps -------------------------------------------------------
     def reduced(self, dims) -> "IndsNetworkMap":
@@ -471,7 +478,16 @@ def reduced_indsnetworkmap(s: IndsNetworkMap, dims) -> IndsNetworkMap:
     return s.reduced(dims)
 
 
-def grid_points(s: IndsNetworkMap, N: int, d: int) -> list:
+def grid_points(s: IndsNetworkMap, *args) -> list:
+    """grid_points(s, N, d): N uniform points of variable d; grid_points(s, d):
+    N = base^L with L the number of digit legs of d, i.e. every grid point of
+    a real variable (src/IndexMaps/abstractindexmap.jl:149-155)."""
+    s = _map(s)
+    if len(args) == 1:
+        (d,) = args
+        legs = [l for l in s.inds() if l.dim == d]
+        return s.grid_points(legs[0].base ** len(legs), d)
+    N, d = args
     return s.grid_points(N, d)
 
 

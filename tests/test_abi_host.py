@@ -111,6 +111,13 @@ def test_grid_points():
     pts = s.grid_points(16, 1)
     assert pts[0] == 0.0 and all(p < 1 for p in pts)
     assert np.allclose(np.diff(pts), 1 / 16)
+    assert ina.grid_points(s, 1) == [i / 256 for i in range(256)]  # every point (abstractindexmap.jl:149-155)
+    assert ina.grid_points(s, 16, 1) == pts
+    # complex map: the N x N products of the real and imaginary grids (complexindexmap.jl:134-144)
+    sc = ina.complex_continuous_siteinds(ina.named_grid((8, 1)), [[(i, 1) for i in range(1, 5)]],
+                                         [[(i, 1) for i in range(5, 9)]])
+    zs = ina.grid_points(sc, 4, 1)
+    assert len(zs) == 16 and set(zs) == {i / 4 + 1j * j / 4 for i in range(4) for j in range(4)}
 
 
 def test_reduced_maps():
