@@ -353,3 +353,23 @@ def test_library_stencil_terms_reject_bad_input():
                                    C.byref(nt), C.byref(nf)) == _lib.ERR_INVALID_ARGUMENT
     assert L.tnfa_op_stencil_terms(C.byref(t), 1, w, 7, 0, 0, 0, None, None, None, None,
                                    C.byref(nt), C.byref(nf)) == _lib.ERR_INVALID_ARGUMENT
+
+
+def test_complex_map_legs_match_oracle():
+    """The product's complex maps carry, vertex by vertex, the same (variable,
+    digit, real/imaginary) legs in the same order as the oracle's
+    complex_siteinds (src/digit_inds.jl:88-115), for default and explicit
+    vertex lists."""
+    import itensornumericalanalysis as ina
+
+    cases = [(ina.named_comb_tree((2, 3)), O.comb_tree_graph((2, 3)), None, None, 1),
+             (ina.named_comb_tree((2, 3)), O.comb_tree_graph((2, 3)), [[(1, 1), (1, 2), (1, 3)]],
+              [[(2, 1), (2, 2), (2, 3)]], 1),
+             (ina.named_grid((3, 2)), O.grid_graph((3, 2)), None, None, 2)]
+    for g, og, rdv, idv, md in cases:
+        s = ina.complex_continuous_siteinds(g, rdv, idv, map_dimension=md)
+        so = O.complex_siteinds(og, rdv, idv, map_dimension=md)
+        for v in g.vertices():
+            mine = [(l.dim, l.digit, l.kind == "real") for l in s.inds(v)]
+            theirs = [so.info[i] for i in so.site[v]]
+            assert mine == theirs, (v, mine, theirs)
