@@ -1,0 +1,33 @@
+"""bench.py's host-side arithmetic (no device): the roofline object of the
+dominant kernel family, from the library's per-family CUDA-event stats."""
+import sys
+from pathlib import Path
+
+import pytest
+
+sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
+import bench  # noqa: E402
+
+
+PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 2000.0, "bf16_tflops_sustained": 1700.0}
+
+
+def test_roofline_of_the_sliced_kernel():
+    pts = 131072
+    fl = 2.0 * bench.CHI**3 * pts * 28  # 28 two-child vertices, one launch each
+    stats = {"contract_oz": {"launches": 28, "ms": 10.0, "flops": fl, "bytes": 0.0},
+             "digitize": {"launches": 1, "ms": 0.5, "flops": 0.0, "bytes": 0.0}}
+    r = bench.roofline(stats, "contract_oz", PEAKS)
+    assert r["achieved"] == pytest.approx(fl / 1e-2 / 1e12)
+    assert r["frac"] == pytest.approx(r["achieved"] / 1700.0)
+    assert r["frac_of_burst_peak"] == pytest.approx(r["achieved"] / 2000.0)
+    assert r["mma_passes"] == bench.MMA_PASSES["contract_oz"] == 26
+    assert r["frac_executed"] == pytest.approx(26 * r["frac"])
+    # DRAM traffic per launch: the captured bytes per point times the points one launch covers
+    assert r["traffic"] == pytest.approx(bench.OZ_DRAM_BYTES_PER_POINT * pts)
+    assert r["kernel_share"] == pytest.approx(10.0 / 10.5)
+    assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
+
+
+def test_roofline_without_a_family():
+    assert bench.roofline({}, None, PEAKS) is None
