@@ -31,3 +31,29 @@ def test_roofline_of_the_sliced_kernel():
 
 def test_roofline_without_a_family():
     assert bench.roofline({}, None, PEAKS) is None
+
+
+class _Proc:
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+
+def test_clock_sampler_parses_nvidia_smi_lines():
+    """The clocks object of the JSON line: median SM clock under load, the
+    maximum, and every throttle reason seen Active."""
+    c = bench.ClockSampler(0)
+    c.proc = _Proc()
+    c.lines = ["1965, 2070, 900.5, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+               "2070, 2070, 1000.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+               "2010, 2070, 950.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+               "garbage line"]
+    r = c.stop()
+    assert r["sm_mhz"] == 2010.0 and r["sm_max_mhz"] == 2070.0 and r["samples"] == 3
+    assert r["reasons"] == ["sw_power_cap"]
+
+
+def test_clock_sampler_without_nvidia_smi():
+    assert bench.ClockSampler(0).stop()["reasons"] == ["nvidia-smi unavailable"]
