@@ -57,3 +57,33 @@ def test_clock_sampler_parses_nvidia_smi_lines():
 
 def test_clock_sampler_without_nvidia_smi():
     assert bench.ClockSampler(0).stop()["reasons"] == ["nvidia-smi unavailable"]
+
+
+def test_uneven_mps_batch_follows_the_config():
+    """512 MPS, L in 10..30, chi in 8..128 capped per bond at min(chi, 2^k,
+    2^(L-k)), unit-Frobenius Gaussian tensors, the same batch for the same seed."""
+    import numpy as np
+
+    from itensornumericalanalysis.workloads import uneven_mps_batch
+
+    batch = uneven_mps_batch(n=512, seed=3)
+    again = uneven_mps_batch(n=4, seed=3)
+    assert len(batch) == 512
+    Ls, chis = [], []
+    for (s, ts) in batch:
+        order = s.layout.order
+        L = len(order)
+        Ls.append(L)
+        assert 10 <= L <= 30
+        bonds = [np.shape(ts[v])[2] for v in order[:-1]]
+        chi = max(bonds)
+        chis.append(chi)
+        # chi is the largest bond: either the drawn chi or, when every bond is
+        # capped, the largest cap; either way every bond is min(chi, caps)
+        assert bonds == [min(chi, 2**k, 2 ** (L - k)) for k in range(1, L)]
+        for v in order:
+            assert abs(np.linalg.norm(ts[v]) - 1.0) < 1e-12
+    assert min(Ls) == 10 and max(Ls) == 30
+    assert 8 <= min(chis) and max(chis) <= 128 and max(chis) >= 100
+    for (s, ts), (s2, ts2) in zip(batch[:4], again):
+        assert all(np.array_equal(ts[v], ts2[w]) for v, w in zip(s.layout.order, s2.layout.order))
