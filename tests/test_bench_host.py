@@ -87,3 +87,21 @@ def test_uneven_mps_batch_follows_the_config():
     assert 8 <= min(chis) and max(chis) <= 128 and max(chis) >= 100
     for (s, ts), (s2, ts2) in zip(batch[:4], again):
         assert all(np.array_equal(ts[v], ts2[w]) for v, w in zip(s.layout.order, s2.layout.order))
+
+
+def test_config3_workload_shapes():
+    """60-vertex heap binary tree, 3 variables x 20 digits, chi = 128: 29
+    vertices with two children (the root among them), one with one child, 30
+    leaves; FP32 tensors of unit Frobenius norm; 470 MB in all."""
+    import numpy as np
+
+    s, ts = bench.config3_tensors(1)
+    lay = s.layout
+    nch = [len(c) for c in lay.children]
+    assert len(lay.order) == 60 and nch.count(0) == 30 and nch.count(2) == 29 and nch.count(1) == 1
+    assert sorted(s.ndigits(d) for d in (1, 2, 3)) == [20, 20, 20]
+    nbytes = sum(t.nbytes for t in ts.values())
+    assert abs(nbytes / 1e6 - 470) < 10
+    assert all(t.dtype == np.float32 and abs(float(np.linalg.norm(t)) - 1) < 1e-5 for t in ts.values())
+    X = bench.config3_points(1000, 1)
+    assert X.shape == (1000, 3) and X.min() >= 0 and X.max() < 1
